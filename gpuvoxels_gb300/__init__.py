@@ -1,0 +1,312 @@
+"""gpuvoxels_gb300: GB300-native Voxelyze3 soft-body step engine.
+
+Python mirror of the reference's simulation interface over the C ABI
+(include/gpuvoxels_gb300.h):
+
+* ``SimulationManager`` mirrors ``VX3_SimulationManager`` (Voxelyze3/src/VX3/
+  VX3_SimulationManager.cuh:15-46): a base VXA plus VXD files in, ``start()``
+  runs them all and fills ``h_results`` sorted by fitness (NaN last).
+* ``Context`` exposes every entry point: load, step/run (plain or batched),
+  the serving pair submit/poll, state readout, the report writer.
+
+The compute path is the CUDA library built by ``gpuvoxels_gb300.build``; there
+is no CPU fallback.  Loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Iterable, List, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+PLAIN, BATCHED = 0, 1
+SIM_IDLE, SIM_RUNNING, SIM_DONE, SIM_DIVERGED, SIM_ERROR = range(5)
+ERRORS = {-1: "VX3_E_PARSE", -2: "VX3_E_OOM_BUDGET", -3: "VX3_E_DIVERGED", -4: "VX3_E_TIMEOUT", -5: "VX3_E_CUDA",
+          -6: "VX3_E_ARG", -7: "VX3_E_STATE"}
+
+# Every symbol include/gpuvoxels_gb300.h declares.
+EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_set_external", "vx3_run", "vx3_step",
+           "vx3_submit", "vx3_poll", "vx3_pending", "vx3_get_result", "vx3_sim_info_get", "vx3_get_state",
+           "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
+           "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_sim_bytes", "vx3_bytes_in_use",
+           "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula"]
+
+
+class VX3Error(RuntimeError):
+    pass
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("status", ctypes.c_int32), ("num_voxel", ctypes.c_int32),
+                ("num_measured_voxel", ctypes.c_int32), ("num_close_pairs", ctypes.c_int32), ("steps", ctypes.c_int64),
+                ("current_time", ctypes.c_double), ("fitness_score", ctypes.c_double), ("vox_size", ctypes.c_double),
+                ("initial_center_of_mass", ctypes.c_double * 3), ("current_center_of_mass", ctypes.c_double * 3),
+                ("total_distance_of_all_voxels", ctypes.c_double), ("submit_time_s", ctypes.c_double),
+                ("start_time_s", ctypes.c_double), ("finish_time_s", ctypes.c_double)]
+
+
+class SimInfo(ctypes.Structure):
+    _fields_ = [("num_voxel", ctypes.c_int32), ("num_link", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("dt", ctypes.c_double), ("current_time", ctypes.c_double),
+                ("steps", ctypes.c_int64)]
+
+
+_LIB = None
+
+
+def library(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Loads (building first if needed) the in-tree CUDA library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if build_if_missing and (not os.path.exists(path) or _build.needs_build()):
+        _build.build()
+    if not os.path.exists(path):
+        raise VX3Error(f"CUDA engine library not built: {path}")
+    L = ctypes.CDLL(path)
+    P, I, I64, D, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_char_p
+    sig = {
+        "vx3_create": (P, [I, ctypes.c_size_t]), "vx3_destroy": (None, [P]), "vx3_last_error": (S, [P]),
+        "vx3_load_vxa": (I, [P, S, S, S, ctypes.POINTER(I64)]),
+        "vx3_set_external": (I, [P, I64, I, I, P, P, P, P]),
+        "vx3_run": (I, [P, P, I, I, I64]), "vx3_step": (I, [P, P, I, I, I64]),
+        "vx3_submit": (I, [P, I64, I64]), "vx3_poll": (I, [P, P, I, I]), "vx3_pending": (I, [P]),
+        "vx3_get_result": (I, [P, I64, ctypes.POINTER(Result)]), "vx3_sim_info_get": (I, [P, I64, ctypes.POINTER(SimInfo)]),
+        "vx3_get_state": (I, [P, I64, P, P, P]), "vx3_get_voxel_state": (I, [P, I64, P, P, P]),
+        "vx3_get_link_state": (I, [P, I64, P, P, P]), "vx3_write_report": (I, [P, P, I, S, S]),
+        "vx3_free_sim": (I, [P, I64]), "vx3_last_timing": (I, [P, P]), "vx3_set_tuning": (I, [P, I, I, I, I, I]),
+        "vx3_autotune": (I, [P, P, I]), "vx3_set_profiling": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
+        "vx3_bytes_in_use": (ctypes.c_size_t, [P]),
+        "vx3_inspect_vxa": (I, [S, S, P, P, ctypes.c_char_p, I]),
+        "vx3_inspect_topology": (I, [S, S, P, P, P, P, P, P, P]),
+        "vx3_inspect_formula": (I, [S, S, I, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _b(s: Optional[str]):
+    return None if s is None else s.encode()
+
+
+def inspect_vxa(base_xml: str, vxd_xml: Optional[str] = None) -> dict:
+    """Host-only: what the engine would simulate for this VXA/VXD (no GPU needed)."""
+    L = library()
+    counts = np.zeros(6, np.int32)
+    env = np.zeros(12)
+    err = ctypes.create_string_buffer(512)
+    rc = L.vx3_inspect_vxa(_b(base_xml), _b(vxd_xml), _p(counts), _p(env), err, 512)
+    if rc:
+        raise VX3Error(f"{ERRORS.get(rc, rc)}: {err.value.decode()}")
+    nv, nl, nvm, nlm = (int(x) for x in counts[:4])
+    vox = np.zeros((nv, 4), np.int32); lnk = np.zeros((max(nl, 1), 4), np.int32); ph = np.zeros(nv)
+    vm = np.zeros((nvm, 18), np.float32); vnom = np.zeros(nvm); lidx = np.zeros((max(nlm, 1), 2), np.int32)
+    lm = np.zeros((max(nlm, 1), 20), np.float32)
+    L.vx3_inspect_topology(_b(base_xml), _b(vxd_xml), _p(vox), _p(lnk), _p(ph), _p(vm), _p(vnom), _p(lidx), _p(lm))
+    keys = ["vox_size", "dt_frac", "gravity_mult", "floor", "collisions", "vary_temp", "temp_amplitude", "temp_period",
+            "enable_expansion", "initial_temp", "bounding_radius", "watch_distance"]
+    return dict(counts=dict(voxels=nv, links=nl, voxel_materials=nvm, link_materials=nlm, surface=int(counts[4]),
+                            externals=int(counts[5])),
+                env=dict(zip(keys, env.tolist())), voxels=vox, links=lnk[:nl], phase=ph, voxmat=vm, nom=vnom,
+                linkmat_idx=lidx[:nlm], linkmat=lm[:nlm])
+
+
+def eval_formula(base_xml: str, which: str, vars9: Sequence[float], vxd_xml: Optional[str] = None) -> float:
+    L = library()
+    v = np.asarray(vars9, np.float64)
+    out = np.zeros(1)
+    rc = L.vx3_inspect_formula(_b(base_xml), _b(vxd_xml), 0 if which == "stop" else 1, _p(v), _p(out))
+    if rc:
+        raise VX3Error(ERRORS.get(rc, str(rc)))
+    return float(out[0])
+
+
+class Context:
+    """One device context: an HBM budget, a stream, and the simulations loaded into it."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.L = library()
+        self.h = self.L.vx3_create(device, hbm_budget_bytes)
+        if not self.h:
+            raise VX3Error("vx3_create failed (no CUDA device, or the budget could not be reserved)")
+        self.names = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.vx3_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc < 0:
+            raise VX3Error(f"{ERRORS.get(rc, rc)}: {self.L.vx3_last_error(self.h).decode()}")
+        return rc
+
+    def load_vxa(self, base_xml: str, vxd_xml: Optional[str] = None, name: str = "") -> int:
+        out = ctypes.c_int64()
+        self._check(self.L.vx3_load_vxa(self.h, _b(base_xml), _b(vxd_xml), name.encode(), ctypes.byref(out)))
+        self.names[out.value] = name
+        return out.value
+
+    def set_external(self, sim: int, voxel: int, dof_fixed: int = 0, force=(0, 0, 0), moment=(0, 0, 0),
+                     translate=(0, 0, 0), rotate=(0, 0, 0)):
+        f = np.asarray(force, np.float32); m = np.asarray(moment, np.float32)
+        t = np.asarray(translate, np.float64); r = np.asarray(rotate, np.float64)
+        self._check(self.L.vx3_set_external(self.h, sim, voxel, dof_fixed, _p(f), _p(m), _p(t), _p(r)))
+
+    def _ids(self, ids):
+        a = np.ascontiguousarray(np.atleast_1d(np.asarray(ids, np.int64)))
+        return a
+
+    def step(self, ids, steps: int, mode: int = BATCHED):
+        a = self._ids(ids)
+        self._check(self.L.vx3_step(self.h, _p(a), len(a), mode, steps))
+
+    def run(self, ids, mode: int = BATCHED, max_steps: int = 0):
+        a = self._ids(ids)
+        self._check(self.L.vx3_run(self.h, _p(a), len(a), mode, max_steps))
+
+    def submit(self, sim: int, horizon_steps: int):
+        self._check(self.L.vx3_submit(self.h, sim, horizon_steps))
+
+    def poll(self, chunk_steps: int = 64, max_results: int = 4096) -> List[Result]:
+        buf = (Result * max_results)()
+        n = self._check(self.L.vx3_poll(self.h, buf, max_results, chunk_steps))
+        return [buf[i] for i in range(n)]
+
+    def pending(self) -> int:
+        return self.L.vx3_pending(self.h)
+
+    def result(self, sim: int) -> Result:
+        r = Result()
+        self._check(self.L.vx3_get_result(self.h, sim, ctypes.byref(r)))
+        return r
+
+    def info(self, sim: int) -> SimInfo:
+        r = SimInfo()
+        self._check(self.L.vx3_sim_info_get(self.h, sim, ctypes.byref(r)))
+        return r
+
+    def voxel_state(self, sim: int) -> dict:
+        nv = self.info(sim).num_voxel
+        d = np.zeros((nv, 13)); f = np.zeros((nv, 4), np.float32); fl = np.zeros(nv, np.int32)
+        self._check(self.L.vx3_get_voxel_state(self.h, sim, _p(d), _p(f), _p(fl)))
+        return dict(pos=d[:, 0:3], linMom=d[:, 3:6], orient=d[:, 6:10], angMom=d[:, 10:13], temp=f[:, 0],
+                    pStrain=f[:, 1:4], flags=fl)
+
+    def link_state(self, sim: int) -> dict:
+        nl = self.info(sim).num_link
+        d = np.zeros((nl, 9)); f = np.zeros((nl, 3), np.float32); fl = np.zeros(nl, np.int32)
+        self._check(self.L.vx3_get_link_state(self.h, sim, _p(d), _p(f), _p(fl)))
+        return dict(pos2=d[:, 0:3], angle1v=d[:, 3:6], angle2v=d[:, 6:9], strain=f[:, 0], maxStrain=f[:, 1],
+                    strainOffset=f[:, 2], smallAngle=fl & 1, flags=fl)
+
+    def get_state(self, sim: int):
+        nv = self.info(sim).num_voxel
+        pos = np.zeros((nv, 3)); q = np.zeros((nv, 4)); fl = np.zeros(nv, np.uint8)
+        self._check(self.L.vx3_get_state(self.h, sim, _p(pos), _p(q), _p(fl)))
+        return pos, q, fl
+
+    def write_report(self, ids, path: str, input_dir: str = ""):
+        a = self._ids(ids)
+        self._check(self.L.vx3_write_report(self.h, _p(a), len(a), input_dir.encode(), path.encode()))
+
+    def free(self, sim: int):
+        self._check(self.L.vx3_free_sim(self.h, sim))
+
+    def timing(self) -> dict:
+        o = np.zeros(7)
+        self.L.vx3_last_timing(self.h, _p(o))
+        return dict(device_ms=o[0], wall_ms=o[1], voxel_steps=int(o[2]), launches=int(o[3]), link_ms=o[4],
+                    contact_ms=o[5], voxel_ms=o[6])
+
+    def set_tuning(self, block_links=0, block_voxels=0, items_links=0, items_voxels=0, graph_steps=0):
+        self.L.vx3_set_tuning(self.h, block_links, block_voxels, items_links, items_voxels, graph_steps)
+
+    def autotune(self, ids):
+        a = self._ids(ids)
+        self._check(self.L.vx3_autotune(self.h, _p(a), len(a)))
+
+    def set_profiling(self, on: bool):
+        self.L.vx3_set_profiling(self.h, int(on))
+
+    def bytes_in_use(self) -> int:
+        return int(self.L.vx3_bytes_in_use(self.h))
+
+
+@dataclass
+class SimulationResult:
+    """VX3_SimulationResult (Voxelyze3/src/VX3/VX3_SimulationResult.h:4-33)."""
+    vxa_filename: str
+    fitness_score: float
+    currentTime: float
+    num_voxel: int
+    num_measured_voxel: int
+    voxSize: float
+    numClosePairs: int
+    initialCenterOfMass: tuple
+    currentCenterOfMass: tuple
+    total_distance_of_all_voxels: float
+    status: int
+
+
+class SimulationManager:
+    """Mirror of VX3_SimulationManager(sub_batches, base, input_dir, nDevices).start()
+    (Voxelyze3/src/VX3/VX3_SimulationManager.cu:123-155, 416-460) on one GB300."""
+
+    def __init__(self, sub_batches: Sequence[Sequence[str]], base: str, input_dir: str, num_of_devices: int = 1,
+                 mode: int = BATCHED, hbm_budget_bytes: int = 0):
+        self.files = [f for batch in sub_batches for f in batch]
+        self.base = base
+        self.input_dir = input_dir
+        self.mode = mode
+        self.budget = hbm_budget_bytes
+        self.h_results: List[SimulationResult] = []
+        self.ctx: Optional[Context] = None
+        self.ids: List[int] = []
+
+    def start(self):
+        base_xml = open(self.base).read()
+        self.ctx = Context(0, self.budget)
+        for f in self.files:
+            vxd = open(os.path.join(self.input_dir, f)).read()
+            self.ids.append(self.ctx.load_vxa(base_xml, vxd, os.path.basename(f)))
+        self.ctx.run(self.ids, self.mode)
+        res = []
+        for f, i in zip(self.files, self.ids):
+            r = self.ctx.result(i)
+            res.append(SimulationResult(os.path.basename(f), r.fitness_score, r.current_time, r.num_voxel,
+                                        r.num_measured_voxel, r.vox_size, r.num_close_pairs,
+                                        tuple(r.initial_center_of_mass), tuple(r.current_center_of_mass),
+                                        r.total_distance_of_all_voxels, r.status))
+        nan = [r for r in res if r.fitness_score != r.fitness_score]
+        ok = sorted([r for r in res if r.fitness_score == r.fitness_score], key=lambda r: -r.fitness_score)
+        self.h_results = ok + nan
+        return self.h_results
+
+    def write_report(self, path: str):
+        self.ctx.write_report(self.ids, path, self.input_dir)

@@ -1,0 +1,353 @@
+// C ABI over the engine (declarations and reference citations in include/gpuvoxels_gb300.h).
+#include "../../include/gpuvoxels_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "world.h"
+
+struct vx3_ctx {
+    gvx::Engine* eng = nullptr;
+    std::string err;
+    std::map<int64_t, std::string> names;
+};
+
+namespace {
+int fail(vx3_ctx* c, int code, const std::string& m) {
+    if (c) c->err = m;
+    return code;
+}
+void to_c(const gvx::SimResult& r, vx3_result* o) {
+    o->id = r.id;
+    o->status = r.status;
+    o->num_voxel = r.num_voxel;
+    o->num_measured_voxel = r.num_measured_voxel;
+    o->num_close_pairs = r.num_close_pairs;
+    o->steps = r.steps;
+    o->current_time = r.current_time;
+    o->fitness_score = r.fitness;
+    o->vox_size = r.vox_size;
+    for (int k = 0; k < 3; k++) { o->initial_center_of_mass[k] = r.initial_com[k]; o->current_center_of_mass[k] = r.current_com[k]; }
+    o->total_distance_of_all_voxels = r.total_distance;
+    o->submit_time_s = r.submit_s;
+    o->start_time_s = r.start_s;
+    o->finish_time_s = r.finish_s;
+}
+std::string num(double v) {
+    char b[64];
+    snprintf(b, sizeof(b), "%.17g", v);
+    return b;
+}
+}  // namespace
+
+extern "C" {
+
+vx3_ctx* vx3_create(int device, size_t budget) {
+    std::string err;
+    gvx::Engine* e = gvx::engine_create(device, budget, &err);
+    if (!e) {
+        fprintf(stderr, "vx3_create: %s\n", err.c_str());
+        return nullptr;
+    }
+    vx3_ctx* c = new vx3_ctx();
+    c->eng = e;
+    return c;
+}
+
+void vx3_destroy(vx3_ctx* c) {
+    if (!c) return;
+    gvx::engine_destroy(c->eng);
+    delete c;
+}
+
+const char* vx3_last_error(vx3_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int vx3_load_vxa(vx3_ctx* c, const char* base, const char* vxd, const char* name, vx3_sim_id* out) {
+    if (!c || !base || !out) return fail(c, VX3_E_ARG, "null argument");
+    gvx::SimDesc d;
+    std::string err;
+    if (!gvx::parse_vxa(base, vxd, &d, &err)) return fail(c, VX3_E_PARSE, err);
+    d.name = name ? name : "";
+    int64_t id;
+    if (c->eng->add_sim(d, &id, &err)) return fail(c, VX3_E_PARSE, err);
+    c->names[id] = d.name;
+    *out = id;
+    return VX3_OK;
+}
+
+int vx3_set_external(vx3_ctx* c, vx3_sim_id id, int voxel, int dof, const float force[3], const float moment[3],
+                     const double translate[3], const double rotate[3]) {
+    if (!c) return VX3_E_ARG;
+    gvx::External x;
+    x.voxel = voxel;
+    x.dof_fixed = dof;
+    for (int k = 0; k < 3; k++) {
+        x.force[k] = force ? force[k] : 0.0f;
+        x.moment[k] = moment ? moment[k] : 0.0f;
+        x.translate[k] = translate ? translate[k] : 0.0;
+        x.rotate[k] = rotate ? rotate[k] : 0.0;
+    }
+    std::string err;
+    int e = c->eng->set_external(id, x, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_run(vx3_ctx* c, const vx3_sim_id* ids, int n, int mode, int64_t max_steps) {
+    if (!c || (!ids && n > 0) || n < 0) return fail(c, VX3_E_ARG, "bad arguments");
+    std::string err;
+    int e = c->eng->run(ids, n, mode, max_steps, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_step(vx3_ctx* c, const vx3_sim_id* ids, int n, int mode, int64_t steps) {
+    if (!c || (!ids && n > 0) || n < 0 || steps < 0) return fail(c, VX3_E_ARG, "bad arguments");
+    std::string err;
+    int e = c->eng->step(ids, n, mode, steps, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_submit(vx3_ctx* c, vx3_sim_id id, int64_t horizon) {
+    if (!c) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->submit(id, horizon, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_poll(vx3_ctx* c, vx3_result* out, int max, int chunk) {
+    if (!c || (max > 0 && !out)) return VX3_E_ARG;
+    std::vector<gvx::SimResult> rs((size_t)std::max(1, max));
+    std::string err;
+    int n = c->eng->poll(rs.data(), max, chunk, &err);
+    if (n < 0) return fail(c, n, err);
+    for (int i = 0; i < n; i++) to_c(rs[i], &out[i]);
+    return n;
+}
+
+int vx3_pending(vx3_ctx* c) { return c ? c->eng->pending() : VX3_E_ARG; }
+
+int vx3_get_result(vx3_ctx* c, vx3_sim_id id, vx3_result* out) {
+    if (!c || !out) return VX3_E_ARG;
+    gvx::SimResult r;
+    std::string err;
+    int e = c->eng->result(id, &r, &err);
+    if (e) return fail(c, e, err);
+    to_c(r, out);
+    return VX3_OK;
+}
+
+int vx3_sim_info_get(vx3_ctx* c, vx3_sim_id id, vx3_sim_info* out) {
+    if (!c || !out) return VX3_E_ARG;
+    int nv, nl, st;
+    double dt, t;
+    int64_t steps;
+    int e = c->eng->info(id, &nv, &nl, &dt, &t, &steps, &st);
+    if (e) return fail(c, e, "unknown simulation id");
+    out->num_voxel = nv;
+    out->num_link = nl;
+    out->status = st;
+    out->pad = 0;
+    out->dt = dt;
+    out->current_time = t;
+    out->steps = steps;
+    return VX3_OK;
+}
+
+int vx3_get_state(vx3_ctx* c, vx3_sim_id id, double* pos, double* orient, uint8_t* flags) {
+    if (!c) return VX3_E_ARG;
+    vx3_sim_info info;
+    if (int e = vx3_sim_info_get(c, id, &info)) return e;
+    std::vector<double> d13((size_t)info.num_voxel * 13);
+    std::vector<int32_t> fl((size_t)info.num_voxel);
+    std::string err;
+    int e = c->eng->voxel_state(id, d13.data(), nullptr, fl.data(), &err);
+    if (e) return fail(c, e, err);
+    for (int i = 0; i < info.num_voxel; i++) {
+        if (pos) for (int k = 0; k < 3; k++) pos[3 * (size_t)i + k] = d13[13 * (size_t)i + k];
+        if (orient) for (int k = 0; k < 4; k++) orient[4 * (size_t)i + k] = d13[13 * (size_t)i + 6 + k];
+        if (flags) flags[i] = (uint8_t)(fl[i] >> 6);
+    }
+    return VX3_OK;
+}
+
+int vx3_get_voxel_state(vx3_ctx* c, vx3_sim_id id, double* d13, float* f4, int32_t* flags) {
+    if (!c) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->voxel_state(id, d13, f4, flags, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_get_link_state(vx3_ctx* c, vx3_sim_id id, double* d9, float* f3, int32_t* flags) {
+    if (!c) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->link_state(id, d9, f3, flags, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_write_report(vx3_ctx* c, const vx3_sim_id* ids, int n, const char* input_dir, const char* path) {
+    if (!c || !path || (n > 0 && !ids)) return VX3_E_ARG;
+    std::vector<std::pair<vx3_result, std::string>> rs;
+    for (int i = 0; i < n; i++) {
+        vx3_result r;
+        if (int e = vx3_get_result(c, ids[i], &r)) return e;
+        rs.emplace_back(r, c->names[ids[i]]);
+    }
+    // VX3_SimulationResult::compareFitnessScore: diverged (NaN) last, then descending fitness
+    std::stable_sort(rs.begin(), rs.end(), [](const std::pair<vx3_result, std::string>& a, const std::pair<vx3_result, std::string>& b) {
+        if (std::isnan(b.first.fitness_score)) return !std::isnan(a.first.fitness_score);
+        if (std::isnan(a.first.fitness_score)) return false;
+        return a.first.fitness_score > b.first.fitness_score;
+    });
+    std::string dir = input_dir ? input_dir : "";
+    while (!dir.empty() && dir.back() == '/') dir.pop_back();
+    size_t slash = dir.rfind('/');
+    if (slash != std::string::npos) dir = dir.substr(slash + 1);
+    std::string o = "<?xml version=\"1.0\" encoding=\"utf-8\"?>\n<report><inputdir>" + gvx::xml_escape(dir) + "</inputdir>";
+    if (!rs.empty())
+        o += "<bestfit><filename>" + gvx::xml_escape(rs[0].second) + "</filename><fitness_score>" + num(rs[0].first.fitness_score) +
+             "</fitness_score></bestfit>";
+    o += "<detail>";
+    for (auto& p : rs) {
+        std::string nm = p.second.substr(0, p.second.find('.'));
+        if (nm.empty()) nm = "sim" + std::to_string(p.first.id);
+        const vx3_result& r = p.first;
+        o += "<" + nm + ">";
+        o += "<currentTime>" + num(r.current_time) + "</currentTime>";
+        o += "<fitness_score>" + num(r.fitness_score) + "</fitness_score>";
+        o += "<num_voxel>" + std::to_string(r.num_voxel) + "</num_voxel>";
+        o += "<num_measured_voxel>" + std::to_string(r.num_measured_voxel) + "</num_measured_voxel>";
+        o += "<voxSize>" + num(r.vox_size) + "</voxSize>";
+        o += "<numClosePairs>" + std::to_string(r.num_close_pairs) + "</numClosePairs>";
+        o += "<initialCenterOfMass><x>" + num(r.initial_center_of_mass[0]) + "</x><y>" + num(r.initial_center_of_mass[1]) + "</y><z>" +
+             num(r.initial_center_of_mass[2]) + "</z></initialCenterOfMass>";
+        o += "<currentCenterOfMass><x>" + num(r.current_center_of_mass[0]) + "</x><y>" + num(r.current_center_of_mass[1]) + "</y><z>" +
+             num(r.current_center_of_mass[2]) + "</z></currentCenterOfMass>";
+        o += "<total_distance_of_all_voxels>" + num(r.total_distance_of_all_voxels) + "</total_distance_of_all_voxels>";
+        o += "</" + nm + ">";
+    }
+    o += "</detail></report>\n";
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, VX3_E_ARG, std::string("cannot open ") + path);
+    fwrite(o.data(), 1, o.size(), f);
+    fclose(f);
+    return VX3_OK;
+}
+
+int vx3_free_sim(vx3_ctx* c, vx3_sim_id id) {
+    if (!c) return VX3_E_ARG;
+    c->names.erase(id);
+    return c->eng->free_sim(id) ? fail(c, VX3_E_ARG, "unknown simulation id") : VX3_OK;
+}
+
+int vx3_last_timing(vx3_ctx* c, double* out) {
+    if (!c || !out) return VX3_E_ARG;
+    const gvx::Timing& t = c->eng->timing();
+    out[0] = t.device_ms;
+    out[1] = t.wall_ms;
+    out[2] = (double)t.voxel_steps;
+    out[3] = (double)t.launches;
+    out[4] = t.link_kernel_ms;
+    out[5] = t.contact_kernel_ms;
+    out[6] = t.voxel_kernel_ms;
+    return VX3_OK;
+}
+
+int vx3_set_tuning(vx3_ctx* c, int bl, int bv, int il, int iv, int gs) {
+    if (!c) return VX3_E_ARG;
+    return c->eng->set_tuning(bl, bv, il, iv, gs);
+}
+
+int vx3_autotune(vx3_ctx* c, const vx3_sim_id* ids, int n) {
+    if (!c) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->autotune(ids, n, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_set_profiling(vx3_ctx* c, int on) {
+    if (!c) return VX3_E_ARG;
+    c->eng->set_profiling(on);
+    return VX3_OK;
+}
+
+int64_t vx3_sim_bytes(vx3_ctx* c, vx3_sim_id id) {
+    if (!c) return VX3_E_ARG;
+    (void)id;
+    return -1;
+}
+
+size_t vx3_bytes_in_use(vx3_ctx* c) { return c ? c->eng->bytes_in_use() : 0; }
+
+static int inspect_world(const char* base, const char* vxd, gvx::SimWorld* w, std::string* err) {
+    if (!base) { *err = "null VXA"; return VX3_E_ARG; }
+    gvx::SimDesc d;
+    if (!gvx::parse_vxa(base, vxd, &d, err)) return VX3_E_PARSE;
+    if (!gvx::build_world(d, w, err)) return VX3_E_PARSE;
+    return VX3_OK;
+}
+
+int vx3_inspect_vxa(const char* base, const char* vxd, int32_t* counts, double* env, char* errbuf, int err_len) {
+    gvx::SimWorld w;
+    std::string err;
+    int e = inspect_world(base, vxd, &w, &err);
+    if (e) {
+        if (errbuf && err_len > 0) { strncpy(errbuf, err.c_str(), (size_t)err_len - 1); errbuf[err_len - 1] = 0; }
+        return e;
+    }
+    if (counts) {
+        counts[0] = w.nv; counts[1] = w.nl; counts[2] = (int32_t)w.vmats.size(); counts[3] = (int32_t)w.lmats.size();
+        counts[4] = w.surface_count; counts[5] = (int32_t)w.desc.externals.size();
+    }
+    if (env) {
+        const gvx::SimDesc& d = w.desc;
+        double v[12] = {d.vox_size, d.dt_frac, d.gravity_mult, (double)d.floor, (double)d.collisions, (double)d.vary_temp,
+                        d.temp_amplitude, d.temp_period, (double)d.enable_expansion, d.initial_temp, d.bounding_radius, d.watch_distance};
+        memcpy(env, v, sizeof(v));
+    }
+    return VX3_OK;
+}
+
+int vx3_inspect_topology(const char* base, const char* vxd, int32_t* vox4, int32_t* lnk4, double* phase, float* vmat18, double* vnom,
+                         int32_t* lidx2, float* lmat20) {
+    gvx::SimWorld w;
+    std::string err;
+    if (int e = inspect_world(base, vxd, &w, &err)) return e;
+    for (int i = 0; i < w.nv; i++) {
+        if (vox4) for (int k = 0; k < 4; k++) vox4[4 * i + k] = w.desc.voxels[4 * i + k];
+        if (phase) phase[i] = w.desc.phase.empty() ? 0.0 : w.desc.phase[i];
+    }
+    for (int i = 0; i < w.nl; i++)
+        if (lnk4) { lnk4[4 * i] = w.link_neg[i]; lnk4[4 * i + 1] = w.link_pos[i]; lnk4[4 * i + 2] = w.link_axis[i]; lnk4[4 * i + 3] = w.link_mat[i]; }
+    for (size_t k = 0; k < w.vmats.size(); k++) {
+        const gvx::VoxelMaterial& m = w.vmats[k];
+        float v[18] = {m.E, m.nu, m.rho, m.cte, m.mus, m.muk, m.zi, m.zg, m.zc, m.eHat, m.mass, m.massInv, m.sqrtMass, m.I, m.Iinv, m.c2m, m.c2i, m.grav};
+        if (vmat18) memcpy(vmat18 + 18 * k, v, sizeof(v));
+        if (vnom) vnom[k] = m.nom;
+    }
+    for (size_t k = 0; k < w.lmats.size(); k++) {
+        const gvx::LinkMaterial& m = w.lmats[k];
+        if (lidx2) { lidx2[2 * k] = m.vox1; lidx2[2 * k + 1] = m.vox2; }
+        float v[20] = {m.E, m.nu, m.eHat, m.a1, m.a2, m.b1, m.b2, m.b3, m.sqA1, m.sqA2xIp, m.sqB1, m.sqB2xFMp, m.sqB3xIp,
+                       m.sigmaYield, m.sigmaFail, m.epsYield, m.epsFail, m.linear ? 1.0f : 0.0f, (float)m.nom, m.rho};
+        if (lmat20) memcpy(lmat20 + 20 * k, v, sizeof(v));
+    }
+    return VX3_OK;
+}
+
+int vx3_inspect_formula(const char* base, const char* vxd, int which, const double* vars, double* out) {
+    if (!base || !vars || !out) return VX3_E_ARG;
+    gvx::SimDesc d;
+    std::string err;
+    if (!gvx::parse_vxa(base, vxd, &d, &err)) return VX3_E_PARSE;
+    const gvx::MathTree& m = which == 0 ? d.stop_formula : d.fitness;
+    gvx::MathVars mv{vars[0], vars[1], vars[2], vars[3], vars[4], vars[5], vars[6], (int)vars[7], (int)vars[8]};
+    *out = gvx::mathtree_eval(m, mv);
+    return VX3_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,992 @@
+// GB300 step engine: HBM arena, per-simulation upload, batched stepping with
+// work queues captured in CUDA graphs, and the continuous-batching serving loop.
+#include "engine.h"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+
+namespace gvx {
+
+namespace {
+
+#define CK(x)                                                                                 \
+    do {                                                                                      \
+        cudaError_t _e = (x);                                                                 \
+        if (_e != cudaSuccess) {                                                              \
+            if (err) *err = std::string(#x) + ": " + cudaGetErrorString(_e);                  \
+            return -5;                                                                        \
+        }                                                                                     \
+    } while (0)
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// First-fit allocator over one device allocation (the HBM budget).
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0;
+    std::map<size_t, size_t> free_;   // offset -> length
+    size_t used = 0;
+    void init(char* b, size_t s) { base = b; size = s; free_.clear(); free_[0] = s; used = 0; }
+    bool alloc(size_t n, size_t* off) {
+        n = align256(n);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *off = it->first;
+                size_t rest = it->second - n, o = it->first + n;
+                free_.erase(it);
+                if (rest) free_[o] = rest;
+                used += n;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t n) {
+        n = align256(n);
+        used -= n;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+        }
+    }
+};
+
+struct Layout {
+    size_t total = 0;
+    size_t add(size_t bytes) { size_t o = total; total += align256(bytes); return o; }
+};
+
+struct SimRec {
+    int64_t id = 0;
+    SimWorld w;
+    int slot = -1;                 // index into device tables while resident
+    bool resident = false;
+    size_t off = 0, bytes = 0;
+    dev::Sim dsim{};
+    int32_t status = SIM_IDLE;
+    float dt = 0, optdt = 0;
+    int cycle_step = 0;
+    double init_com[3] = {0, 0, 0};
+    int num_measured = 0;
+    int64_t horizon = 0;
+    double submit_s = 0, start_s = 0, finish_s = 0;
+    bool retired = false;
+    SimResult result{};
+    int n_vox_items = 0;
+};
+
+class EngineImpl final : public Engine {
+public:
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evk_[6] = {};
+    Arena arena_;
+    char* arena_base_ = nullptr;
+    std::map<int64_t, std::unique_ptr<SimRec>> sims_;
+    int64_t next_id_ = 1;
+    // device tables
+    int cap_slots_ = 0;
+    dev::Sim* d_sims_ = nullptr;
+    dev::Ctl* d_ctl_ = nullptr;
+    std::vector<SimRec*> slot_owner_;
+    int* d_tickets_ = nullptr;
+    dev::Item* d_items_ = nullptr;
+    int cap_items_ = 0;
+    double* d_partials_ = nullptr;
+    double* d_com4_ = nullptr;
+    // tuning
+    int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 512, graph_steps_ = 64;
+    int sm_count_ = 152;
+    int profiling_ = 0;
+    Timing timing_;
+    double t0_ = now_s();
+    // serving
+    std::deque<int64_t> queue_;
+    std::vector<int64_t> active_;
+    // cached batch (items + graph) for a set of slots
+    std::vector<int> batch_slots_;
+    int n_link_items_ = 0, n_contact_items_ = 0, n_vox_items_ = 0;
+    bool any_collide_ = false;
+    cudaGraphExec_t graph_ = nullptr;
+    int graph_len_ = 0;
+    bool batch_dirty_ = true;
+
+    ~EngineImpl() override {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        cudaSetDevice(device_);
+        cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_partials_); cudaFree(d_com4_);
+        cudaFree(arena_base_);
+        if (ev0_) cudaEventDestroy(ev0_);
+        if (ev1_) cudaEventDestroy(ev1_);
+        for (auto& e : evk_) if (e) cudaEventDestroy(e);
+        if (stream_) cudaStreamDestroy(stream_);
+    }
+
+    int init(int device, size_t budget, std::string* err) {
+        device_ = device;
+        CK(cudaSetDevice(device));
+        CK(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
+        CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        CK(cudaEventCreate(&ev0_));
+        CK(cudaEventCreate(&ev1_));
+        for (auto& e : evk_) CK(cudaEventCreate(&e));
+        if (budget == 0) {
+            size_t fr = 0, tot = 0;
+            CK(cudaMemGetInfo(&fr, &tot));
+            budget = fr / 2;
+        }
+        CK(cudaMalloc(&arena_base_, budget));
+        arena_.init(arena_base_, budget);
+        CK(cudaMalloc(&d_tickets_, 4 * sizeof(int)));
+        CK(cudaMemset(d_tickets_, 0, 4 * sizeof(int)));
+        CK(cudaMalloc(&d_com4_, 4 * sizeof(double)));
+        return grow_slots(64, err);
+    }
+
+    int grow_slots(int n, std::string* err) {
+        if (n <= cap_slots_) return 0;
+        int nc = std::max(n, 2 * cap_slots_);
+        dev::Sim* ns = nullptr;
+        dev::Ctl* nctl = nullptr;
+        CK(cudaMalloc(&ns, sizeof(dev::Sim) * nc));
+        CK(cudaMalloc(&nctl, sizeof(dev::Ctl) * nc));
+        CK(cudaMemset(nctl, 0, sizeof(dev::Ctl) * nc));
+        if (cap_slots_) {
+            CK(cudaStreamSynchronize(stream_));
+            CK(cudaMemcpy(ns, d_sims_, sizeof(dev::Sim) * cap_slots_, cudaMemcpyDeviceToDevice));
+            CK(cudaMemcpy(nctl, d_ctl_, sizeof(dev::Ctl) * cap_slots_, cudaMemcpyDeviceToDevice));
+            cudaFree(d_sims_);
+            cudaFree(d_ctl_);
+        }
+        d_sims_ = ns;
+        d_ctl_ = nctl;
+        slot_owner_.resize(nc, nullptr);
+        cap_slots_ = nc;
+        batch_dirty_ = true;
+        return 0;
+    }
+
+    int64_t sim_bytes_world(const SimWorld& w) const {
+        Layout L;
+        compute_layout(w, &L, nullptr);
+        return (int64_t)L.total;
+    }
+    int64_t sim_bytes(const SimDesc& d) const override {
+        SimWorld w;
+        std::string e;
+        if (!build_world(d, &w, &e)) return -1;
+        return sim_bytes_world(w);
+    }
+
+    struct Offs {
+        size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
+        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext;
+        int hash_size;
+    };
+    static void compute_layout(const SimWorld& w, Layout* L, Offs* o) {
+        Offs t{};
+        const size_t nv = w.nv, nl = w.nl;
+        const bool col = w.desc.collisions;
+        t.vm = L->add(sizeof(dev::VMat) * w.vmats.size());
+        t.lm = L->add(sizeof(dev::LMat) * std::max<size_t>(1, w.lmats.size()));
+        t.ext = L->add(sizeof(dev::Ext) * std::max<size_t>(1, w.desc.externals.size()));
+        for (int k = 0; k < 3; k++) t.pos[k] = L->add(8 * nv);
+        for (int k = 0; k < 3; k++) t.mom[k] = L->add(8 * nv);
+        for (int k = 0; k < 4; k++) t.q[k] = L->add(8 * nv);
+        for (int k = 0; k < 3; k++) t.am[k] = L->add(8 * nv);
+        t.temp = L->add(4 * nv);
+        t.ps = L->add(4 * 3 * nv);
+        t.vfl = L->add(4 * nv);
+        t.vmat = L->add(nv);
+        t.vext = L->add(4 * nv);
+        t.phase = L->add(8 * nv);
+        t.sf = L->add(8 * 18 * nv);
+        t.sm = L->add(8 * 18 * nv);
+        t.ss = L->add(4 * 6 * nv);
+        t.lneg = L->add(4 * std::max<size_t>(1, nl));
+        t.lpos = L->add(4 * std::max<size_t>(1, nl));
+        t.lax = L->add(std::max<size_t>(1, nl));
+        t.lmt = L->add(std::max<size_t>(1, nl));
+        t.lst = L->add(8 * 9 * std::max<size_t>(1, nl));
+        t.lsf = L->add(4 * 3 * std::max<size_t>(1, nl));
+        t.lfl = L->add(std::max<size_t>(1, nl));
+        t.ijk = L->add(2 * 3 * nv);
+        if (col) {
+            size_t ns = std::max(1, w.surface_count);
+            int hs = 1;
+            while (hs < 2 * (int)ns) hs <<= 1;
+            t.hash_size = hs;
+            t.surf = L->add(4 * ns);
+            t.reach = L->add(4 * dev::kReachWords * nv);
+            t.ccount = L->add(4 * nv);
+            t.cforce = L->add(4 * 3 * dev::kContactCap * nv);
+            t.hhead = L->add(4 * 2 * (size_t)hs);
+            t.hnext = L->add(4 * nv);
+        }
+        if (o) *o = t;
+    }
+
+    int add_sim(const SimDesc& d, int64_t* id, std::string* err) override {
+        auto r = std::make_unique<SimRec>();
+        if (!build_world(d, &r->w, err)) return -1;
+        r->id = next_id_++;
+        *id = r->id;
+        // initial centre of mass from the lattice positions
+        double sx = 0, sy = 0, sz = 0, tm = 0;
+        for (int i = 0; i < r->w.nv; i++) {
+            const VoxelMaterial& m = r->w.vmats[d.voxels[4 * i + 3]];
+            if (!m.is_measured) continue;
+            r->num_measured++;
+            double wgt = m.mass;
+            sx += d.voxels[4 * i] * m.nom * wgt; sy += d.voxels[4 * i + 1] * m.nom * wgt; sz += d.voxels[4 * i + 2] * m.nom * wgt;
+            tm += wgt;
+        }
+        if (tm != 0) { r->init_com[0] = sx / tm; r->init_com[1] = sy / tm; r->init_com[2] = sz / tm; }
+        r->submit_s = now_s() - t0_;
+        sims_[r->id] = std::move(r);
+        return 0;
+    }
+
+    SimRec* find(int64_t id) {
+        auto it = sims_.find(id);
+        return it == sims_.end() ? nullptr : it->second.get();
+    }
+
+    int set_external(int64_t id, const External& x, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        if (r->resident) { *err = "externals must be set before the first step"; return -7; }
+        if (x.voxel < 0 || x.voxel >= r->w.nv) { *err = "voxel index out of range"; return -6; }
+        auto& ex = r->w.desc.externals;
+        bool found = false;
+        for (auto& e : ex) if (e.voxel == x.voxel) { e = x; found = true; }
+        if (!found) ex.push_back(x);
+        std::string e2;
+        SimDesc dd = r->w.desc;
+        if (!build_world(dd, &r->w, &e2)) { *err = e2; return -1; }
+        return 0;
+    }
+
+    int free_slot() {
+        for (int i = 0; i < cap_slots_; i++) if (!slot_owner_[i]) return i;
+        return -1;
+    }
+
+    // Copies a simulation's topology and initial state to the device.
+    int upload(SimRec* r, std::string* err) {
+        if (r->resident) return 0;
+        SimWorld& w = r->w;
+        Layout L;
+        Offs o;
+        compute_layout(w, &L, &o);
+        size_t off;
+        if (!arena_.alloc(L.total, &off)) {
+            if (err) *err = "HBM budget exhausted";
+            return -2;
+        }
+        int slot = free_slot();
+        if (slot < 0) {
+            int e = grow_slots(cap_slots_ * 2, err);
+            if (e) { arena_.release(off, L.total); return e; }
+            slot = free_slot();
+        }
+        r->off = off;
+        r->bytes = L.total;
+        char* base = arena_base_ + off;
+        std::vector<char> h(L.total, 0);
+        const size_t nv = w.nv, nl = w.nl;
+        auto P = [&](size_t o2) { return h.data() + o2; };
+        // materials
+        dev::VMat* vm = (dev::VMat*)P(o.vm);
+        for (size_t i = 0; i < w.vmats.size(); i++) {
+            const VoxelMaterial& m = w.vmats[i];
+            dev::VMat& x = vm[i];
+            x.E = m.E; x.nu = m.nu; x.cte = m.cte; x.mus = m.mus; x.muk = m.muk; x.eHat = m.eHat;
+            x.mass = m.mass; x.massInv = m.massInv; x.Iinv = m.Iinv;
+            x.dampNum = 2 * m.sqrtMass * m.zi;
+            x.gDampT = m.zg * m.c2m; x.gDampR = m.zg * m.c2i; x.cDampT = m.zc * m.c2m;
+            x.gravForce = -m.mass * 9.80665f * m.grav;
+            x.penStiff = (float)(2 * m.E * m.nom);
+            x.sizef = (float)m.nom;
+            x.nom = m.nom;
+            x.measured = m.is_measured;
+        }
+        dev::LMat* lm = (dev::LMat*)P(o.lm);
+        for (size_t i = 0; i < w.lmats.size(); i++) {
+            const LinkMaterial& m = w.lmats[i];
+            dev::LMat& x = lm[i];
+            x.E = m.E; x.nu = m.nu; x.eHat = m.eHat; x.a1 = m.a1; x.a2 = m.a2; x.b1 = m.b1; x.b2 = m.b2; x.b3 = m.b3;
+            x.sqA1 = m.sqA1; x.sqA2xIp = m.sqA2xIp; x.sqB1 = m.sqB1; x.sqB2xFMp = m.sqB2xFMp; x.sqB3xIp = m.sqB3xIp;
+            x.epsFail = m.epsFail; x.linear = m.linear; x.n = m.n;
+            for (int k = 0; k < 18; k++) { x.strain[k] = k < kMaxModelPoints + 2 ? m.strain[k] : 0; x.stress[k] = k < kMaxModelPoints + 2 ? m.stress[k] : 0; }
+        }
+        dev::Ext* ex = (dev::Ext*)P(o.ext);
+        for (size_t i = 0; i < w.desc.externals.size(); i++) {
+            const External& e = w.desc.externals[i];
+            dev::Ext& x = ex[i];
+            x.dof = e.dof_fixed;
+            for (int k = 0; k < 3; k++) { x.f[k] = e.force[k]; x.m[k] = e.moment[k]; x.tr[k] = e.translate[k]; }
+            double rx = e.rotate[0], ry = e.rotate[1], rz = e.rotate[2];
+            if (rx != 0 || ry != 0 || rz != 0) {
+                /* CVX_External::rotationChanged -> Quat3D::FromRotationVector (Quat3D.h:128-143) */
+                double tx = 0.5 * rx, ty = 0.5 * ry, tz = 0.5 * rz;
+                double m2 = tx * tx + ty * ty + tz * tz, qw, s;
+                if (m2 * m2 < 5.328e-15) { qw = 1.0 - 0.5 * m2; s = 1.0 - m2 / 6.0; }
+                else { double mm = sqrt(m2); qw = cos(mm); s = sin(mm) / mm; }
+                x.rq[0] = qw; x.rq[1] = tx * s; x.rq[2] = ty * s; x.rq[3] = tz * s;
+            } else { x.rq[0] = 1; x.rq[1] = x.rq[2] = x.rq[3] = 0; }
+        }
+        double* px = (double*)P(o.pos[0]); double* py = (double*)P(o.pos[1]); double* pz = (double*)P(o.pos[2]);
+        double* qw = (double*)P(o.q[0]);
+        uint32_t* vfl = (uint32_t*)P(o.vfl);
+        uint8_t* vmat = (uint8_t*)P(o.vmat);
+        int32_t* vext = (int32_t*)P(o.vext);
+        double* ph = (double*)P(o.phase);
+        int16_t* ijk = (int16_t*)P(o.ijk);
+        for (size_t i = 0; i < nv; i++) {
+            int mi = w.desc.voxels[4 * i + 3];
+            double nom = w.vmats[mi].nom;
+            px[i] = w.desc.voxels[4 * i] * nom; py[i] = w.desc.voxels[4 * i + 1] * nom; pz[i] = w.desc.voxels[4 * i + 2] * nom;
+            qw[i] = 1.0;
+            uint32_t f = dev::VF_STATIC;
+            for (int d = 0; d < 6; d++) if (w.vox_links[i * 6 + d] >= 0) f |= 1u << d;
+            if (w.vox_interior[i]) f |= dev::VF_INTERIOR;
+            if (w.vox_ext[i] >= 0) f |= dev::VF_EXT;
+            if (w.vmats[mi].is_measured) f |= dev::VF_MEASURED;
+            vfl[i] = f;
+            vmat[i] = (uint8_t)mi;
+            vext[i] = w.vox_ext[i];
+            ph[i] = w.desc.phase.empty() ? 0.0 : w.desc.phase[i];
+            for (int k = 0; k < 3; k++) ijk[k * nv + i] = (int16_t)w.desc.voxels[4 * i + k];
+        }
+        memcpy(P(o.lneg), w.link_neg.data(), 4 * nl);
+        memcpy(P(o.lpos), w.link_pos.data(), 4 * nl);
+        memcpy(P(o.lax), w.link_axis.data(), nl);
+        memcpy(P(o.lmt), w.link_mat.data(), nl);
+        memset(P(o.lfl), dev::LF_SMALL, std::max<size_t>(1, nl));
+        int flags = 0;
+        if (w.desc.floor) flags |= dev::SF_FLOOR;
+        if (w.desc.collisions) flags |= dev::SF_COLLIDE;
+        if (w.desc.vary_temp && w.desc.temp_period > 0) flags |= dev::SF_VARY;
+        if (w.desc.enable_expansion) flags |= dev::SF_EXPAND;
+        double max_bsa = 0;
+        if (w.desc.collisions) {
+            int32_t* surf = (int32_t*)P(o.surf);
+            int k = 0;
+            for (size_t i = 0; i < nv; i++) if (!w.vox_interior[i]) surf[k++] = (int32_t)i;
+            std::vector<uint32_t> masks = reach_masks(w, 5, dev::kReachWords);
+            memcpy(P(o.reach), masks.data(), 4 * masks.size());
+            memset(P(o.hhead), 0xFF, 4 * 2 * (size_t)o.hash_size);
+            // largest contact distance: 0.625*(bsa1+bsa2) with the largest actuation expansion
+            double amp = (flags & dev::SF_VARY) ? fabs(w.desc.temp_amplitude) : fabs(w.desc.initial_temp);
+            for (auto& m : w.vmats) max_bsa = std::max(max_bsa, m.nom * (1 + amp * fabs(m.cte)));
+        }
+        dev::Sim& S = r->dsim;
+        S = dev::Sim{};
+        S.nv = (int)nv; S.nl = (int)nl; S.nsurf = w.surface_count; S.flags = flags;
+        S.temp_amp = w.desc.temp_amplitude; S.temp_period = w.desc.temp_period;
+        S.cell_size = std::max(1e-9, 2 * 0.625 * max_bsa * 1.01);
+        S.hash_size = o.hash_size > 0 ? o.hash_size : 1;
+        S.env_radius = 0.625f;
+        auto D = [&](size_t o2) { return base + o2; };
+        S.vm = (const dev::VMat*)D(o.vm); S.lm = (const dev::LMat*)D(o.lm); S.ext = (const dev::Ext*)D(o.ext);
+        S.px = (double*)D(o.pos[0]); S.py = (double*)D(o.pos[1]); S.pz = (double*)D(o.pos[2]);
+        S.mx = (double*)D(o.mom[0]); S.my = (double*)D(o.mom[1]); S.mz = (double*)D(o.mom[2]);
+        S.qw = (double*)D(o.q[0]); S.qx = (double*)D(o.q[1]); S.qy = (double*)D(o.q[2]); S.qz = (double*)D(o.q[3]);
+        S.ax = (double*)D(o.am[0]); S.ay = (double*)D(o.am[1]); S.az = (double*)D(o.am[2]);
+        S.temp = (float*)D(o.temp); S.ps = (float*)D(o.ps); S.vfl = (uint32_t*)D(o.vfl);
+        S.vmat = (const uint8_t*)D(o.vmat); S.vext = (const int32_t*)D(o.vext); S.phase = (const double*)D(o.phase);
+        S.sf = (double*)D(o.sf); S.sm = (double*)D(o.sm); S.ss = (float*)D(o.ss);
+        S.lneg = (const int32_t*)D(o.lneg); S.lpos = (const int32_t*)D(o.lpos);
+        S.lax = (const uint8_t*)D(o.lax); S.lmt = (const uint8_t*)D(o.lmt);
+        S.lst = (double*)D(o.lst); S.lsf = (float*)D(o.lsf); S.lfl = (uint8_t*)D(o.lfl);
+        S.ijk = (const int16_t*)D(o.ijk);
+        if (w.desc.collisions) {
+            S.surf = (const int32_t*)D(o.surf); S.reach = (const uint32_t*)D(o.reach);
+            S.ccount = (int32_t*)D(o.ccount); S.cforce = (float*)D(o.cforce);
+            S.hash_head = (int32_t*)D(o.hhead); S.hash_next = (int32_t*)D(o.hnext);
+        }
+        CK(cudaMemcpyAsync(base, h.data(), L.total, cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(d_sims_ + slot, &S, sizeof(S), cudaMemcpyHostToDevice, stream_));
+        dev::Ctl c{};
+        c.status = SIM_IDLE;
+        c.stop = w.desc.stop_formula;
+        c.hash_parity = 0;
+        CK(cudaMemcpyAsync(d_ctl_ + slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+        // first actuation temperature (t = 0), then the stable step from it
+        int g = std::min(4 * sm_count_, (int)((nv + 255) / 256));
+        dev::k_init_temp<<<std::max(1, g), 256, 0, stream_>>>(d_sims_, slot, w.desc.initial_temp);
+        CK(cudaGetLastError());
+        if (nl > 0) {
+            int gl = std::min(4 * sm_count_, (int)((nl + 255) / 256));
+            dev::k_dt<<<std::max(1, gl), 256, 0, stream_>>>(d_sims_, d_ctl_, slot);
+            CK(cudaGetLastError());
+        }
+        if (w.desc.collisions && w.surface_count > 0) {
+            dev::k_hash_build<<<std::max(1, std::min(4 * sm_count_, (w.surface_count + 255) / 256)), 256, 0, stream_>>>(d_sims_, d_ctl_, slot);
+            CK(cudaGetLastError());
+        }
+        uint32_t bits = 0;
+        CK(cudaMemcpyAsync(&bits, &d_ctl_[slot].maxf2_bits, 4, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        float maxf2;
+        memcpy(&maxf2, &bits, 4);
+        if (!(maxf2 > 0.0f)) {   // no links: per-voxel frequencies (Voxelyze.cpp:302-307)
+            maxf2 = 0.0f;
+            for (size_t i = 0; i < nv; i++) {
+                const VoxelMaterial& m = w.vmats[w.desc.voxels[4 * i + 3]];
+                float f2 = (float)(m.E * m.nom / m.mass);
+                if (f2 > maxf2) maxf2 = f2;
+            }
+        }
+        float opt = maxf2 <= 0.0f ? 0.0f : 1.0f / (6.283185f * sqrtf(maxf2));
+        if (opt < 1e-10f) opt = 1e-10f;
+        r->optdt = opt;
+        r->dt = (float)(w.desc.dt_frac * (double)opt);
+        r->cycle_step = r->dt > 0 ? (int)(w.desc.temp_period / r->dt) : 0;
+        c.dt = r->dt;
+        c.optdt = opt;
+        c.cycle_step = r->cycle_step;
+        c.maxf2_bits = bits;
+        CK(cudaMemcpyAsync(d_ctl_ + slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        r->slot = slot;
+        r->resident = true;
+        r->status = SIM_IDLE;
+        slot_owner_[slot] = r;
+        batch_dirty_ = true;
+        return 0;
+    }
+
+    void release(SimRec* r) {
+        if (!r->resident) return;
+        cudaStreamSynchronize(stream_);
+        arena_.release(r->off, r->bytes);
+        slot_owner_[r->slot] = nullptr;
+        r->resident = false;
+        r->slot = -1;
+        batch_dirty_ = true;
+    }
+
+    // Builds work items for a set of slots: links, contacts and voxels.
+    int build_items(const std::vector<int>& slots, std::string* err) {
+        std::vector<dev::Item> items;
+        n_link_items_ = n_contact_items_ = n_vox_items_ = 0;
+        any_collide_ = false;
+        for (int s : slots) {
+            SimRec* r = slot_owner_[s];
+            for (int b = 0; b < r->w.nl; b += items_links_) items.push_back({s, b, std::min(r->w.nl, b + items_links_), 0});
+        }
+        n_link_items_ = (int)items.size();
+        for (int s : slots) {
+            SimRec* r = slot_owner_[s];
+            if (!r->w.desc.collisions || r->w.surface_count == 0) continue;
+            any_collide_ = true;
+            const int chunk = 128;
+            for (int b = 0; b < r->w.surface_count; b += chunk) items.push_back({s, b, std::min(r->w.surface_count, b + chunk), 0});
+        }
+        n_contact_items_ = (int)items.size() - n_link_items_;
+        std::vector<std::pair<int, int>> ctl_items;   // slot -> (begin, count)
+        for (int s : slots) {
+            SimRec* r = slot_owner_[s];
+            int begin = (int)items.size() - n_link_items_ - n_contact_items_;
+            int cnt = 0;
+            for (int b = 0; b < r->w.nv; b += items_voxels_) { items.push_back({s, b, std::min(r->w.nv, b + items_voxels_), cnt}); cnt++; }
+            r->n_vox_items = cnt;
+            ctl_items.emplace_back(begin, cnt);
+        }
+        n_vox_items_ = (int)items.size() - n_link_items_ - n_contact_items_;
+        if ((int)items.size() > cap_items_) {
+            cudaFree(d_items_);
+            cudaFree(d_partials_);
+            cap_items_ = std::max((int)items.size(), 2 * cap_items_);
+            CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
+            CK(cudaMalloc(&d_partials_, sizeof(double) * 4 * cap_items_));
+        }
+        if (!items.empty()) CK(cudaMemcpyAsync(d_items_, items.data(), sizeof(dev::Item) * items.size(), cudaMemcpyHostToDevice, stream_));
+        for (size_t i = 0; i < slots.size(); i++) {
+            int vals[2] = {ctl_items[i].second, ctl_items[i].first};   // n_vox_items, item_begin
+            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].n_vox_items, vals, sizeof(vals), cudaMemcpyHostToDevice, stream_));
+            int zero = 0;
+            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+        }
+        CK(cudaMemsetAsync(d_tickets_, 0, 4 * sizeof(int), stream_));
+        return 0;
+    }
+
+    int grid_for(int n_items, int block) const {
+        int per_sm = block >= 256 ? 4 : 8;
+        return std::max(1, std::min(n_items, sm_count_ * per_sm));
+    }
+
+    void launch_step(cudaStream_t st, bool prof) {
+        const dev::Item* li = d_items_;
+        const dev::Item* ci = d_items_ + n_link_items_;
+        const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
+        if (prof) cudaEventRecord(evk_[0], st);
+        dev::k_links<<<grid_for(n_link_items_, block_links_), block_links_, 0, st>>>(d_sims_, d_ctl_, li, n_link_items_, d_tickets_);
+        if (prof) cudaEventRecord(evk_[1], st);
+        if (any_collide_) dev::k_contacts<<<grid_for(n_contact_items_, 128), 128, 0, st>>>(d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
+        if (prof) cudaEventRecord(evk_[2], st);
+        dev::k_voxels<<<grid_for(n_vox_items_, block_voxels_), block_voxels_, 0, st>>>(d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_,
+                                                                                      d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
+        if (prof) cudaEventRecord(evk_[3], st);
+    }
+
+    int set_running(const std::vector<int>& slots, const std::vector<int64_t>& targets, std::string* err) {
+        for (size_t i = 0; i < slots.size(); i++) {
+            int32_t st = SIM_RUNNING;
+            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].status, &st, 4, cudaMemcpyHostToDevice, stream_));
+            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].target, &targets[i], 8, cudaMemcpyHostToDevice, stream_));
+        }
+        return 0;
+    }
+
+    int read_ctl(int slot, dev::Ctl* c, std::string* err) {
+        CK(cudaMemcpyAsync(c, d_ctl_ + slot, offsetof(dev::Ctl, stop), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
+    // Runs until every listed simulation has left the RUNNING state.
+    int drive(const std::vector<SimRec*>& rs, int mode, std::string* err) {
+        int64_t vsteps_before = 0;
+        std::vector<int64_t> steps0(rs.size());
+        for (size_t i = 0; i < rs.size(); i++) {
+            dev::Ctl c;
+            if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
+            steps0[i] = c.steps;
+        }
+        timing_.launches = 0;
+        double w0 = now_s();
+        CK(cudaEventRecord(ev0_, stream_));
+        if (mode == MODE_PLAIN) {
+            for (size_t i = 0; i < rs.size(); i++) {
+                std::vector<int> one{rs[i]->slot};
+                if (int e = build_items(one, err)) return e;
+                for (;;) {
+                    for (int k = 0; k < 16; k++) { launch_step(stream_, false); timing_.launches += any_collide_ ? 3 : 2; }
+                    dev::Ctl c;
+                    if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
+                    if (c.status != SIM_RUNNING) break;
+                }
+            }
+            batch_dirty_ = true;
+        } else {
+            std::vector<int> slots;
+            for (auto* r : rs) slots.push_back(r->slot);
+            if (batch_dirty_ || slots != batch_slots_) {
+                if (int e = build_items(slots, err)) return e;
+                batch_slots_ = slots;
+                if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+                batch_dirty_ = false;
+            }
+            if (!graph_) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < graph_steps_; k++) launch_step(stream_, false);
+                CK(cudaStreamEndCapture(stream_, &g));
+                CK(cudaGraphInstantiate(&graph_, g, 0));
+                cudaGraphDestroy(g);
+                graph_len_ = graph_steps_;
+            }
+            for (;;) {
+                if (profiling_) {
+                    launch_step(stream_, true);
+                    timing_.launches += any_collide_ ? 3 : 2;
+                } else {
+                    CK(cudaGraphLaunch(graph_, stream_));
+                    timing_.launches += (int64_t)graph_len_ * (any_collide_ ? 3 : 2);
+                }
+                bool running = false;
+                // poll a compact status array
+                for (auto* r : rs) {
+                    int32_t st;
+                    CK(cudaMemcpyAsync(&st, &d_ctl_[r->slot].status, 4, cudaMemcpyDeviceToHost, stream_));
+                    CK(cudaStreamSynchronize(stream_));
+                    if (st == SIM_RUNNING) { running = true; break; }
+                }
+                if (!running) break;
+            }
+        }
+        CK(cudaEventRecord(ev1_, stream_));
+        CK(cudaEventSynchronize(ev1_));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0_, ev1_);
+        timing_.device_ms = ms;
+        timing_.wall_ms = (now_s() - w0) * 1e3;
+        if (profiling_) {
+            float a = 0, b = 0, c = 0;
+            cudaEventElapsedTime(&a, evk_[0], evk_[1]);
+            cudaEventElapsedTime(&b, evk_[1], evk_[2]);
+            cudaEventElapsedTime(&c, evk_[2], evk_[3]);
+            timing_.link_kernel_ms = a; timing_.contact_kernel_ms = b; timing_.voxel_kernel_ms = c;
+        }
+        for (size_t i = 0; i < rs.size(); i++) {
+            dev::Ctl c;
+            if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
+            rs[i]->status = c.status;
+            vsteps_before += (c.steps - steps0[i]) * rs[i]->w.nv;
+        }
+        timing_.voxel_steps = vsteps_before;
+        return 0;
+    }
+
+    int prepare(const int64_t* ids, int n, std::vector<SimRec*>* rs, std::string* err) {
+        for (int i = 0; i < n; i++) {
+            SimRec* r = find(ids[i]);
+            if (!r) { *err = "unknown simulation id"; return -6; }
+            if (int e = upload(r, err)) return e;
+            rs->push_back(r);
+        }
+        return 0;
+    }
+
+    int step(const int64_t* ids, int n, int mode, int64_t steps, std::string* err) override {
+        std::vector<SimRec*> rs;
+        if (int e = prepare(ids, n, &rs, err)) return e;
+        std::vector<int> slots;
+        std::vector<int64_t> targets;
+        for (auto* r : rs) {
+            dev::Ctl c;
+            if (int e = read_ctl(r->slot, &c, err)) return e;
+            if (c.status == SIM_DIVERGED || c.status == SIM_ERROR) continue;
+            slots.push_back(r->slot);
+            targets.push_back(c.steps + steps);
+        }
+        if (slots.empty()) return 0;
+        // the stop formula is not applied by step(): clear it for the call, restore afterwards
+        std::vector<MathTree> saved(slots.size());
+        for (size_t i = 0; i < slots.size(); i++) {
+            CK(cudaMemcpy(&saved[i], &d_ctl_[slots[i]].stop, sizeof(MathTree), cudaMemcpyDeviceToHost));
+            MathTree none;
+            none.n = 0;
+            CK(cudaMemcpy(&d_ctl_[slots[i]].stop, &none, sizeof(MathTree), cudaMemcpyHostToDevice));
+        }
+        if (int e = set_running(slots, targets, err)) return e;
+        std::vector<SimRec*> act;
+        for (auto* r : rs) if (std::find(slots.begin(), slots.end(), r->slot) != slots.end()) act.push_back(r);
+        int e = drive(act, mode, err);
+        for (size_t i = 0; i < slots.size(); i++) cudaMemcpy(&d_ctl_[slots[i]].stop, &saved[i], sizeof(MathTree), cudaMemcpyHostToDevice);
+        for (auto* r : act) {
+            int32_t st;
+            cudaMemcpy(&st, &d_ctl_[r->slot].status, 4, cudaMemcpyDeviceToHost);
+            if (st == SIM_DONE) { st = SIM_IDLE; cudaMemcpy(&d_ctl_[r->slot].status, &st, 4, cudaMemcpyHostToDevice); }
+            r->status = st;
+        }
+        return e;
+    }
+
+    int run(const int64_t* ids, int n, int mode, int64_t max_steps, std::string* err) override {
+        std::vector<SimRec*> rs;
+        if (int e = prepare(ids, n, &rs, err)) return e;
+        std::vector<int> slots;
+        std::vector<int64_t> targets;
+        std::vector<SimRec*> act;
+        for (auto* r : rs) {
+            dev::Ctl c;
+            if (int e = read_ctl(r->slot, &c, err)) return e;
+            if (c.status != SIM_IDLE) continue;
+            // StopConditionMet is checked before each step (VX3_SimulationManager.cu:62-64)
+            if (r->w.desc.stop_formula.n > 0) {
+                MathVars mv{c.com[0], c.com[1], c.com[2], 0, c.t, c.recent_angle, 0, 0, r->w.nv};
+                if (mathtree_eval(r->w.desc.stop_formula, mv) > 0) { finish(r, SIM_DONE, err); continue; }
+            }
+            int64_t cap = max_steps > 0 ? max_steps : 1000000;   // VX3 maximum step count
+            slots.push_back(r->slot);
+            targets.push_back(c.steps + cap);
+            act.push_back(r);
+        }
+        if (act.empty()) return 0;
+        if (int e = set_running(slots, targets, err)) return e;
+        int e = drive(act, mode, err);
+        if (e) return e;
+        for (auto* r : act) finish(r, r->status, err);
+        return 0;
+    }
+
+    int com(SimRec* r, double* out, std::string* err) {
+        dev::k_com<<<1, 256, 0, stream_>>>(d_sims_, r->slot, d_com4_);
+        CK(cudaGetLastError());
+        double c4[4];
+        CK(cudaMemcpyAsync(c4, d_com4_, sizeof(c4), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        if (c4[3] == 0) out[0] = out[1] = out[2] = 0;
+        else for (int k = 0; k < 3; k++) out[k] = c4[k] / c4[3];
+        return 0;
+    }
+
+    // Final centre of mass and fitness (VX3_SimulationManager.cu:116-117, VX3_VoxelyzeKernel.cu:530-534)
+    int finish(SimRec* r, int status, std::string* err) {
+        dev::Ctl c;
+        if (int e = read_ctl(r->slot, &c, err)) return e;
+        SimResult& R = r->result;
+        R = SimResult{};
+        R.id = r->id;
+        R.status = status == SIM_RUNNING ? SIM_DONE : status;
+        R.num_voxel = r->w.nv;
+        R.num_measured_voxel = r->num_measured;
+        R.steps = c.steps;
+        R.current_time = c.t;
+        R.vox_size = r->w.desc.vox_size;
+        for (int k = 0; k < 3; k++) R.initial_com[k] = r->init_com[k];
+        if (int e = com(r, R.current_com, err)) return e;
+        MathVars mv{R.current_com[0] - R.initial_com[0], R.current_com[1] - R.initial_com[1], R.current_com[2] - R.initial_com[2],
+                    0, c.t, c.recent_angle, 0, 0, r->w.nv};
+        R.fitness = mathtree_eval(r->w.desc.fitness, mv);
+        // total distance travelled by measured voxels (VX3_SimulationManager.cu:442-452)
+        std::vector<double> p(3 * (size_t)r->w.nv);
+        CK(cudaMemcpyAsync(p.data(), r->dsim.px, 8 * r->w.nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(p.data() + r->w.nv, r->dsim.py, 8 * r->w.nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(p.data() + 2 * (size_t)r->w.nv, r->dsim.pz, 8 * r->w.nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        double tot = 0;
+        for (int i = 0; i < r->w.nv; i++) {
+            if (!r->w.vmats[r->w.desc.voxels[4 * i + 3]].is_measured) continue;
+            double nom = r->w.vmats[r->w.desc.voxels[4 * i + 3]].nom;
+            double dx = p[i] - r->w.desc.voxels[4 * i] * nom, dy = p[r->w.nv + i] - r->w.desc.voxels[4 * i + 1] * nom,
+                   dz = p[2 * (size_t)r->w.nv + i] - r->w.desc.voxels[4 * i + 2] * nom;
+            tot += sqrt(dx * dx + dy * dy + dz * dz);
+        }
+        R.total_distance = tot;
+        R.submit_s = r->submit_s;
+        R.start_s = r->start_s;
+        r->finish_s = now_s() - t0_;
+        R.finish_s = r->finish_s;
+        r->status = R.status;
+        r->retired = true;
+        return 0;
+    }
+
+    // ---------------------------------------------------------------- serving
+    int submit(int64_t id, int64_t horizon, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        r->horizon = horizon;
+        r->submit_s = now_s() - t0_;
+        queue_.push_back(id);
+        return 0;
+    }
+    int pending() const override { return (int)(queue_.size() + active_.size()); }
+
+    int poll(SimResult* out, int max, int chunk, std::string* err) override {
+        // admit while the HBM budget allows (first come, first served)
+        while (!queue_.empty()) {
+            SimRec* r = find(queue_.front());
+            if (!r) { queue_.pop_front(); continue; }
+            std::string e2;
+            int e = upload(r, &e2);
+            if (e == -2) {
+                if (active_.empty()) { *err = "simulation larger than the HBM budget"; return -2; }
+                break;
+            }
+            if (e) { *err = e2; return e; }
+            queue_.pop_front();
+            r->start_s = now_s() - t0_;
+            std::vector<int> one{r->slot};
+            std::vector<int64_t> tg{r->horizon > 0 ? r->horizon : 1000000};
+            if (int e3 = set_running(one, tg, err)) return e3;
+            active_.push_back(r->id);
+            batch_dirty_ = true;
+        }
+        if (active_.empty()) return 0;
+        std::vector<int> slots;
+        for (int64_t id : active_) slots.push_back(find(id)->slot);
+        if (batch_dirty_ || slots != batch_slots_) {
+            if (int e = build_items(slots, err)) return e;
+            batch_slots_ = slots;
+            if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+            batch_dirty_ = false;
+        }
+        int k = std::max(1, chunk);
+        if (!graph_ || graph_len_ != k) {
+            if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+            for (int s = 0; s < k; s++) launch_step(stream_, false);
+            CK(cudaStreamEndCapture(stream_, &g));
+            CK(cudaGraphInstantiate(&graph_, g, 0));
+            cudaGraphDestroy(g);
+            graph_len_ = k;
+        }
+        CK(cudaGraphLaunch(graph_, stream_));
+        timing_.launches += (int64_t)k * (any_collide_ ? 3 : 2);
+        std::vector<int32_t> st(active_.size());
+        for (size_t i = 0; i < active_.size(); i++)
+            CK(cudaMemcpyAsync(&st[i], &d_ctl_[find(active_[i])->slot].status, 4, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        int nout = 0;
+        std::vector<int64_t> still;
+        for (size_t i = 0; i < active_.size(); i++) {
+            SimRec* r = find(active_[i]);
+            if (st[i] == SIM_RUNNING) { still.push_back(active_[i]); continue; }
+            if (int e = finish(r, st[i], err)) return e;
+            if (nout < max) out[nout++] = r->result;
+            release(r);
+        }
+        active_ = still;
+        return nout;
+    }
+
+    int result(int64_t id, SimResult* out, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        if (!r->retired) {
+            if (!r->resident) { *err = "simulation has not run"; return -7; }
+            if (int e = finish(r, r->status, err)) return e;
+            r->retired = false;
+        }
+        *out = r->result;
+        return 0;
+    }
+
+    int info(int64_t id, int* nv, int* nl, double* dt, double* t, int64_t* steps, int* status) override {
+        SimRec* r = find(id);
+        if (!r) return -6;
+        *nv = r->w.nv; *nl = r->w.nl;
+        *dt = r->dt; *t = 0; *steps = 0; *status = r->status;
+        if (r->resident) {
+            dev::Ctl c;
+            std::string e;
+            if (read_ctl(r->slot, &c, &e)) return -5;
+            *t = c.t; *steps = c.steps; *status = c.status; *dt = c.dt;
+        }
+        return 0;
+    }
+
+    int voxel_state(int64_t id, double* d13, float* f4, int32_t* flags, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        if (!r->resident) if (int e = upload(r, err)) return e;
+        const int nv = r->w.nv;
+        std::vector<double> buf(13 * (size_t)nv);
+        double* srcs[13] = {r->dsim.px, r->dsim.py, r->dsim.pz, r->dsim.mx, r->dsim.my, r->dsim.mz, r->dsim.qw, r->dsim.qx,
+                            r->dsim.qy, r->dsim.qz, r->dsim.ax, r->dsim.ay, r->dsim.az};
+        for (int k = 0; k < 13; k++) CK(cudaMemcpyAsync(buf.data() + (size_t)k * nv, srcs[k], 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        std::vector<float> tb((size_t)nv), ps(3 * (size_t)nv);
+        std::vector<uint32_t> fl((size_t)nv);
+        CK(cudaMemcpyAsync(tb.data(), r->dsim.temp, 4 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(ps.data(), r->dsim.ps, 12 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(fl.data(), r->dsim.vfl, 4 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (int i = 0; i < nv; i++) {
+            if (d13) for (int k = 0; k < 13; k++) d13[13 * (size_t)i + k] = buf[(size_t)k * nv + i];
+            if (f4) { f4[4 * (size_t)i] = tb[i]; for (int k = 0; k < 3; k++) f4[4 * (size_t)i + 1 + k] = ps[(size_t)k * nv + i]; }
+            if (flags) flags[i] = (int32_t)fl[i];
+        }
+        return 0;
+    }
+
+    int link_state(int64_t id, double* d9, float* f3, int32_t* flags, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        if (!r->resident) if (int e = upload(r, err)) return e;
+        const int nl = r->w.nl;
+        if (nl == 0) return 0;
+        std::vector<double> st(9 * (size_t)nl);
+        std::vector<float> sf(3 * (size_t)nl);
+        std::vector<uint8_t> fl((size_t)nl);
+        CK(cudaMemcpyAsync(st.data(), r->dsim.lst, 72 * (size_t)nl, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(sf.data(), r->dsim.lsf, 12 * (size_t)nl, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(fl.data(), r->dsim.lfl, nl, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (int i = 0; i < nl; i++) {
+            if (d9) for (int k = 0; k < 9; k++) d9[9 * (size_t)i + k] = st[(size_t)k * nl + i];
+            if (f3) for (int k = 0; k < 3; k++) f3[3 * (size_t)i + k] = sf[(size_t)k * nl + i];
+            if (flags) flags[i] = fl[i];
+        }
+        return 0;
+    }
+
+    int free_sim(int64_t id) override {
+        SimRec* r = find(id);
+        if (!r) return -6;
+        for (auto it = queue_.begin(); it != queue_.end(); ++it) if (*it == id) { queue_.erase(it); break; }
+        for (auto it = active_.begin(); it != active_.end(); ++it) if (*it == id) { active_.erase(it); break; }
+        release(r);
+        sims_.erase(id);
+        return 0;
+    }
+
+    const Timing& timing() const override { return timing_; }
+    void set_profiling(int on) override { profiling_ = on; }
+    size_t bytes_in_use() const override { return arena_.used; }
+    int device_check(std::string* err) override {
+        CK(cudaStreamSynchronize(stream_));
+        CK(cudaGetLastError());
+        return 0;
+    }
+    int set_tuning(int bl, int bv, int il, int iv, int gs) override {
+        if (bl > 0) block_links_ = std::min(256, bl);
+        if (bv > 0) block_voxels_ = std::min(256, std::max(32, bv & ~31));
+        if (il > 0) items_links_ = il;
+        if (iv > 0) items_voxels_ = iv;
+        if (gs > 0) graph_steps_ = gs;
+        batch_dirty_ = true;
+        return 0;
+    }
+    // Project autotuner: time a few graph replays of the batch for each candidate
+    // (block size, elements per work item) and keep the fastest.
+    int autotune(const int64_t* ids, int n, std::string* err) override {
+        std::vector<SimRec*> rs;
+        if (int e = prepare(ids, n, &rs, err)) return e;
+        std::vector<int> slots;
+        for (auto* r : rs) slots.push_back(r->slot);
+        struct Cand { int bl, bv, il, iv; };
+        const Cand cands[] = {{128, 128, 256, 128}, {128, 256, 512, 256}, {256, 256, 1024, 512}, {256, 256, 2048, 1024}, {128, 128, 1024, 512}};
+        double best = 1e30;
+        Cand bc = cands[2];
+        // snapshot the simulations' device regions so tuning does not advance them
+        std::vector<std::vector<char>> snap(rs.size());
+        std::vector<dev::Ctl> csnap(rs.size());
+        for (size_t i = 0; i < rs.size(); i++) {
+            snap[i].resize(rs[i]->bytes);
+            CK(cudaMemcpy(snap[i].data(), arena_base_ + rs[i]->off, rs[i]->bytes, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(&csnap[i], d_ctl_ + rs[i]->slot, sizeof(dev::Ctl), cudaMemcpyDeviceToHost));
+        }
+        std::vector<int64_t> tg(slots.size(), (int64_t)1 << 40);
+        for (const Cand& c : cands) {
+            block_links_ = c.bl; block_voxels_ = c.bv; items_links_ = c.il; items_voxels_ = c.iv;
+            if (int e = build_items(slots, err)) return e;
+            if (int e = set_running(slots, tg, err)) return e;
+            for (int w = 0; w < 2; w++) launch_step(stream_, false);
+            CK(cudaEventRecord(ev0_, stream_));
+            for (int k = 0; k < 8; k++) launch_step(stream_, false);
+            CK(cudaEventRecord(ev1_, stream_));
+            CK(cudaEventSynchronize(ev1_));
+            float ms;
+            cudaEventElapsedTime(&ms, ev0_, ev1_);
+            if (ms < best) { best = ms; bc = c; }
+        }
+        for (size_t i = 0; i < rs.size(); i++) {
+            CK(cudaMemcpy(arena_base_ + rs[i]->off, snap[i].data(), rs[i]->bytes, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_ctl_ + rs[i]->slot, &csnap[i], sizeof(dev::Ctl), cudaMemcpyHostToDevice));
+        }
+        block_links_ = bc.bl; block_voxels_ = bc.bv; items_links_ = bc.il; items_voxels_ = bc.iv;
+        batch_dirty_ = true;
+        return 0;
+    }
+};
+
+}  // namespace
+
+Engine* engine_create(int device, size_t budget, std::string* err) {
+    auto* e = new EngineImpl();
+    if (e->init(device, budget, err)) { delete e; return nullptr; }
+    return e;
+}
+void engine_destroy(Engine* e) { delete e; }
+
+}  // namespace gvx

@@ -1,0 +1,83 @@
+// GB300 step engine: device layout, batching and serving.  Host-side interface.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mathtree.h"
+#include "world.h"
+
+namespace gvx {
+
+enum SimStatus : int32_t {
+    SIM_IDLE = 0,       // loaded, not scheduled
+    SIM_RUNNING = 1,
+    SIM_DONE = 2,       // stop condition or horizon reached
+    SIM_DIVERGED = 3,   // a link strain exceeded 100 (Voxelyze3/src/old/Voxelyze.cpp:263-269)
+    SIM_ERROR = 4,      // contact list overflow or other device-detected error
+};
+
+enum RunMode : int32_t { MODE_PLAIN = 0, MODE_BATCHED = 1 };
+
+struct SimResult {
+    int64_t id;
+    int32_t status;
+    int32_t num_voxel;
+    int32_t num_measured_voxel;
+    int32_t num_close_pairs;
+    int64_t steps;
+    double current_time;
+    double fitness;
+    double vox_size;
+    double initial_com[3];
+    double current_com[3];
+    double total_distance;
+    double submit_s, start_s, finish_s;   // host wall clock (seconds since context creation)
+};
+
+struct Timing {
+    double device_ms = 0;        // CUDA-event time of the last run/step call on the context stream
+    double wall_ms = 0;
+    int64_t voxel_steps = 0;     // voxels x steps actually advanced
+    int64_t launches = 0;        // kernel launches issued by the last call (graph nodes counted)
+    double link_kernel_ms = 0;   // per-kernel CUDA-event times (profiling mode only)
+    double voxel_kernel_ms = 0;
+    double contact_kernel_ms = 0;
+};
+
+class Engine;
+Engine* engine_create(int device, size_t budget_bytes, std::string* err);
+void engine_destroy(Engine* e);
+
+class Engine {
+public:
+    virtual ~Engine() = default;
+    virtual int add_sim(const SimDesc& d, int64_t* id, std::string* err) = 0;
+    virtual int set_external(int64_t id, const External& x, std::string* err) = 0;
+    // Advance the given simulations by exactly `steps` steps each (fewer if they stop).
+    virtual int step(const int64_t* ids, int n, int mode, int64_t steps, std::string* err) = 0;
+    // Run the given simulations until their stop condition (or max_steps).
+    virtual int run(const int64_t* ids, int n, int mode, int64_t max_steps, std::string* err) = 0;
+    // Serving: queue a simulation with a step horizon; admitted as memory frees up.
+    virtual int submit(int64_t id, int64_t horizon_steps, std::string* err) = 0;
+    // Serving: advance everything admitted by one chunk, admit/retire; returns finished results.
+    virtual int poll(SimResult* out, int max, int chunk_steps, std::string* err) = 0;
+    virtual int pending() const = 0;
+    virtual int result(int64_t id, SimResult* out, std::string* err) = 0;
+    virtual int info(int64_t id, int* nv, int* nl, double* dt, double* t, int64_t* steps, int* status) = 0;
+    virtual int voxel_state(int64_t id, double* d13, float* f4, int32_t* flags, std::string* err) = 0;
+    virtual int link_state(int64_t id, double* d9, float* f3, int32_t* flags, std::string* err) = 0;
+    virtual int free_sim(int64_t id) = 0;
+    virtual const Timing& timing() const = 0;
+    virtual void set_profiling(int on) = 0;
+    virtual size_t bytes_in_use() const = 0;
+    virtual int device_check(std::string* err) = 0;
+    virtual int set_tuning(int block_links, int block_voxels, int items_links, int items_voxels, int graph_steps) = 0;
+    virtual int autotune(const int64_t* ids, int n, std::string* err) = 0;
+    virtual int64_t sim_bytes(const SimDesc& d) const = 0;
+};
+
+}  // namespace gvx

@@ -1,0 +1,594 @@
+// Step kernels.  One step of every running simulation is three launches
+// (links, contacts when any simulation collides, voxels).  Each launch is a
+// persistent-style grid whose blocks pull work items (simulation, element
+// range) from a queue with an atomic ticket, so thousands of uneven
+// simulations share one launch with no per-simulation launch overhead.
+#pragma once
+#include "physics.cuh"
+
+namespace gvx {
+namespace dev {
+
+constexpr float HB_TURN = 1.2f * 0.05f;   // HYSTERESIS_FACTOR*SA_BOND_BEND_RAD (types.h:57-58)
+constexpr float HB_EXT = 1.2f * 0.50f;    // HYSTERESIS_FACTOR*SA_BOND_EXT_PERC (types.h:57-59)
+
+__device__ __forceinline__ int claim(int* ticket, int* s_item) {
+    __syncthreads();
+    if (threadIdx.x == 0) *s_item = atomicAdd(ticket, 1);
+    __syncthreads();
+    return *s_item;
+}
+
+// CVX_Link::updateForces with orientLink, updateStrain and updateTransverseInfo
+// (Voxelyze3/src/old/VX_Link.cpp:72-113, 136-141, 143-241).  Writes the two
+// end forces/moments and axial strains into the voxels' direction slots.
+__device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool* diverged) {
+    const int ng = __ldg(S.lneg + l), pv = __ldg(S.lpos + l);
+    const int axis = __ldg(S.lax + l);
+    const LMat& m = S.lm[__ldg(S.lmt + l)];
+    const VMat& vN = S.vm[__ldg(S.vmat + ng)];
+    const VMat& vP = S.vm[__ldg(S.vmat + pv)];
+    const float tN = S.temp[ng], tP = S.temp[pv];
+    const double restLen = 0.5 * (base_size(vN, tN) + base_size(vP, tP));   // CVX_Link::updateRestLength
+    const int nl = S.nl;
+    double* st = S.lst;
+    const d3 o2 = D3(st[l], st[nl + l], st[2 * nl + l]);
+    const d3 oa1 = D3(st[3 * nl + l], st[4 * nl + l], st[5 * nl + l]);
+    const d3 oa2 = D3(st[6 * nl + l], st[7 * nl + l], st[8 * nl + l]);
+    float strain = S.lsf[l], maxStrain = S.lsf[nl + l], strainOffset = S.lsf[2 * nl + l];
+    uint8_t fl = S.lfl[l];
+    bool small = fl & LF_SMALL, lvv = fl & LF_LVV;
+
+    // orientLink
+    d3 pos2 = to_axis_x(axis, D3(S.px[pv] - S.px[ng], S.py[pv] - S.py[ng], S.pz[pv] - S.pz[ng]));
+    q4 angle1 = q_to_axis_x(axis, Q4(S.qw[ng], S.qx[ng], S.qy[ng], S.qz[ng]));
+    q4 angle2 = q_to_axis_x(axis, Q4(S.qw[pv], S.qx[pv], S.qy[pv], S.qz[pv]));
+    const q4 tr = Q4(angle1.w, -angle1.x, -angle1.y, -angle1.z);
+    pos2 = qrot(tr, pos2);
+    angle2 = qmul(tr, angle2);
+    angle1 = Q4(1, 0, 0, 0);
+    const float smallTurn = (float)((fabs(pos2.z) + fabs(pos2.y)) / pos2.x);
+    const float extendPerc = (float)(fabs(1 - pos2.x / restLen));
+    if (!small && smallTurn < 0.05f && extendPerc < 0.50f) { small = true; lvv = false; }
+    else if (small && (smallTurn > HB_TURN || extendPerc > HB_EXT)) { small = false; lvv = false; }
+    d3 a1v;
+    if (small) {
+        pos2.x -= restLen;
+        a1v = D3(0, 0, 0);                  // ToRotationVector of the identity
+    } else {
+        angle1 = q_from_angle_to_posx(angle1, pos2);
+        angle2 = qmul(angle1, angle2);
+        pos2 = D3(sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z) - restLen, 0, 0);
+        a1v = q_to_rotvec(angle1);
+    }
+    const d3 a2v = q_to_rotvec(angle2);
+    st[l] = pos2.x; st[nl + l] = pos2.y; st[2 * nl + l] = pos2.z;
+    st[3 * nl + l] = a1v.x; st[4 * nl + l] = a1v.y; st[5 * nl + l] = a1v.z;
+    st[6 * nl + l] = a2v.x; st[7 * nl + l] = a2v.y; st[8 * nl + l] = a2v.z;
+
+    // updateTransverseInfo (the CPU path refreshes it every step when nu != 0)
+    float A, tss;
+    if (m.nu != 0.0f) {
+        const int nv = S.nv;
+        float nx = S.ps[ng], ny = S.ps[nv + ng], nz = S.ps[2 * nv + ng];
+        float px_ = S.ps[pv], py_ = S.ps[nv + pv], pz_ = S.ps[2 * nv + pv];
+        float na, nb, pa, pb;
+        if (axis == 0) { na = ny; nb = nz; pa = py_; pb = pz_; }
+        else if (axis == 1) { na = nx; nb = nz; pa = px_; pb = pz_; }
+        else { na = nx; nb = ny; pa = px_; pb = py_; }
+        A = 0.5f * (voxel_tarea(vN, na, nb) + voxel_tarea(vP, pa, pb));
+        tss = 0.5f * (voxel_tss(vN, na, nb) + voxel_tss(vP, pa, pb));
+    } else {
+        A = 0.5f * (voxel_tarea(vN, 0.f, 0.f) + voxel_tarea(vP, 0.f, 0.f));
+        tss = 0.0f;
+    }
+
+    // updateStrain
+    const float axial = (float)(pos2.x / restLen);
+    float stress;
+    strain = axial;
+    if (m.linear) {
+        if (axial > maxStrain) maxStrain = axial;
+        stress = mat_stress(m, axial, tss, false);
+    } else if (axial > maxStrain) {
+        maxStrain = axial;
+        stress = mat_stress(m, axial, tss, false);
+        if (m.nu != 0.0f) strainOffset = maxStrain - mat_stress(m, axial, 0.0f, false) / (m.eHat * (1 - m.nu));
+        else strainOffset = maxStrain - stress / m.E;
+    } else {
+        const float rel = axial - strainOffset;
+        stress = (m.nu != 0.0f) ? mat_stress(m, rel, tss, true) : m.E * rel;
+    }
+    if (strain > 100) *diverged = true;
+    S.lsf[l] = strain; S.lsf[nl + l] = maxStrain; S.lsf[2 * nl + l] = strainOffset;
+
+    d3 fN, fP, mN, mP;
+    if (m.epsFail != -1.0f && maxStrain > m.epsFail) {
+        fN = fP = mN = mP = D3(0, 0, 0);
+    } else {
+        const float b1 = m.b1, b2 = m.b2, b3 = m.b3, a2 = m.a2;
+        fN = D3((double)(stress * A), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
+        fP = D3(-fN.x, -fN.y, -fN.z);
+        mN = D3(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (2 * a1v.y + a2v.y), b2 * pos2.y - b3 * (2 * a1v.z + a2v.z));
+        mP = D3(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
+        if (lvv) {
+            const d3 dP = D3(0.5 * (pos2.x - o2.x), 0.5 * (pos2.y - o2.y), 0.5 * (pos2.z - o2.z));
+            const d3 d1 = D3(0.5 * (a1v.x - oa1.x), 0.5 * (a1v.y - oa1.y), 0.5 * (a1v.z - oa1.z));
+            const d3 d2 = D3(0.5 * (a2v.x - oa2.x), 0.5 * (a2v.y - oa2.y), 0.5 * (a2v.z - oa2.z));
+            const float sqA1 = m.sqA1, sqA2xIp = m.sqA2xIp, sqB1 = m.sqB1, sqB2xFMp = m.sqB2xFMp, sqB3xIp = m.sqB3xIp;
+            const d3 pc = D3(sqA1 * dP.x, sqB1 * dP.y - sqB2xFMp * (d1.z + d2.z), sqB1 * dP.z + sqB2xFMp * (d1.y + d2.y));
+            const float dmN = vN.dampNum / dt, dmP = vP.dampNum / dt;   // CVX_Voxel::dampingMultiplier
+            fN = D3(fN.x + dmN * pc.x, fN.y + dmN * pc.y, fN.z + dmN * pc.z);
+            fP = D3(fP.x - dmP * pc.x, fP.y - dmP * pc.y, fP.z - dmP * pc.z);
+            const double hN = 0.5 * dmN, hP = 0.5 * dmP;
+            const d3 tN = D3(-sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (2 * d1.y + d2.y), -sqB2xFMp * dP.y + sqB3xIp * (2 * d1.z + d2.z));
+            const d3 tP = D3(sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (d1.y + 2 * d2.y), -sqB2xFMp * dP.y + sqB3xIp * (d1.z + 2 * d2.z));
+            mN = D3(mN.x - hN * tN.x, mN.y - hN * tN.y, mN.z - hN * tN.z);
+            mP = D3(mP.x - hP * tP.x, mP.y - hP * tP.y, mP.z - hP * tP.z);
+        } else {
+            lvv = true;
+        }
+        if (!small) {
+            fN = qrotinv(angle1, fN);
+            mN = qrotinv(angle1, mN);
+        }
+        fP = qrotinv(angle2, fP);
+        mP = qrotinv(angle2, mP);
+        fN = to_axis_orig(axis, fN); fP = to_axis_orig(axis, fP);
+        mN = to_axis_orig(axis, mN); mP = to_axis_orig(axis, mP);
+    }
+    S.lfl[l] = (uint8_t)((small ? LF_SMALL : 0) | (lvv ? LF_LVV : 0));
+
+    // direction slots: the negative-end voxel sees this link in direction 2*axis,
+    // the positive-end voxel in direction 2*axis+1 (CVX_Voxel::force, VX_Voxel.cpp:236-238)
+    const int nv = S.nv;
+    const int dn = 2 * axis, dp = 2 * axis + 1;
+    double* sf = S.sf;
+    double* sm = S.sm;
+    sf[(dn * 3 + 0) * nv + ng] = fN.x; sf[(dn * 3 + 1) * nv + ng] = fN.y; sf[(dn * 3 + 2) * nv + ng] = fN.z;
+    sm[(dn * 3 + 0) * nv + ng] = mN.x; sm[(dn * 3 + 1) * nv + ng] = mN.y; sm[(dn * 3 + 2) * nv + ng] = mN.z;
+    sf[(dp * 3 + 0) * nv + pv] = fP.x; sf[(dp * 3 + 1) * nv + pv] = fP.y; sf[(dp * 3 + 2) * nv + pv] = fP.z;
+    sm[(dp * 3 + 0) * nv + pv] = mP.x; sm[(dp * 3 + 1) * nv + pv] = mP.y; sm[(dp * 3 + 2) * nv + pv] = mP.z;
+    // CVX_Link::axialStrain(positiveEnd)  VX_Link.cpp:115-118
+    const float ratio = vP.E / vN.E;
+    S.ss[dn * nv + ng] = 2.0f * strain / (1.0f + ratio);
+    S.ss[dp * nv + pv] = 2.0f * strain * ratio / (1.0f + ratio);
+}
+
+__global__ void __launch_bounds__(256) k_links(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
+    __shared__ int s_item;
+    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; }
+    for (;;) {
+        const int it = claim(&tickets[0], &s_item);
+        if (it >= n_items) break;
+        const Item w = items[it];
+        Ctl& c = ctl[w.sim];
+        if (c.status != 1) continue;
+        const Sim& S = sims[w.sim];
+        const float dt = c.dt;
+        bool div = false;
+        for (int l = w.begin + threadIdx.x; l < w.end; l += blockDim.x) link_update(S, l, dt, &div);
+        if (div) c.diverged = 1;
+    }
+}
+
+// Overlap test and repelling force for one voxel pair (CVX_Collision::updateContactForce,
+// Voxelyze3/src/old/VX_Collision.cpp:17-23, 42-56).  a < b; returns false when apart.
+__device__ __forceinline__ bool pair_force(const Sim& S, int a, int b, float* f3) {
+    const VMat& ma = S.vm[__ldg(S.vmat + a)];
+    const VMat& mb = S.vm[__ldg(S.vmat + b)];
+    const float ox = (float)(S.px[b] - S.px[a]), oy = (float)(S.py[b] - S.py[a]), oz = (float)(S.pz[b] - S.pz[a]);
+    const float nomDist = (float)((base_size_avg(ma, S.temp[a]) + base_size_avg(mb, S.temp[b])) * S.env_radius);
+    const float len = sqrtf(ox * ox + oy * oy + oz * oz);
+    const float relDist = nomDist - len;
+    if (!(relDist > 0)) return false;
+    float ux = ox, uy = oy, uz = oz;
+    if (len > 0) { const float inv = 1.0f / len; ux = inv * ox; uy = inv * oy; uz = inv * oz; }
+    const double vax = S.mx[a] * ma.massInv, vay = S.my[a] * ma.massInv, vaz = S.mz[a] * ma.massInv;
+    const double vbx = S.mx[b] * mb.massInv, vby = S.my[b] * mb.massInv, vbz = S.mz[b] * mb.massInv;
+    const float rv = (float)((vax * (double)ux + vay * (double)uy + vaz * (double)uz) - (vbx * (double)ux + vby * (double)uy + vbz * (double)uz));
+    const float k = 2.0f / (1.0f / ma.penStiff + 1.0f / mb.penStiff);
+    const float cd = 0.5f * (ma.cDampT + mb.cDampT);
+    const float f = k * relDist + cd * rv;
+    f3[0] = f * ux; f3[1] = f * uy; f3[2] = f * uz;
+    return true;
+}
+
+__device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz, int mask) {
+    return ((uint32_t)cx * 73856093u ^ (uint32_t)cy * 19349663u ^ (uint32_t)cz * 83492791u) & (uint32_t)mask;
+}
+__device__ __forceinline__ int cell_of(double p, double cs) { return (int)floor(p / cs); }
+
+__device__ __forceinline__ void hash_insert(const Sim& S, int v, int parity) {
+    const double cs = S.cell_size;
+    const uint32_t h = cell_hash(cell_of(S.px[v], cs), cell_of(S.py[v], cs), cell_of(S.pz[v], cs), S.hash_size - 1);
+    int* head = S.hash_head + (size_t)parity * S.hash_size;
+    S.hash_next[v] = atomicExch(head + h, v);
+}
+
+// Spatial-hash broadphase + exact contact forces for one surface voxel.  The
+// reference keeps a conservative pair list of surface voxels that are not
+// within 5 lattice links of each other (Voxelyze3/src/old/Voxelyze.cpp:671-751,
+// VX_Voxel.cpp:394-417) and sums the pair forces in increasing partner order;
+// pairs that do not overlap contribute exactly zero, so summing the
+// overlapping pairs in partner order reproduces it.
+__device__ void voxel_contacts(const Sim& S, int v, int parity, int* err) {
+    const double cs = S.cell_size;
+    const int cx = cell_of(S.px[v], cs), cy = cell_of(S.py[v], cs), cz = cell_of(S.pz[v], cs);
+    const int nv = S.nv;
+    const int vx = S.ijk[v], vy = S.ijk[nv + v], vz = S.ijk[2 * nv + v];
+    const int* head = S.hash_head + (size_t)parity * S.hash_size;
+    int partners[kContactCap];
+    int np = 0;
+    bool overflow = false;
+    for (int dz = -1; dz <= 1; dz++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                const int tx = cx + dx, ty = cy + dy, tz = cz + dz;
+                int q = head[cell_hash(tx, ty, tz, S.hash_size - 1)];
+                int guard = 0;
+                while (q >= 0 && guard++ < nv) {
+                    const int nq = S.hash_next[q];
+                    if (q != v && cell_of(S.px[q], cs) == tx && cell_of(S.py[q], cs) == ty && cell_of(S.pz[q], cs) == tz) {
+                        // lattice exclusion: within 5 links of each other
+                        const int ox = S.ijk[q] - vx, oy = S.ijk[nv + q] - vy, oz = S.ijk[2 * nv + q] - vz;
+                        const int l1 = abs(ox) + abs(oy) + abs(oz);
+                        bool near = false;
+                        if (l1 <= 5) {
+                            // index of (ox,oy,oz) in the L1 ball enumerated z-major, then y, then x
+                            int k = 0;
+                            for (int zz = -5; zz < oz; zz++) { int r = 5 - abs(zz); k += (2 * r * r + 2 * r + 1); }
+                            const int r = 5 - abs(oz);
+                            for (int yy = -r; yy < oy; yy++) k += 2 * (r - abs(yy)) + 1;
+                            k += ox + (r - abs(oy));
+                            near = (S.reach[(size_t)v * kReachWords + (k >> 5)] >> (k & 31)) & 1u;
+                        }
+                        if (!near) {
+                            const int a = v < q ? v : q, b = v < q ? q : v;
+                            float f3[3];
+                            // cheap reject before the exact test
+                            if (pair_force(S, a, b, f3)) {
+                                if (np < kContactCap) {
+                                    int k = np++;
+                                    while (k > 0 && partners[k - 1] > q) { partners[k] = partners[k - 1]; k--; }
+                                    partners[k] = q;
+                                } else overflow = true;
+                            }
+                        }
+                    }
+                    q = nq;
+                }
+            }
+    if (overflow) atomicOr(err, 1);
+    float* out = S.cforce + (size_t)v * 3 * kContactCap;
+    for (int k = 0; k < np; k++) {
+        const int q = partners[k];
+        float f3[3];
+        pair_force(S, v < q ? v : q, v < q ? q : v, f3);
+        const float sgn = v < q ? 1.0f : -1.0f;   // contactForce(): +force on voxel1, -force on voxel2
+        out[3 * k] = sgn * f3[0]; out[3 * k + 1] = sgn * f3[1]; out[3 * k + 2] = sgn * f3[2];
+    }
+    S.ccount[v] = np;
+}
+
+__global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
+    __shared__ int s_item;
+    for (;;) {
+        const int it = claim(&tickets[1], &s_item);
+        if (it >= n_items) break;
+        const Item w = items[it];
+        Ctl& c = ctl[w.sim];
+        if (c.status != 1 || c.diverged) continue;
+        const Sim& S = sims[w.sim];
+        const int parity = c.hash_parity;
+        // clear the other table for the insertions made by this step's voxel update
+        int* other = S.hash_head + (size_t)(parity ^ 1) * S.hash_size;
+        const int per = (S.hash_size + S.nsurf - 1) / (S.nsurf > 0 ? S.nsurf : 1);
+        const int cb = w.begin * per, ce = min(S.hash_size, (w.end == S.nsurf) ? S.hash_size : w.end * per);
+        for (int h = cb + threadIdx.x; h < ce; h += blockDim.x) other[h] = -1;
+        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, &c.error);
+    }
+}
+
+// CVX_Voxel::timeStep with force(), moment() and floorForce()
+// (Voxelyze3/src/old/VX_Voxel.cpp:163-297), then the Poisson strain the next
+// step's links will read (CVX_Voxel::strain(true), :299-333) and the next
+// step's actuation temperature (VX3_VoxelyzeKernel.cu:625-650).
+__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, double t_next, int flags, double* com4, int* hash_next_table) {
+    const int nv = S.nv;
+    const VMat& m = S.vm[__ldg(S.vmat + v)];
+    uint32_t fl = S.vfl[v];
+    const Ext* e = (fl & VF_EXT) ? &S.ext[__ldg(S.vext + v)] : nullptr;
+    d3 pos = D3(S.px[v], S.py[v], S.pz[v]);
+    d3 lm = D3(S.mx[v], S.my[v], S.mz[v]);
+    q4 q = Q4(S.qw[v], S.qx[v], S.qy[v], S.qz[v]);
+    d3 am = D3(S.ax[v], S.ay[v], S.az[v]);
+    const float temp = S.temp[v];
+    bool fixed_all = false;
+    if (e && (e->dof & 0x3F) == 0x3F) {
+        fixed_all = true;
+        pos = D3(S.ijk[v] * m.nom + e->tr[0], S.ijk[nv + v] * m.nom + e->tr[1], S.ijk[2 * nv + v] * m.nom + e->tr[2]);
+        q = Q4(e->rq[0], e->rq[1], e->rq[2], e->rq[3]);
+        lm = am = D3(0, 0, 0);
+    } else {
+        // force()
+        d3 F = D3(0, 0, 0);
+        const double* sf = S.sf;
+#pragma unroll
+        for (int d = 0; d < 6; d++)
+            if (fl & (1u << d)) F = D3(F.x + sf[(d * 3) * nv + v], F.y + sf[(d * 3 + 1) * nv + v], F.z + sf[(d * 3 + 2) * nv + v]);
+        F = qrot(q, F);
+        if (e) { F.x += e->f[0]; F.y += e->f[1]; F.z += e->f[2]; }
+        const double vx = m.massInv * lm.x, vy = m.massInv * lm.y, vz = m.massInv * lm.z;
+        F = D3(F.x - m.gDampT * vx, F.y - m.gDampT * vy, F.z - m.gDampT * vz);
+        F.z += m.gravForce;
+        if (flags & SF_COLLIDE) {
+            const int nc = S.ccount[v];
+            const float* cf = S.cforce + (size_t)v * 3 * kContactCap;
+            for (int k = 0; k < nc; k++) { F.x -= cf[3 * k]; F.y -= cf[3 * k + 1]; F.z -= cf[3 * k + 2]; }
+        }
+        // floorForce()
+        const d3 F0 = F;
+        const bool floor = flags & SF_FLOOR;
+        if (floor) {
+            const float pen = (float)(base_size_avg(m, temp) / 2 - m.nom / 2 - pos.z);
+            if (pen >= 0) {
+                const float normal = m.penStiff * pen;
+                F.z += normal - m.cDampT * vz;
+                if (fl & VF_STATIC) {
+                    const float surf = (float)(F.x * F.x + F.y * F.y);
+                    const float fr = (m.mus * normal) * (m.mus * normal);
+                    if (surf > fr) fl &= ~VF_STATIC;
+                } else {
+                    const double hl = sqrt(vx * vx + vy * vy + 0.0 * 0.0);
+                    double nx = vx, ny = vy, nz = 0.0;
+                    if (hl > 0) { const double inv = 1.0 / hl; nx = inv * vx; ny = inv * vy; nz = inv * 0.0; }
+                    const float k = m.muk * normal;
+                    F = D3(F.x - k * nx, F.y - k * ny, F.z - k * nz);
+                }
+            } else {
+                fl &= ~VF_STATIC;
+            }
+        }
+        const d3 fric = D3(F.x - F0.x, F.y - F0.y, F.z - F0.z);
+        lm = D3(lm.x + dt * F.x, lm.y + dt * F.y, lm.z + dt * F.z);
+        const float sdt = dt * m.massInv;
+        d3 tr = D3(sdt * lm.x, sdt * lm.y, sdt * lm.z);
+        if (floor && (float)(base_size_avg(m, temp) / 2 - m.nom / 2 - pos.z) >= 0) {
+            const double work = fric.x * tr.x + fric.y * tr.y;
+            const double hKe = 0.5 * m.massInv * (lm.x * lm.x + lm.y * lm.y);
+            if (hKe + work <= 0) fl |= VF_STATIC;
+            if (fl & VF_STATIC) { lm.x = lm.y = 0; tr.x = tr.y = 0; }
+        } else {
+            fl &= ~VF_STATIC;
+        }
+        pos = D3(pos.x + tr.x, pos.y + tr.y, pos.z + tr.z);
+        // moment()
+        d3 M = D3(0, 0, 0);
+        const double* sm = S.sm;
+#pragma unroll
+        for (int d = 0; d < 6; d++)
+            if (fl & (1u << d)) M = D3(M.x + sm[(d * 3) * nv + v], M.y + sm[(d * 3 + 1) * nv + v], M.z + sm[(d * 3 + 2) * nv + v]);
+        M = qrot(q, M);
+        if (e) { M.x += e->m[0]; M.y += e->m[1]; M.z += e->m[2]; }
+        const double wx = m.Iinv * am.x, wy = m.Iinv * am.y, wz = m.Iinv * am.z;
+        M = D3(M.x - m.gDampR * wx, M.y - m.gDampR * wy, M.z - m.gDampR * wz);
+        am = D3(am.x + dt * M.x, am.y + dt * M.y, am.z + dt * M.z);
+        const float sI = dt * m.Iinv;
+        q = qmul(q_from_rotvec(D3(sI * am.x, sI * am.y, sI * am.z)), q);
+        if (e) {
+            const int d = e->dof;
+            if (d & 1) { pos.x = S.ijk[v] * m.nom + e->tr[0]; lm.x = 0; }
+            if (d & 2) { pos.y = S.ijk[nv + v] * m.nom + e->tr[1]; lm.y = 0; }
+            if (d & 4) { pos.z = S.ijk[2 * nv + v] * m.nom + e->tr[2]; lm.z = 0; }
+            if (d & 0x38) {
+                if ((d & 0x38) == 0x38) {
+                    q = Q4(e->rq[0], e->rq[1], e->rq[2], e->rq[3]);
+                    am = D3(0, 0, 0);
+                } else {
+                    d3 rv = q_to_rotvec(q);
+                    if (d & 8) { rv.x = 0; am.x = 0; }
+                    if (d & 16) { rv.y = 0; am.y = 0; }
+                    if (d & 32) { rv.z = 0; am.z = 0; }
+                    q = q_from_rotvec(rv);
+                }
+            }
+        }
+    }
+    S.px[v] = pos.x; S.py[v] = pos.y; S.pz[v] = pos.z;
+    S.mx[v] = lm.x; S.my[v] = lm.y; S.mz[v] = lm.z;
+    S.qw[v] = q.w; S.qx[v] = q.x; S.qy[v] = q.y; S.qz[v] = q.z;
+    S.ax[v] = am.x; S.ay[v] = am.y; S.az[v] = am.z;
+    S.vfl[v] = fl;
+    if (com4 && (fl & VF_MEASURED)) {
+        const double w = m.mass;
+        com4[0] += pos.x * w; com4[1] += pos.y * w; com4[2] += pos.z * w; com4[3] += w;
+    }
+    // CVX_Voxel::strain(true) for the next step (fully fixed voxels keep their cached value)
+    if (!fixed_all && m.nu != 0.0f) {
+        float s[3] = {0, 0, 0};
+        int nb[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < 6; d++)
+            if (fl & (1u << d)) { s[d >> 1] += S.ss[d * nv + v]; nb[d >> 1]++; }
+        bool ten[3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if (nb[i] == 2) s[i] *= 0.5f;
+            ten[i] = (nb[i] == 2) || (e && nb[i] == 1 && ((e->dof & (1 << i)) || e->f[i] != 0));
+        }
+        if (!(ten[0] && ten[1] && ten[2])) {
+            float add = 0;
+            for (int i = 0; i < 3; i++) if (ten[i]) add += s[i];
+            const float value = (float)pow((double)(1.0f + add), (double)(-m.nu)) - 1.0f;
+            for (int i = 0; i < 3; i++) if (!ten[i]) s[i] = value;
+        }
+        S.ps[v] = s[0]; S.ps[nv + v] = s[1]; S.ps[2 * nv + v] = s[2];
+    }
+    // actuation temperature for the next step
+    if (flags & SF_VARY) {
+        const float two_pi = 2 * 3.1415926f;
+        double T = S.temp_amp * sin((double)two_pi * (t_next / S.temp_period + __ldg(S.phase + v)));
+        if (!(flags & SF_EXPAND) && T > 0) T = 0;
+        S.temp[v] = (float)T;
+    }
+    if ((flags & SF_COLLIDE) && !(fl & VF_INTERIOR)) {
+        // insert into the table the next step's contact pass reads
+        const double cs = S.cell_size;
+        const uint32_t h = cell_hash(cell_of(pos.x, cs), cell_of(pos.y, cs), cell_of(pos.z, cs), S.hash_size - 1);
+        S.hash_next[v] = atomicExch(hash_next_table + h, v);
+    }
+}
+
+__device__ __forceinline__ double block_sum(double x, double* red) {
+    // fixed-order tree reduction (deterministic)
+    const int tid = threadIdx.x;
+    red[tid] = x;
+    __syncthreads();
+    for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+        if (tid < s) red[tid] = red[tid] + red[tid + s];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items,
+                                                int* tickets, double* partials) {
+    __shared__ int s_item, s_last;
+    __shared__ double red[256];
+    if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
+    for (;;) {
+        const int it = claim(&tickets[2], &s_item);
+        if (it >= n_items) break;
+        const Item w = items[it];
+        Ctl& c = ctl[w.sim];
+        if (c.status != 1) continue;
+        const Sim& S = sims[w.sim];
+        const bool div = c.diverged;
+        const float dt = c.dt;
+        const double t_next = c.t + dt;
+        const int64_t stepno = c.steps + 1;
+        const bool com_step = c.cycle_step > 0 && (stepno % c.cycle_step) == 0;
+        const int flags = S.flags;
+        int* hnext = (flags & SF_COLLIDE) ? S.hash_head + (size_t)(c.hash_parity ^ 1) * S.hash_size : nullptr;
+        double acc[4] = {0, 0, 0, 0};
+        if (!div && dt != 0.0f)
+            for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, t_next, flags, com_step ? acc : nullptr, hnext);
+        if (com_step) {
+            for (int k = 0; k < 4; k++) {
+                const double r = block_sum(acc[k], red);
+                if (threadIdx.x == 0) partials[(size_t)it * 4 + k] = r;
+            }
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = (atomicAdd(&c.done_items, 1) == c.n_vox_items - 1);
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            c.done_items = 0;
+            if (div) { c.status = 3; continue; }
+            if (c.error) { c.status = 4; continue; }
+            c.t = t_next;
+            c.steps = stepno;
+            if (flags & SF_COLLIDE) c.hash_parity ^= 1;
+            if (com_step) {
+                double s4[4] = {0, 0, 0, 0};
+                for (int k = 0; k < c.n_vox_items; k++)
+                    for (int j = 0; j < 4; j++) s4[j] += partials[(size_t)(c.item_begin + k) * 4 + j];
+                // VX3_VoxelyzeKernel::doTimeStep cycle sampling (VX3_VoxelyzeKernel.cu:314-334)
+                c.angle_samples++;
+                for (int j = 0; j < 3; j++) { c.com_hist[0][j] = c.com_hist[1][j]; c.com_hist[1][j] = c.com[j]; }
+                if (s4[3] == 0) { c.com[0] = c.com[1] = c.com[2] = 0; }
+                else for (int j = 0; j < 3; j++) c.com[j] = s4[j] / s4[3];
+                const double* A = c.com_hist[0];
+                const double* B = c.com_hist[1];
+                const double* C = c.com;
+                const bool eqBC = B[0] == C[0] && B[1] == C[1] && B[2] == C[2];
+                const bool eqAB = A[0] == B[0] && A[1] == B[1] && A[2] == B[2];
+                if (eqBC || eqAB || c.angle_samples < 3) c.recent_angle = 0;
+                else {
+                    const double bax = B[0] - A[0], bay = B[1] - A[1], baz = B[2] - A[2];
+                    const double cbx = C[0] - B[0], cby = C[1] - B[1], cbz = C[2] - B[2];
+                    c.recent_angle = acos((bax * cbx + bay * cby + baz * cbz) /
+                                          (sqrt(bax * bax + bay * bay + baz * baz) * sqrt(cbx * cbx + cby * cby + cbz * cbz)));
+                }
+            }
+            bool stop = c.target > 0 && stepno >= c.target;
+            if (c.stop.n > 0) {
+                MathVars mv;
+                mv.x = c.com[0]; mv.y = c.com[1]; mv.z = c.com[2]; mv.hit = 0; mv.t = c.t; mv.angle = c.recent_angle;
+                mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = S.nv;
+                if (mathtree_eval(c.stop, mv) > 0) stop = true;
+            }
+            if (stop) c.status = 2;
+        }
+    }
+}
+
+// Stable time step (CVoxelyze::recommendedTimeStep, Voxelyze3/src/old/Voxelyze.cpp:286-311,
+// with CVX_Link::axialStiffness, VX_Link.cpp:251-259): a warp-shuffle max over links.
+__global__ void k_dt(const Sim* __restrict__ sims, Ctl* ctl, int sim) {
+    const Sim& S = sims[sim];
+    float best = 0.0f;
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < S.nl; l += gridDim.x * blockDim.x) {
+        const int ng = S.lneg[l], pv = S.lpos[l];
+        const LMat& m = S.lm[S.lmt[l]];
+        const VMat& vN = S.vm[S.vmat[ng]];
+        const VMat& vP = S.vm[S.vmat[pv]];
+        float k;
+        if (m.nu == 0.0f) k = m.a1;
+        else {
+            const double rl = 0.5 * (base_size(vN, S.temp[ng]) + base_size(vP, S.temp[pv]));
+            const float A = 0.5f * (voxel_tarea(vN, 0.f, 0.f) + voxel_tarea(vP, 0.f, 0.f));
+            k = (float)(m.eHat * A / ((S.lsf[l] + 1) * rl));
+        }
+        const float m1 = vN.mass, m2 = vP.mass;
+        const float f2 = k / (m1 < m2 ? m1 : m2);
+        if (f2 > best) best = f2;
+    }
+    for (int o = 16; o > 0; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(&ctl[sim].maxf2_bits, __float_as_uint(best));
+}
+
+__global__ void k_init_temp(const Sim* __restrict__ sims, int sim, float initial) {
+    const Sim& S = sims[sim];
+    const float two_pi = 2 * 3.1415926f;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < S.nv; v += gridDim.x * blockDim.x) {
+        if (S.flags & SF_VARY) {
+            double T = S.temp_amp * sin((double)two_pi * (0.0 / S.temp_period + S.phase[v]));
+            if (!(S.flags & SF_EXPAND) && T > 0) T = 0;
+            S.temp[v] = (float)T;
+        } else {
+            S.temp[v] = initial;
+        }
+    }
+}
+
+__global__ void k_hash_build(const Sim* __restrict__ sims, Ctl* ctl, int sim) {
+    const Sim& S = sims[sim];
+    const int parity = ctl[sim].hash_parity;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nsurf; i += gridDim.x * blockDim.x) hash_insert(S, S.surf[i], parity);
+}
+
+// Mass-weighted centre of mass of measured voxels (VX3_VoxelyzeKernel::updateCurrentCenterOfMass,
+// VX3_VoxelyzeKernel.cu:477-493); one block, fixed order.
+__global__ void k_com(const Sim* __restrict__ sims, int sim, double* out4) {
+    __shared__ double red[256];
+    const Sim& S = sims[sim];
+    double a[4] = {0, 0, 0, 0};
+    for (int v = threadIdx.x; v < S.nv; v += blockDim.x) {
+        if (!(S.vfl[v] & VF_MEASURED)) continue;
+        const double w = S.vm[S.vmat[v]].mass;
+        a[0] += S.px[v] * w; a[1] += S.py[v] * w; a[2] += S.pz[v] * w; a[3] += w;
+    }
+    for (int k = 0; k < 4; k++) {
+        const double r = block_sum(a[k], red);
+        if (threadIdx.x == 0) out4[k] = r;
+    }
+}
+
+}  // namespace dev
+}  // namespace gvx

@@ -1,0 +1,257 @@
+// Device physics for the Voxelyze step, written for sm_103a.
+//
+// Each function restates one routine of the reference CPU Voxelyze
+// (Voxelyze3/src/old/*.cpp, cited per function) with the same operand types
+// (float vs double) and the same association order.  The file is compiled with
+// -fmad=false so that every multiply and add rounds on its own, as in the
+// reference built without floating-point contraction.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mathtree.h"
+
+namespace gvx {
+namespace dev {
+
+// ---------------------------------------------------------------- layouts
+constexpr int kContactCap = 32;       // contacts kept per voxel per step
+constexpr int kReachWords = 8;        // 231 offsets of the L1 ball of radius 5 -> 8 x 32 bits
+
+// voxel flag bits
+constexpr uint32_t VF_LINKS = 0x3Fu;      // bits 0..5: link present in direction d
+constexpr uint32_t VF_STATIC = 1u << 6;   // FLOOR_STATIC_FRICTION
+constexpr uint32_t VF_INTERIOR = 1u << 7; // all 6 links present
+constexpr uint32_t VF_EXT = 1u << 8;      // has an external
+constexpr uint32_t VF_MEASURED = 1u << 9;
+// link flag bits
+constexpr uint8_t LF_SMALL = 1;           // small-angle mode
+constexpr uint8_t LF_LVV = 2;             // LOCAL_VELOCITY_VALID
+
+// sim flag bits
+constexpr int SF_FLOOR = 1, SF_COLLIDE = 2, SF_VARY = 4, SF_EXPAND = 8;
+
+struct VMat {
+    float E, nu, cte, mus, muk, eHat;
+    float mass, massInv, Iinv;
+    float dampNum;      // 2*sqrtMass*zetaInternal   (numerator of dampingMultiplier)
+    float gDampT, gDampR, cDampT;   // zg*c2m, zg*c2i, zc*c2m
+    float gravForce;    // -mass*9.80665f*gravMult
+    float penStiff;     // (float)(2*E*nom)
+    float sizef;        // (float)nom
+    double nom;
+    int32_t measured;
+    int32_t pad;
+};
+
+struct LMat {
+    float E, nu, eHat, a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp, epsFail;
+    int32_t linear, n;
+    float strain[18], stress[18];
+};
+
+struct Ext {
+    int32_t dof;
+    float f[3], m[3];
+    double tr[3];
+    double rq[4];       // rotationQuat (w,x,y,z)
+};
+
+// Per-simulation device descriptor: pointers into the simulation's region.
+struct Sim {
+    int32_t nv, nl, nsurf, flags;
+    double temp_amp, temp_period;
+    double cell_size;           // spatial hash cell edge (m)
+    int32_t hash_size;          // buckets per table (power of two)
+    float env_radius;           // 0.625
+    const VMat* vm;
+    const LMat* lm;
+    const Ext* ext;
+    // voxel SoA (state)
+    double *px, *py, *pz, *mx, *my, *mz, *qw, *qx, *qy, *qz, *ax, *ay, *az;
+    float* temp;
+    float* ps;                  // poisson strain, 3 blocks of nv
+    uint32_t* vfl;
+    const uint8_t* vmat;
+    const int32_t* vext;
+    const double* phase;
+    // link -> voxel slots (direction d of voxel v): force (18 x nv), moment (18 x nv), axial strain (6 x nv)
+    double* sf;
+    double* sm;
+    float* ss;
+    // links
+    const int32_t *lneg, *lpos;
+    const uint8_t *lax, *lmt;
+    double* lst;                // 9 blocks of nl: pos2 xyz, angle1v xyz, angle2v xyz
+    float* lsf;                 // 3 blocks of nl: strain, maxStrain, strainOffset
+    uint8_t* lfl;
+    // collisions
+    const int32_t* surf;        // surface voxel ids (sorted)
+    const int16_t* ijk;         // lattice indices, 3 blocks of nv
+    const uint32_t* reach;      // kReachWords per voxel
+    int32_t* ccount;            // per voxel
+    float* cforce;              // 3*kContactCap per voxel
+    int32_t* hash_head;         // 2 tables of hash_size
+    int32_t* hash_next;         // per voxel
+};
+
+// Mutable per-simulation control block.
+struct Ctl {
+    double t;
+    float dt, optdt;
+    int32_t status, diverged, error, cycle_step;
+    int64_t steps, target;
+    int32_t done_items, n_vox_items, item_begin, angle_samples;
+    uint32_t maxf2_bits;
+    int32_t hash_parity;
+    double com[3], com_hist[2][3];
+    double recent_angle;
+    MathTree stop;
+};
+
+struct Item {
+    int32_t sim, begin, end, seq;
+};
+
+// ------------------------------------------------------------ small vector math
+struct d3 { double x, y, z; };
+struct q4 { double w, x, y, z; };
+
+__device__ __forceinline__ d3 D3(double x, double y, double z) { d3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ q4 Q4(double w, double x, double y, double z) { q4 r; r.w = w; r.x = x; r.y = y; r.z = z; return r; }
+
+// Quat3D::operator*  Voxelyze3/src/old/Quat3D.h:87
+__device__ __forceinline__ q4 qmul(const q4& a, const q4& f) {
+    return Q4(a.w * f.w - a.x * f.x - a.y * f.y - a.z * f.z,
+              a.w * f.x + a.x * f.w + a.y * f.z - a.z * f.y,
+              a.w * f.y - a.x * f.z + a.y * f.w + a.z * f.x,
+              a.w * f.z + a.x * f.y - a.y * f.x + a.z * f.w);
+}
+// Quat3D::RotateVec3D  Quat3D.h:174-181
+__device__ __forceinline__ d3 qrot(const q4& q, const d3& f) {
+    double tw = f.x * q.x + f.y * q.y + f.z * q.z;
+    double tx = f.x * q.w - f.y * q.z + f.z * q.y;
+    double ty = f.x * q.z + f.y * q.w - f.z * q.x;
+    double tz = -f.x * q.y + f.y * q.x + f.z * q.w;
+    return D3(q.w * tx + q.x * tw + q.y * tz - q.z * ty,
+              q.w * ty - q.x * tz + q.y * tw + q.z * tx,
+              q.w * tz + q.x * ty - q.y * tx + q.z * tw);
+}
+// Quat3D::RotateVec3DInv  Quat3D.h:192-199
+__device__ __forceinline__ d3 qrotinv(const q4& q, const d3& f) {
+    double tw = q.x * f.x + q.y * f.y + q.z * f.z;
+    double tx = q.w * f.x - q.y * f.z + q.z * f.y;
+    double ty = q.w * f.y + q.x * f.z - q.z * f.x;
+    double tz = q.w * f.z - q.x * f.y + q.y * f.x;
+    return D3(tw * q.x + tx * q.w + ty * q.z - tz * q.y,
+              tw * q.y - tx * q.z + ty * q.w + tz * q.x,
+              tw * q.z + tx * q.y - ty * q.x + tz * q.w);
+}
+// Quat3D::ToRotationVector  Quat3D.h:121-126
+__device__ __forceinline__ d3 q_to_rotvec(const q4& q) {
+    if (q.w >= 1.0 || q.w <= -1.0) return D3(0, 0, 0);
+    double sl = 1.0 - q.w * q.w;
+    if (sl < 2.4e-3) {
+        double s = sqrt((2 - 2 * q.w) / sl);
+        return D3((q.x * 2.0) * s, (q.y * 2.0) * s, (q.z * 2.0) * s);
+    }
+    double a = acos(q.w);
+    double inv = 1.0 / sqrt(sl);
+    return D3(((q.x * 2.0) * a) * inv, ((q.y * 2.0) * a) * inv, ((q.z * 2.0) * a) * inv);
+}
+// Quat3D::FromRotationVector  Quat3D.h:128-143
+__device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
+    double tx = 0.5 * v.x, ty = 0.5 * v.y, tz = 0.5 * v.z;
+    double m2 = tx * tx + ty * ty + tz * tz;
+    double w, s;
+    if (m2 * m2 < 5.328e-15) {
+        w = 1.0 - 0.5 * m2;
+        s = 1.0 - m2 / 6.0;
+    } else {
+        double m = sqrt(m2);
+        double sn, cs;
+        sincos(m, &sn, &cs);
+        w = cs;
+        s = sn / m;
+    }
+    return Q4(w, tx * s, ty * s, tz * s);
+}
+// Quat3D::FromAngleToPosX  Quat3D.h:145-170; `cur` is returned for a zero vector
+__device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r) {
+    if (r.x == 0 && r.y == 0 && r.z == 0) return cur;
+    double yox = r.y / r.x, zox = r.z / r.x;
+    if (yox < 1.732e-2 && yox > -1.732e-2 && zox < 1.732e-2 && zox > -1.732e-2) {
+        double y = 0.5 * zox, z = -0.5 * yox;
+        return Q4(1 + 0.5 * (-y * y - z * z), 0, y, z);
+    }
+    double l = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+    double nx = r.x, ny = r.y, nz = r.z;
+    if (l > 0) { double li = 1.0 / l; nx *= li; ny *= li; nz *= li; }
+    double theta = acos(nx);
+    if (theta > 3.14159265358979 - 1e-7) return Q4(0, 0, 1, 0);
+    double ami = 1.0 / sqrt(nz * nz + ny * ny);
+    double a = 0.5 * theta;
+    double sn, cs;
+    sincos(a, &sn, &cs);
+    return Q4(cs, 0, nz * ami * sn, -ny * ami * sn);
+}
+// CVX_Link::toAxisX / toAxisOriginal  Voxelyze3/src/old/VX_Link.h:106-111
+__device__ __forceinline__ d3 to_axis_x(int axis, const d3& v) {
+    if (axis == 1) return D3(v.y, -v.x, v.z);
+    if (axis == 2) return D3(v.z, v.y, -v.x);
+    return v;
+}
+__device__ __forceinline__ q4 q_to_axis_x(int axis, const q4& q) {
+    if (axis == 1) return Q4(q.w, q.y, -q.x, q.z);
+    if (axis == 2) return Q4(q.w, q.z, q.y, -q.x);
+    return q;
+}
+__device__ __forceinline__ d3 to_axis_orig(int axis, const d3& v) {
+    if (axis == 1) return D3(-v.y, v.x, v.z);
+    if (axis == 2) return D3(-v.z, v.y, v.x);
+    return v;
+}
+
+// CVX_Material::stress  Voxelyze3/src/old/VX_Material.cpp:182-212
+__device__ __forceinline__ float mat_stress(const LMat& m, float strain, float tss, bool forceLinear) {
+    if (m.epsFail != -1.0f && strain > m.epsFail) return 0.0f;
+    if (strain <= m.strain[1] || m.linear || forceLinear) {
+        if (m.nu == 0.0f) return m.E * strain;
+        return m.eHat * ((1 - m.nu) * strain + m.nu * tss);
+    }
+    int dc = m.n;
+    for (int i = 2; i < dc; i++) {
+        if (strain <= m.strain[i] || i == dc - 1) {
+            float perc = (strain - m.strain[i - 1]) / (m.strain[i] - m.strain[i - 1]);
+            float basic = m.stress[i - 1] + perc * (m.stress[i] - m.stress[i - 1]);
+            if (m.nu == 0.0f) return basic;
+            float mod = (m.stress[i] - m.stress[i - 1]) / (m.strain[i] - m.strain[i - 1]);
+            float modHat = mod / ((1 - 2 * m.nu) * (1 + m.nu));
+            float effS = basic / mod;
+            float effT = tss * (effS / strain);
+            return modHat * ((1 - m.nu) * effS + m.nu * effT);
+        }
+    }
+    return 0.0f;
+}
+
+// CVX_Voxel::baseSize(axis) and baseSizeAverage  Voxelyze3/src/old/VX_Voxel.h:91-92
+__device__ __forceinline__ double base_size(const VMat& m, float temp) { return (m.nom * 1.0) * (1 + temp * m.cte); }
+__device__ __forceinline__ double base_size_avg(const VMat& m, float temp) {
+    double b = base_size(m, temp);
+    return (b + b + b) / 3.0f;
+}
+// CVX_Voxel::transverseArea  VX_Voxel.cpp:360-373  (psa, psb: the two transverse Poisson strains)
+__device__ __forceinline__ float voxel_tarea(const VMat& m, float psa, float psb) {
+    float size = m.sizef;
+    if (m.nu == 0) return size * size;
+    return (float)(size * size * (1 + (double)psa) * (1 + (double)psb));
+}
+// CVX_Voxel::transverseStrainSum  VX_Voxel.cpp:345-358
+__device__ __forceinline__ float voxel_tss(const VMat& m, float psa, float psb) {
+    if (m.nu == 0) return 0;
+    return psa + psb;
+}
+
+}  // namespace dev
+}  // namespace gvx

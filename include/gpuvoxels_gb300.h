@@ -1,0 +1,167 @@
+/* gpuvoxels_gb300: GB300-native Voxelyze3 soft-body step engine, C ABI.
+ *
+ * Drop-in boundary for the reference's simulation path.  The reference has no
+ * plugin API; its boundary is the batch manager and per-simulation kernel object
+ * (reference paths relative to the liusida/gpuVoxels root):
+ *   - VX3_SimulationManager(sub_batches, base, input_dir, nDevices).start() -> h_results
+ *       Voxelyze3/src/VX3/VX3_SimulationManager.cuh:15-46, .cu:123-155
+ *   - VX3_VoxelyzeKernel(CVX_Sim*) + __device__ doTimeStep(float dt = -1)
+ *       Voxelyze3/src/VX3/VX3_VoxelyzeKernel.cuh:24-30, .cu:237-359
+ *   - the worker's report writer  Voxelyze3/src/Executables/vx3_node_worker.cu:98-141
+ * Each entry point below names the reference interface it replaces.
+ *
+ * Conventions: status codes are 0 (OK) or negative (VX3_E_*); the caller owns
+ * every buffer it passes; one context per host thread; calls on one context are
+ * not re-entrant; all device work of a context is ordered on its own stream.
+ * vx3_last_error() returns the message of the context's most recent failure.
+ */
+#ifndef GPUVOXELS_GB300_H
+#define GPUVOXELS_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VX3_OK 0
+#define VX3_E_PARSE (-1)      /* malformed VXA/VXD, unsupported feature */
+#define VX3_E_OOM_BUDGET (-2) /* the HBM budget of the context cannot hold the simulation */
+#define VX3_E_DIVERGED (-3)   /* reported in vx3_result.status, not returned */
+#define VX3_E_TIMEOUT (-4)
+#define VX3_E_CUDA (-5)
+#define VX3_E_ARG (-6)
+#define VX3_E_STATE (-7)
+
+/* vx3_result.status / vx3_sim_info.status */
+#define VX3_SIM_IDLE 0
+#define VX3_SIM_RUNNING 1
+#define VX3_SIM_DONE 2
+#define VX3_SIM_DIVERGED 3
+#define VX3_SIM_ERROR 4
+
+/* run modes */
+#define VX3_PLAIN 0   /* one simulation per launch, step by step (the reference's per-simulation form) */
+#define VX3_BATCHED 1 /* all listed simulations packed into shared launches, CUDA-graph captured */
+
+typedef struct vx3_ctx vx3_ctx;
+typedef int64_t vx3_sim_id;
+
+/* One finished simulation: the fields of VX3_SimulationResult
+ * (Voxelyze3/src/VX3/VX3_SimulationResult.h:4-33) plus serving timestamps. */
+typedef struct {
+    vx3_sim_id id;
+    int32_t status;
+    int32_t num_voxel;
+    int32_t num_measured_voxel;
+    int32_t num_close_pairs;
+    int64_t steps;
+    double current_time;
+    double fitness_score;
+    double vox_size;
+    double initial_center_of_mass[3];
+    double current_center_of_mass[3];
+    double total_distance_of_all_voxels;
+    double submit_time_s, start_time_s, finish_time_s;
+} vx3_result;
+
+typedef struct {
+    int32_t num_voxel;
+    int32_t num_link;
+    int32_t status;
+    int32_t pad;
+    double dt;
+    double current_time;
+    int64_t steps;
+} vx3_sim_info;
+
+/* Replaces VX3_SimulationManager construction (VX3_SimulationManager.cu:123-130) and its
+ * heap sizing (:384-396): reserves `hbm_budget_bytes` of device memory (0 = half of free). */
+vx3_ctx* vx3_create(int device, size_t hbm_budget_bytes);
+/* Replaces ~VX3_SimulationManager (VX3_SimulationManager.cu:131-136). */
+void vx3_destroy(vx3_ctx* ctx);
+const char* vx3_last_error(vx3_ctx* ctx);
+
+/* Replaces VX3_SimulationManager::readVXD for one file (VX3_SimulationManager.cu:277-380):
+ * merges the VXD into the base VXA (Utils/ctool.h:49-57), reads it, builds the
+ * voxel/link topology.  Host only; device memory is taken when the simulation first runs. */
+int vx3_load_vxa(vx3_ctx* ctx, const char* base_vxa_xml, const char* vxd_xml_or_null, const char* name, vx3_sim_id* out);
+
+/* Replaces CVX_Voxel::external() fixes/forces (Voxelyze3/src/old/VX_External.h:58-79):
+ * dof_fixed bits 0-2 fix x/y/z translation, 3-5 fix x/y/z rotation.  Before the first step only. */
+int vx3_set_external(vx3_ctx* ctx, vx3_sim_id id, int voxel, int dof_fixed, const float force[3], const float moment[3],
+                     const double translate[3], const double rotate[3]);
+
+/* Replaces VX3_SimulationManager::start() for a batch (VX3_SimulationManager.cu:138-155):
+ * runs every listed simulation until its StopConditionFormula holds (or max_steps, 0 = 1e6). */
+int vx3_run(vx3_ctx* ctx, const vx3_sim_id* ids, int n, int mode, int64_t max_steps);
+/* Replaces n calls of VX3_VoxelyzeKernel::doTimeStep() (VX3_VoxelyzeKernel.cu:237-359). */
+int vx3_step(vx3_ctx* ctx, const vx3_sim_id* ids, int n, int mode, int64_t steps);
+
+/* Serving pair (no reference counterpart beyond the dir-watch daemon, Executables/vx3_node_daemon.cu:16-66):
+ * submit queues a loaded simulation with a horizon in steps; poll admits queued simulations as
+ * the HBM budget allows, advances all admitted ones by `chunk_steps`, retires finished ones and
+ * returns up to `max` results (the count, or a negative status). */
+int vx3_submit(vx3_ctx* ctx, vx3_sim_id id, int64_t horizon_steps);
+int vx3_poll(vx3_ctx* ctx, vx3_result* out, int max, int chunk_steps);
+int vx3_pending(vx3_ctx* ctx);
+
+/* Replaces VX3_SimulationManager::collectResults for one simulation (VX3_SimulationManager.cu:416-458). */
+int vx3_get_result(vx3_ctx* ctx, vx3_sim_id id, vx3_result* out);
+int vx3_sim_info_get(vx3_ctx* ctx, vx3_sim_id id, vx3_sim_info* out);
+
+/* Voxel state in the reference's CVX_Voxel member layout (Voxelyze3/src/old/VX_Voxel.h:166-182):
+ * pos[3*nv], orient[4*nv] (w,x,y,z) and flags[nv]; any pointer may be NULL. */
+int vx3_get_state(vx3_ctx* ctx, vx3_sim_id id, double* pos, double* orient, uint8_t* flags);
+/* Full voxel state: d13 = pos3 linMom3 orient4 angMom3, f4 = temperature, poisson strain3, flags. */
+int vx3_get_voxel_state(vx3_ctx* ctx, vx3_sim_id id, double* d13, float* f4, int32_t* flags);
+/* Link state (CVX_Link, VX_Link.h:68-99): d9 = pos2 angle1v angle2v, f3 = strain maxStrain strainOffset, flags. */
+int vx3_get_link_state(vx3_ctx* ctx, vx3_sim_id id, double* d9, float* f3, int32_t* flags);
+
+/* Replaces the worker's report (Executables/vx3_node_worker.cu:98-141): report.inputdir,
+ * report.bestfit.{filename,fitness_score}, report.detail.<name>.{...}; results sorted by
+ * fitness with NaN last (VX3_SimulationResult.h:26-33). */
+int vx3_write_report(vx3_ctx* ctx, const vx3_sim_id* ids, int n, const char* input_dir, const char* path);
+
+/* Releases a simulation's device memory and host state. */
+int vx3_free_sim(vx3_ctx* ctx, vx3_sim_id id);
+
+/* Timing of the last vx3_run/vx3_step call on the context stream:
+ * out[0] device ms (CUDA events), out[1] wall ms, out[2] voxel-steps, out[3] kernel launches,
+ * out[4..6] link/contact/voxel kernel ms of the last profiled step. */
+int vx3_last_timing(vx3_ctx* ctx, double* out7);
+/* Tuning: threads per block and elements per work item for the link and voxel
+ * launches, and steps per captured graph; 0 keeps the current value. */
+int vx3_set_tuning(vx3_ctx* ctx, int block_links, int block_voxels, int items_links, int items_voxels, int graph_steps);
+/* Times candidate launch shapes on the given simulations (state restored afterwards) and keeps the fastest. */
+int vx3_autotune(vx3_ctx* ctx, const vx3_sim_id* ids, int n);
+int vx3_set_profiling(vx3_ctx* ctx, int on);
+/* Device bytes a loaded simulation needs when resident (for HBM-budget admission). */
+int64_t vx3_sim_bytes(vx3_ctx* ctx, vx3_sim_id id);
+size_t vx3_bytes_in_use(vx3_ctx* ctx);
+
+/* Host-only inspection (no device, no context): reads a VXA (+VXD) the way vx3_load_vxa does and
+ * reports what the engine would simulate.  Replaces reading CVX_Sim/CVoxelyze members after
+ * CVX_Sim::Import (Voxelyze3/src/VXA/VX_Sim.cpp:59-153).
+ *   counts[6] = voxels, links, voxel materials, link materials, surface voxels, externals
+ *   env[12]   = voxel size, DtFrac, gravity (g), floor, collisions, vary temperature, amplitude,
+ *               period, expansion, initial temperature, bounding radius, watch distance
+ * Returns VX3_OK or VX3_E_PARSE (message in err, up to err_len bytes). */
+int vx3_inspect_vxa(const char* base_vxa_xml, const char* vxd_xml_or_null, int32_t* counts, double* env, char* err, int err_len);
+/* Topology and derived constants, sized from vx3_inspect_vxa counts; any pointer may be NULL.
+ *   vox4[4*nv]  = ix, iy, iz, material;  lnk4[4*nl] = negative voxel, positive voxel, axis, link material
+ *   phase[nv]; vmat18[18*nvm] and vnom[nvm] in CVX_MaterialVoxel order (E, nu, rho, cte, muStatic, muKinetic,
+ *   zetaInternal, zetaGlobal, zetaCollision, eHat, mass, 1/mass, sqrt(mass), inertia, 1/inertia,
+ *   2sqrt(mEs), 2sqrt(IEs^3), gravity); lidx2[2*nlm] constituent voxel materials;
+ *   lmat20[20*nlm] = E, nu, eHat, a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp,
+ *   sigmaYield, sigmaFail, epsYield, epsFail, linear, nomSize, rho. */
+int vx3_inspect_topology(const char* base_vxa_xml, const char* vxd_xml_or_null, int32_t* vox4, int32_t* lnk4, double* phase,
+                         float* vmat18, double* vnom, int32_t* lidx2, float* lmat20);
+/* Stop/fitness formula evaluation as the engine performs it (Utils/VX3_MathTree.h:50-192);
+ * which: 0 stop condition, 1 fitness.  vars = x, y, z, hit, t, angle, closeness, numClosePairs, num_voxel. */
+int vx3_inspect_formula(const char* base_vxa_xml, const char* vxd_xml_or_null, int which, const double* vars9, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
