@@ -24,6 +24,7 @@ import numpy as np
 from . import build as _build
 
 PLAIN, BATCHED = 0, 1
+EXACT, FMA = 0, 1
 SIM_IDLE, SIM_RUNNING, SIM_DONE, SIM_DIVERGED, SIM_ERROR = range(5)
 ERRORS = {-1: "VX3_E_PARSE", -2: "VX3_E_OOM_BUDGET", -3: "VX3_E_DIVERGED", -4: "VX3_E_TIMEOUT", -5: "VX3_E_CUDA",
           -6: "VX3_E_ARG", -7: "VX3_E_STATE"}
@@ -32,7 +33,7 @@ ERRORS = {-1: "VX3_E_PARSE", -2: "VX3_E_OOM_BUDGET", -3: "VX3_E_DIVERGED", -4: "
 EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_set_external", "vx3_run", "vx3_step",
            "vx3_submit", "vx3_poll", "vx3_pending", "vx3_get_result", "vx3_sim_info_get", "vx3_get_state",
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
-           "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_sim_bytes", "vx3_bytes_in_use",
+           "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula"]
 
 
@@ -80,7 +81,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_get_state": (I, [P, I64, P, P, P]), "vx3_get_voxel_state": (I, [P, I64, P, P, P]),
         "vx3_get_link_state": (I, [P, I64, P, P, P]), "vx3_write_report": (I, [P, P, I, S, S]),
         "vx3_free_sim": (I, [P, I64]), "vx3_last_timing": (I, [P, P]), "vx3_set_tuning": (I, [P, I, I, I, I, I]),
-        "vx3_autotune": (I, [P, P, I]), "vx3_set_profiling": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
+        "vx3_autotune": (I, [P, P, I]), "vx3_set_profiling": (I, [P, I]), "vx3_set_precision": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
         "vx3_bytes_in_use": (ctypes.c_size_t, [P]),
         "vx3_inspect_vxa": (I, [S, S, P, P, ctypes.c_char_p, I]),
         "vx3_inspect_topology": (I, [S, S, P, P, P, P, P, P, P]),
@@ -253,6 +254,13 @@ class Context:
 
     def set_profiling(self, on: bool):
         self.L.vx3_set_profiling(self.h, int(on))
+
+    def set_precision(self, mode: int):
+        """EXACT (default, the reference's rounding) or FMA (contracted multiply-adds)."""
+        self._check(self.L.vx3_set_precision(self.h, mode))
+
+    def sim_bytes(self, sim: int) -> int:
+        return self._check(self.L.vx3_sim_bytes(self.h, sim))
 
     def bytes_in_use(self) -> int:
         return int(self.L.vx3_bytes_in_use(self.h))

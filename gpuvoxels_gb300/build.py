@@ -21,7 +21,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgpuvoxels_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "world.cpp", "xml_dom.cpp", "capi.cpp"]
+SOURCES = ["kernels_exact.cu", "kernels_fast.cu", "engine.cu", "world.cpp", "xml_dom.cpp", "capi.cpp"]
 
 
 def nvcc() -> str:
@@ -35,7 +35,8 @@ def _flags(src: str):
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", CSRC,
               "-I", os.path.join(HERE, "..", "include")]
     if src.endswith(".cu"):
-        return common + ARCH + ["-lineinfo", "-fmad=false", "-Xptxas", "-warn-spills"]
+        fmad = "-fmad=true" if src == "kernels_fast.cu" else "-fmad=false"
+        return common + ARCH + ["-lineinfo", fmad, "-Xptxas", "-warn-spills"]
     return common
 
 

@@ -277,8 +277,13 @@ int vx3_set_profiling(vx3_ctx* c, int on) {
 
 int64_t vx3_sim_bytes(vx3_ctx* c, vx3_sim_id id) {
     if (!c) return VX3_E_ARG;
-    (void)id;
-    return -1;
+    int64_t b = c->eng->sim_bytes_id(id);
+    return b < 0 ? fail(c, VX3_E_ARG, "unknown simulation id") : b;
+}
+
+int vx3_set_precision(vx3_ctx* c, int mode) {
+    if (!c || (mode != VX3_EXACT && mode != VX3_FMA)) return fail(c, VX3_E_ARG, "precision must be VX3_EXACT or VX3_FMA");
+    return c->eng->set_precision(mode == VX3_FMA);
 }
 
 size_t vx3_bytes_in_use(vx3_ctx* c) { return c ? c->eng->bytes_in_use() : 0; }

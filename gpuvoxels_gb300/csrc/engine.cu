@@ -1,7 +1,8 @@
 // GB300 step engine: HBM arena, per-simulation upload, batched stepping with
 // work queues captured in CUDA graphs, and the continuous-batching serving loop.
 #include "engine.h"
-#include "kernels.cuh"
+#include "kernelset.h"
+#include "layout.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -107,9 +108,11 @@ public:
     double* d_partials_ = nullptr;
     double* d_com4_ = nullptr;
     // tuning
-    int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 512, graph_steps_ = 64;
+    int block_links_ = 256, block_voxels_ = 256, items_links_ = 256, items_voxels_ = 256, graph_steps_ = 64;
     int sm_count_ = 152;
     int profiling_ = 0;
+    KernelSet ks_ = kernelset_exact();
+    int64_t exact_steps_ = -1;     // >= 0 while step() advances a known number of steps
     Timing timing_;
     double t0_ = now_s();
     // serving
@@ -189,6 +192,17 @@ public:
         if (!build_world(d, &w, &e)) return -1;
         return sim_bytes_world(w);
     }
+    int64_t sim_bytes_id(int64_t id) override {
+        SimRec* r = find(id);
+        return r ? sim_bytes_world(r->w) : -6;
+    }
+    int set_precision(int fma) override {
+        ks_ = fma ? kernelset_fast() : kernelset_exact();
+        if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        batch_dirty_ = true;
+        return 0;
+    }
+    int precision() const override { return ks_.name[0] == 'f' ? 1 : 0; }
 
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
@@ -427,15 +441,15 @@ public:
         CK(cudaMemcpyAsync(d_ctl_ + slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
         // first actuation temperature (t = 0), then the stable step from it
         int g = std::min(4 * sm_count_, (int)((nv + 255) / 256));
-        dev::k_init_temp<<<std::max(1, g), 256, 0, stream_>>>(d_sims_, slot, w.desc.initial_temp);
+        ks_.init_temp(std::max(1, g), stream_, d_sims_, slot, w.desc.initial_temp);
         CK(cudaGetLastError());
         if (nl > 0) {
             int gl = std::min(4 * sm_count_, (int)((nl + 255) / 256));
-            dev::k_dt<<<std::max(1, gl), 256, 0, stream_>>>(d_sims_, d_ctl_, slot);
+            ks_.dt(std::max(1, gl), stream_, d_sims_, d_ctl_, slot);
             CK(cudaGetLastError());
         }
         if (w.desc.collisions && w.surface_count > 0) {
-            dev::k_hash_build<<<std::max(1, std::min(4 * sm_count_, (w.surface_count + 255) / 256)), 256, 0, stream_>>>(d_sims_, d_ctl_, slot);
+            ks_.hash_build(std::max(1, std::min(4 * sm_count_, (w.surface_count + 255) / 256)), stream_, d_sims_, d_ctl_, slot);
             CK(cudaGetLastError());
         }
         uint32_t bits = 0;
@@ -536,12 +550,12 @@ public:
         const dev::Item* ci = d_items_ + n_link_items_;
         const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
         if (prof) cudaEventRecord(evk_[0], st);
-        dev::k_links<<<grid_for(n_link_items_, block_links_), block_links_, 0, st>>>(d_sims_, d_ctl_, li, n_link_items_, d_tickets_);
+        ks_.links(grid_for(n_link_items_, block_links_), block_links_, st, d_sims_, d_ctl_, li, n_link_items_, d_tickets_);
         if (prof) cudaEventRecord(evk_[1], st);
-        if (any_collide_) dev::k_contacts<<<grid_for(n_contact_items_, 128), 128, 0, st>>>(d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
+        if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (prof) cudaEventRecord(evk_[2], st);
-        dev::k_voxels<<<grid_for(n_vox_items_, block_voxels_), block_voxels_, 0, st>>>(d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_,
-                                                                                      d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
+        ks_.voxels(grid_for(n_vox_items_, block_voxels_), block_voxels_, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_,
+                   d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
         if (prof) cudaEventRecord(evk_[3], st);
     }
 
@@ -576,6 +590,10 @@ public:
             for (size_t i = 0; i < rs.size(); i++) {
                 std::vector<int> one{rs[i]->slot};
                 if (int e = build_items(one, err)) return e;
+                if (exact_steps_ >= 0) {
+                    for (int64_t k = 0; k < exact_steps_; k++) { launch_step(stream_, false); timing_.launches += any_collide_ ? 3 : 2; }
+                    continue;
+                }
                 for (;;) {
                     for (int k = 0; k < 16; k++) { launch_step(stream_, false); timing_.launches += any_collide_ ? 3 : 2; }
                     dev::Ctl c;
@@ -602,23 +620,41 @@ public:
                 cudaGraphDestroy(g);
                 graph_len_ = graph_steps_;
             }
-            for (;;) {
-                if (profiling_) {
-                    launch_step(stream_, true);
-                    timing_.launches += any_collide_ ? 3 : 2;
-                } else {
-                    CK(cudaGraphLaunch(graph_, stream_));
-                    timing_.launches += (int64_t)graph_len_ * (any_collide_ ? 3 : 2);
+            const int per_step = any_collide_ ? 3 : 2;
+            if (exact_steps_ >= 0) {
+                // a known step count: whole graphs, then single steps for the remainder, no polling
+                int64_t left = exact_steps_;
+                while (left > 0) {
+                    if (!profiling_ && left >= graph_len_) {
+                        CK(cudaGraphLaunch(graph_, stream_));
+                        timing_.launches += (int64_t)graph_len_ * per_step;
+                        left -= graph_len_;
+                    } else {
+                        launch_step(stream_, profiling_ != 0);
+                        timing_.launches += per_step;
+                        left -= 1;
+                    }
                 }
-                bool running = false;
-                // poll a compact status array
-                for (auto* r : rs) {
-                    int32_t st;
-                    CK(cudaMemcpyAsync(&st, &d_ctl_[r->slot].status, 4, cudaMemcpyDeviceToHost, stream_));
+            } else {
+                int lo = INT32_MAX, hi = -1;
+                for (auto* r : rs) { lo = std::min(lo, r->slot); hi = std::max(hi, r->slot); }
+                std::vector<int32_t> st((size_t)(hi - lo + 1));
+                for (;;) {
+                    if (profiling_) {
+                        launch_step(stream_, true);
+                        timing_.launches += per_step;
+                    } else {
+                        CK(cudaGraphLaunch(graph_, stream_));
+                        timing_.launches += (int64_t)graph_len_ * per_step;
+                    }
+                    // one strided copy of every status word, then a single synchronisation
+                    CK(cudaMemcpy2DAsync(st.data(), sizeof(int32_t), &d_ctl_[lo].status, sizeof(dev::Ctl), sizeof(int32_t),
+                                         (size_t)(hi - lo + 1), cudaMemcpyDeviceToHost, stream_));
                     CK(cudaStreamSynchronize(stream_));
-                    if (st == SIM_RUNNING) { running = true; break; }
+                    bool running = false;
+                    for (auto* r : rs) if (st[(size_t)(r->slot - lo)] == SIM_RUNNING) { running = true; break; }
+                    if (!running) break;
                 }
-                if (!running) break;
             }
         }
         CK(cudaEventRecord(ev1_, stream_));
@@ -669,23 +705,31 @@ public:
         if (slots.empty()) return 0;
         // the stop formula is not applied by step(): clear it for the call, restore afterwards
         std::vector<MathTree> saved(slots.size());
+        MathTree none;
+        none.n = 0;
         for (size_t i = 0; i < slots.size(); i++) {
-            CK(cudaMemcpy(&saved[i], &d_ctl_[slots[i]].stop, sizeof(MathTree), cudaMemcpyDeviceToHost));
-            MathTree none;
-            none.n = 0;
-            CK(cudaMemcpy(&d_ctl_[slots[i]].stop, &none, sizeof(MathTree), cudaMemcpyHostToDevice));
+            CK(cudaMemcpyAsync(&saved[i], &d_ctl_[slots[i]].stop, sizeof(MathTree), cudaMemcpyDeviceToHost, stream_));
+            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].stop, &none, sizeof(MathTree), cudaMemcpyHostToDevice, stream_));
         }
+        CK(cudaStreamSynchronize(stream_));
         if (int e = set_running(slots, targets, err)) return e;
         std::vector<SimRec*> act;
         for (auto* r : rs) if (std::find(slots.begin(), slots.end(), r->slot) != slots.end()) act.push_back(r);
+        exact_steps_ = steps;
         int e = drive(act, mode, err);
-        for (size_t i = 0; i < slots.size(); i++) cudaMemcpy(&d_ctl_[slots[i]].stop, &saved[i], sizeof(MathTree), cudaMemcpyHostToDevice);
-        for (auto* r : act) {
-            int32_t st;
-            cudaMemcpy(&st, &d_ctl_[r->slot].status, 4, cudaMemcpyDeviceToHost);
-            if (st == SIM_DONE) { st = SIM_IDLE; cudaMemcpy(&d_ctl_[r->slot].status, &st, 4, cudaMemcpyHostToDevice); }
-            r->status = st;
+        exact_steps_ = -1;
+        for (size_t i = 0; i < slots.size(); i++)
+            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].stop, &saved[i], sizeof(MathTree), cudaMemcpyHostToDevice, stream_));
+        std::vector<int32_t> st(act.size());
+        for (size_t i = 0; i < act.size(); i++)
+            CK(cudaMemcpyAsync(&st[i], &d_ctl_[act[i]->slot].status, 4, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        const int32_t idle = SIM_IDLE;
+        for (size_t i = 0; i < act.size(); i++) {
+            if (st[i] == SIM_DONE) { st[i] = SIM_IDLE; CK(cudaMemcpyAsync(&d_ctl_[act[i]->slot].status, &idle, 4, cudaMemcpyHostToDevice, stream_)); }
+            act[i]->status = st[i];
         }
+        CK(cudaStreamSynchronize(stream_));
         return e;
     }
 
@@ -718,7 +762,7 @@ public:
     }
 
     int com(SimRec* r, double* out, std::string* err) {
-        dev::k_com<<<1, 256, 0, stream_>>>(d_sims_, r->slot, d_com4_);
+        ks_.com(stream_, d_sims_, r->slot, d_com4_);
         CK(cudaGetLastError());
         double c4[4];
         CK(cudaMemcpyAsync(c4, d_com4_, sizeof(c4), cudaMemcpyDeviceToHost, stream_));

@@ -78,6 +78,10 @@ public:
     virtual int set_tuning(int block_links, int block_voxels, int items_links, int items_voxels, int graph_steps) = 0;
     virtual int autotune(const int64_t* ids, int n, std::string* err) = 0;
     virtual int64_t sim_bytes(const SimDesc& d) const = 0;
+    virtual int64_t sim_bytes_id(int64_t id) = 0;
+    // 0: exact build (no contraction, the reference's rounding); 1: FMA build
+    virtual int set_precision(int fma) = 0;
+    virtual int precision() const = 0;
 };
 
 }  // namespace gvx

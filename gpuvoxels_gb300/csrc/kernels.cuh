@@ -7,7 +7,7 @@
 #include "physics.cuh"
 
 namespace gvx {
-namespace dev {
+namespace GVX_KNS {
 
 constexpr float HB_TURN = 1.2f * 0.05f;   // HYSTERESIS_FACTOR*SA_BOND_BEND_RAD (types.h:57-58)
 constexpr float HB_EXT = 1.2f * 0.50f;    // HYSTERESIS_FACTOR*SA_BOND_EXT_PERC (types.h:57-59)
@@ -590,5 +590,23 @@ __global__ void k_com(const Sim* __restrict__ sims, int sim, double* out4) {
     }
 }
 
-}  // namespace dev
+}  // namespace GVX_KNS
+}  // namespace gvx
+
+// ---------------------------------------------------------------- launch table
+namespace gvx {
+namespace GVX_KNS {
+inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_links<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
+inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
+inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk, double* p) {
+    k_voxels<<<g, b, 0, s>>>(sims, ctl, it, n, tk, p);
+}
+inline void l_dt(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, int sim) { k_dt<<<g, 256, 0, s>>>(sims, ctl, sim); }
+inline void l_init_temp(int g, cudaStream_t s, const Sim* sims, int sim, float t0) { k_init_temp<<<g, 256, 0, s>>>(sims, sim, t0); }
+inline void l_hash_build(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, int sim) { k_hash_build<<<g, 256, 0, s>>>(sims, ctl, sim); }
+inline void l_com(cudaStream_t s, const Sim* sims, int sim, double* out4) { k_com<<<1, 256, 0, s>>>(sims, sim, out4); }
+inline KernelSet make_kernelset(const char* name) {
+    return KernelSet{name, l_links, l_contacts, l_voxels, l_dt, l_init_temp, l_hash_build, l_com};
+}
+}  // namespace GVX_KNS
 }  // namespace gvx

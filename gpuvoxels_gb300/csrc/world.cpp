@@ -444,7 +444,9 @@ float strain_of(const VoxelMaterial* m, float stress) {
 VoxelMaterial make_voxel_material(const PaletteMaterial& p, const SimDesc& d) {
     VoxelMaterial m;
     m.nu = 0.0f; m.rho = 1.0f; m.cte = 0.0f; m.mus = 0.0f; m.muk = 0.0f; m.zi = 1.0f; m.zg = 0.0f; m.zc = 0.0f;
-    set_linear(&m, 1.0f, -1.0f);
+    // CVoxelyze::addMaterial() starts from CVX_MaterialVoxel(1e6, 1e3); a model setter that rejects
+    // its arguments (e.g. bilinear with Fail_Stress <= Yield_Stress) leaves this linear model in place.
+    set_linear(&m, 1e6f, -1.0f);
     switch (p.model) {
     case 0: set_linear(&m, (float)p.E, -1.0f); break;
     case 1: set_linear(&m, (float)p.E, (float)p.fail_stress); break;

@@ -136,6 +136,13 @@ int vx3_set_tuning(vx3_ctx* ctx, int block_links, int block_voxels, int items_li
 /* Times candidate launch shapes on the given simulations (state restored afterwards) and keeps the fastest. */
 int vx3_autotune(vx3_ctx* ctx, const vx3_sim_id* ids, int n);
 int vx3_set_profiling(vx3_ctx* ctx, int on);
+/* Kernel build used by the context (no reference counterpart: the reference has one GPU build).
+ * VX3_EXACT (default): every FP64/FP32 multiply and add rounded separately, as the reference's CPU path.
+ * VX3_FMA: multiply-add pairs contracted into FMAs; fewer FP64 instructions, results within the
+ * parity tolerance of the reference rather than bit-faithful to its rounding. */
+#define VX3_EXACT 0
+#define VX3_FMA 1
+int vx3_set_precision(vx3_ctx* ctx, int mode);
 /* Device bytes a loaded simulation needs when resident (for HBM-budget admission). */
 int64_t vx3_sim_bytes(vx3_ctx* ctx, vx3_sim_id id);
 size_t vx3_bytes_in_use(vx3_ctx* ctx);

@@ -450,6 +450,11 @@ class RefSim:
             RefSim._lib.vxref_free(self.h)
             self.h = None
 
+    def set_external(self, voxel, dof_fixed=0, force=(0, 0, 0), moment=(0, 0, 0), translate=(0, 0, 0), rotate=(0, 0, 0)):
+        f = np.asarray(force, np.float32); m = np.asarray(moment, np.float32)
+        t = np.asarray(translate, np.float64); r = np.asarray(rotate, np.float64)
+        RefSim._lib.vxref_set_external(self.h, int(voxel), int(dof_fixed), _p(f), _p(m), _p(t), _p(r))
+
     def step(self, n):
         return RefSim._lib.vxref_step(self.h, int(n))
 

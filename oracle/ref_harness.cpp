@@ -164,6 +164,17 @@ void vxref_externals(void* h, int* dof, double* vals) {
     }
 }
 
+// Fixes / forces one voxel through the reference's own CVX_External API (VX_External.cpp:53-66).
+void vxref_set_external(void* h, int voxel, int dof, const float* force, const float* moment, const double* translate,
+                        const double* rotate) {
+    RefSim* r = (RefSim*)h;
+    CVX_External* e = r->sim.Vx.voxel(voxel)->external();
+    const double disp[6] = {translate[0], translate[1], translate[2], rotate[0], rotate[1], rotate[2]};
+    for (int k = 0; k < 6; k++) if (dof & (1 << k)) e->setDisplacement((dofComponent)(1 << k), disp[k]);
+    e->addForce(Vec3D<float>(force[0], force[1], force[2]));
+    e->addMoment(Vec3D<float>(moment[0], moment[1], moment[2]));
+}
+
 // Advance n steps with VX3 step-driver semantics.  Returns steps done; stops at divergence.
 int vxref_step(void* h, int n) {
     RefSim* r = (RefSim*)h;

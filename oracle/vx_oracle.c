@@ -329,14 +329,16 @@ static float mat_modulus(const mat_t* m, float strain) {
     return 0.0f;
 }
 
-/* Palette material -> CVX_MaterialVoxel: CVX_Material::clear (VX_Material.cpp:71-90),
+/* Palette material -> CVX_MaterialVoxel: CVX_Material::CVX_Material(1e6, 1e3) (VX_Material.cpp:15-22, 71-90),
  * CVX_Sim::CopyMat (Voxelyze3/src/VXA/VX_Sim.cpp:368-420) and the damping setters
  * applied in CVX_Sim::Import (VX_Sim.cpp:80-83). */
 static void vmat_from_palette(mat_t* m, const vxo_material* p, double nom, float grav) {
     memset(m, 0, sizeof(*m));
     m->nu = 0.0f; m->rho = 1.0f; m->cte = 0.0f; m->mus = 0.0f; m->muk = 0.0f;
     m->zi = 1.0f; m->zg = 0.0f; m->zc = 0.0f;
-    mat_set_linear(m, 1.0f, -1.0f);
+    /* CVoxelyze::addMaterial() builds CVX_MaterialVoxel(1e6, 1e3): a model setter that rejects
+       its arguments leaves this linear 1e6 Pa model in place (VX_Material.cpp:15-22) */
+    mat_set_linear(m, 1e6f, -1.0f);
     switch (p->model) {
     case 0: mat_set_linear(m, p->E, -1.0f); break;
     case 1: mat_set_linear(m, p->E, p->fail_stress); break;

@@ -1,0 +1,109 @@
+"""Generates the golden fixtures under tests/golden/ from the reference itself.
+
+Each fixture is a small VXA world (seeded, built by gpuvoxels_gb300.synth or
+below), run through the reference's own CPU Voxelyze compiled from the
+reference sources (oracle/_ref, see oracle/Makefile) with the VX3 step-driver
+semantics of oracle/ref_harness.cpp.  The .npz files keep the VXA text, the
+externals, and the reference's topology, material constants (as float bit
+patterns) and state snapshots.
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Only needed where the reference sources exist; the committed .npz files are
+what the tests read.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from gpuvoxels_gb300 import synth  # noqa: E402
+from oracle.oracle import RefSim, desc_from_vxa  # noqa: E402
+
+
+def grid_world(cells, materials, **kw):
+    """cells: (Z, Y, X) material ids (0 = empty)."""
+    cells = np.asarray(cells, np.int32)
+    phase = np.zeros(cells.shape)
+    return synth.vxa_document(cells, phase, materials, **kw)
+
+
+SOFT = dict(E=1e5, rho=1000.0, nu=0.35, cte=0.0, mus=1.0, muk=0.5)
+STIFF = dict(E=1e6, rho=1000.0, nu=0.35, cte=0.0, mus=0.8, muk=0.4)
+
+
+def worlds():
+    w = {}
+    w["c0_seed0"] = dict(vxa=synth.config0_creature(0).vxa, ext=[], snaps=[1, 100, 300])
+    c1 = synth.random_creature(11, (8, 8, 8), 0.7,
+                               [dict(E=2.1e5, rho=1000.0, nu=0.35, cte=0.01, mus=1.0, muk=0.5),
+                                dict(E=3.7e6, rho=1000.0, nu=0.35, cte=0.0, mus=1.0, muk=0.5),
+                                dict(E=9.0e5, rho=1000.0, nu=0.35, cte=0.01, mus=1.0, muk=0.5),
+                                dict(E=6.3e6, rho=1000.0, nu=0.35, cte=0.0, mus=1.0, muk=0.5)])
+    w["c1_poisson"] = dict(vxa=c1.vxa, ext=[], snaps=[1, 150, 300])
+    # two blocks: the upper one falls onto the lower one (self-collision between unlinked voxels)
+    blocks = np.zeros((5, 3, 3), np.int32)
+    blocks[0:2] = 1
+    blocks[3:5] = 1
+    w["falling_blocks"] = dict(vxa=grid_world(blocks, [SOFT], collision=True, expansion=False, vary_temp=False,
+                                              damping=(1.0, 0.8, 0.01)), ext=[], snaps=[600, 1400, 2000])
+    # bilinear cantilever: root fixed, tip pulled and pushed down (plasticity path, no gravity/floor)
+    bil = dict(E=1e6, rho=1000.0, nu=0.0, cte=0.0, mus=0.0, muk=0.0)
+    beam = np.ones((1, 1, 6), np.int32)
+    vxa = grid_world(beam, [bil], gravity=0.0, floor=False, vary_temp=False, volume_effects=False)
+    vxa = vxa.replace("<MatModel>0</MatModel><Elastic_Mod>1000000.0</Elastic_Mod><Fail_Stress>0</Fail_Stress>",
+                      "<MatModel>2</MatModel><Elastic_Mod>1000000.0</Elastic_Mod><Plastic_Mod>200000.0</Plastic_Mod>"
+                      "<Yield_Stress>10000.0</Yield_Stress><Fail_Stress>40000.0</Fail_Stress>")
+    w["bilinear_cantilever"] = dict(vxa=vxa, ext=[dict(voxel=0, dof_fixed=0x3F), dict(voxel=5, force=(2.0, 0.0, -0.3))],
+                                    snaps=[1, 200, 500])
+    # large-angle bending: a tip moment rotates the end voxels past the small-angle threshold
+    beam3 = np.ones((1, 1, 4), np.int32)
+    vxa = grid_world(beam3, [STIFF], gravity=0.0, floor=False, vary_temp=False)
+    w["large_angle"] = dict(vxa=vxa, ext=[dict(voxel=0, dof_fixed=0x3F), dict(voxel=3, moment=(0.0, 0.02, 0.05))],
+                            snaps=[1, 300, 800])
+    # partial fixes: translations of two corners, two rotation axes of another, moment in the middle
+    plate = np.ones((1, 3, 3), np.int32)
+    vxa = grid_world(plate, [STIFF], vary_temp=False)
+    w["partial_fix"] = dict(vxa=vxa, ext=[dict(voxel=0, dof_fixed=0x07), dict(voxel=8, dof_fixed=0x07, translate=(0.0, 0.0, 0.001)),
+                                          dict(voxel=2, dof_fixed=0x18), dict(voxel=4, moment=(0.01, 0.0, 0.0), force=(0.0, 0.5, 0.0))],
+                            snaps=[1, 200, 400])
+    return w
+
+
+def run(name, spec):
+    d = desc_from_vxa(spec["vxa"])
+    r = RefSim(spec["vxa"], d)
+    for e in spec["ext"]:
+        r.set_external(e["voxel"], e.get("dof_fixed", 0), e.get("force", (0, 0, 0)), e.get("moment", (0, 0, 0)),
+                       e.get("translate", (0, 0, 0)), e.get("rotate", (0, 0, 0)))
+    topo = r.topology()
+    mats = r.materials()
+    out = dict(vxa=np.array(spec["vxa"]), ext=np.array(repr(spec["ext"])), snaps=np.array(spec["snaps"], np.int64),
+               voxels=topo["voxels"], links=topo["links"], phase=topo["phase"],
+               voxmat_bits=mats["voxmat"].view(np.uint32), nom=mats["nom"],
+               linkmat_idx=mats["linkmat_idx"], linkmat_bits=mats["linkmat"].view(np.uint32))
+    done = 0
+    for k, s in enumerate(spec["snaps"]):
+        r.step(s - done)
+        done = s
+        vs, ls, sc = r.voxel_state(), r.link_state(), r.scalars()
+        out[f"s{k}_pos"] = vs["pos"]; out[f"s{k}_orient"] = vs["orient"]
+        out[f"s{k}_linMom"] = vs["linMom"]; out[f"s{k}_angMom"] = vs["angMom"]
+        out[f"s{k}_temp"] = vs["temp"]; out[f"s{k}_pStrain"] = vs["pStrain"]; out[f"s{k}_flags"] = vs["flags"]
+        out[f"s{k}_strain"] = ls["strain"]; out[f"s{k}_maxStrain"] = ls["maxStrain"]; out[f"s{k}_smallAngle"] = ls["smallAngle"]
+        out[f"s{k}_scalars"] = np.array([sc["t"], sc["optimal_dt"], sc["dt"], sc["diverged"], sc["steps"]])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: {r.nvox} voxels, {r.nlink} links, steps {spec['snaps']}")
+
+
+if __name__ == "__main__":
+    if not RefSim.available():
+        sys.exit("oracle/_ref/libvxref.so missing: run `make -C oracle ref` where the reference sources exist")
+    for name, spec in worlds().items():
+        run(name, spec)

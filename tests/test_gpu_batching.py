@@ -1,0 +1,121 @@
+"""Batching and serving semantics on the GPU: the batched form, the plain
+one-simulation-per-launch form, and a simulation served in a mix of others all
+produce identical results; divergence retires one simulation without touching
+the rest; the HBM budget gates admission."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleSim, desc_from_vxa
+
+import gpuvoxels_gb300 as g
+from gpuvoxels_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def test_plain_and_batched_are_bit_identical(ctx):
+    cs = synth.config1_batch(4, seed=9)
+    a = [ctx.load_vxa(c.vxa, name=f"p{i}") for i, c in enumerate(cs)]
+    b = [ctx.load_vxa(c.vxa, name=f"q{i}") for i, c in enumerate(cs)]
+    try:
+        for s in a:
+            ctx.step(s, 200, g.PLAIN)
+        ctx.step(b, 200, g.BATCHED)
+        for x, y in zip(a, b):
+            assert np.array_equal(_bits(ctx.voxel_state(x)["pos"]), _bits(ctx.voxel_state(y)["pos"]))
+            assert np.array_equal(_bits(ctx.voxel_state(x)["orient"]), _bits(ctx.voxel_state(y)["orient"]))
+    finally:
+        for s in a + b:
+            ctx.free(s)
+
+
+def test_served_alone_and_in_mix_are_identical():
+    c_probe = synth.config0_creature(21, stop_time=0.02)
+    others = synth.config1_batch(5, seed=13, sim_time=0.01)
+    with g.Context(0, 2 << 30) as c1:
+        s = c1.load_vxa(c_probe.vxa, name="alone")
+        c1.submit(s, 0)
+        res = []
+        while c1.pending():
+            res += c1.poll(chunk_steps=32)
+        r_alone = [r for r in res if r.id == s][0]
+    with g.Context(0, 2 << 30) as c2:
+        ids = [c2.load_vxa(o.vxa, name=f"o{i}") for i, o in enumerate(others[:2])]
+        for i in ids:
+            c2.submit(i, 0)
+        c2.poll(chunk_steps=7)                        # the probe arrives while others run
+        s2 = c2.load_vxa(c_probe.vxa, name="mix")
+        c2.submit(s2, 0)
+        for o in others[2:]:
+            c2.submit(c2.load_vxa(o.vxa, name="late"), 0)
+        res2 = []
+        while c2.pending():
+            res2 += c2.poll(chunk_steps=32)
+        r_mix = [r for r in res2 if r.id == s2][0]
+    assert r_alone.steps == r_mix.steps
+    assert r_alone.current_time == r_mix.current_time
+    assert list(r_alone.current_center_of_mass) == list(r_mix.current_center_of_mass)
+    assert r_alone.fitness_score == r_mix.fitness_score
+    assert r_alone.total_distance_of_all_voxels == r_mix.total_distance_of_all_voxels
+
+
+def test_divergence_retires_only_that_simulation(ctx):
+    ok = synth.config0_creature(2)
+    # a DtFrac far beyond the stable step makes the link strains explode
+    bad = synth.config0_creature(3, dt_frac=40.0)
+    s_ok, s_bad = ctx.load_vxa(ok.vxa, name="ok"), ctx.load_vxa(bad.vxa, name="bad")
+    try:
+        ctx.step([s_ok, s_bad], 300, g.BATCHED)
+        assert ctx.info(s_bad).status == g.SIM_DIVERGED
+        o = OracleSim(desc_from_vxa(bad.vxa))
+        o.step(300)
+        assert o.scalars()["diverged"] == 1 and ctx.info(s_bad).steps == o.scalars()["steps"]
+        assert ctx.info(s_ok).steps == 300 and ctx.info(s_ok).status != g.SIM_DIVERGED
+        ref = OracleSim(desc_from_vxa(ok.vxa))
+        ref.step(300)
+        assert np.abs(ctx.voxel_state(s_ok)["pos"] - ref.voxel_state()["pos"]).max() / 0.01 <= 1e-6
+    finally:
+        ctx.free(s_ok)
+        ctx.free(s_bad)
+
+
+def test_hbm_budget_admission():
+    big = synth.config0_creature(4)
+    with g.Context(0, 64 << 10) as c:         # 64 KiB budget: too small for one creature
+        s = c.load_vxa(big.vxa)
+        with pytest.raises(g.VX3Error, match="OOM_BUDGET"):
+            c.step(s, 1)
+    cs = synth.config1_batch(12, seed=17, sim_time=0.005)
+    with g.Context(0, 24 << 20) as c:         # room for a few at a time: the rest wait in the queue
+        ids = [c.load_vxa(x.vxa) for x in cs]
+        for i in ids:
+            c.submit(i, 0)
+        peak, done = 0, []
+        while c.pending():
+            done += c.poll(chunk_steps=64)
+            peak = max(peak, c.bytes_in_use())
+        assert len(done) == len(ids) and peak <= 24 << 20
+        assert all(r.status == g.SIM_DONE for r in done)
+
+
+def test_report_matches_worker_format(ctx, tmp_path):
+    cs = [synth.config0_creature(30 + i, stop_time=0.01) for i in range(3)]
+    ids = [ctx.load_vxa(c.vxa, name=f"bot_{i:04d}.vxd") for i, c in enumerate(cs)]
+    try:
+        ctx.run(ids)
+        p = tmp_path / "report.xml"
+        ctx.write_report(ids, str(p), "/data/generation_0001")
+        txt = p.read_text()
+        assert "<inputdir>generation_0001</inputdir>" in txt
+        fits = sorted([ctx.result(i).fitness_score for i in ids], reverse=True)
+        best = [i for i in ids if ctx.result(i).fitness_score == fits[0]][0]
+        assert f"<filename>bot_{ids.index(best):04d}.vxd</filename>" in txt
+        for i in range(3):
+            assert f"<bot_{i:04d}><currentTime>" in txt
+    finally:
+        for i in ids:
+            ctx.free(i)
