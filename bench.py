@@ -204,6 +204,8 @@ def run_ours(args):
     budget = int(args.budget_gb * (1 << 30))
     # ---- device-resident throughput
     ctx = g.Context(local, budget)
+    prec = g.FMA if args.precision == "fma" else g.EXACT
+    ctx.set_precision(prec)
     ids = [ctx.load_vxa(c.vxa, name=f"c{i}") for i, c in enumerate(cs)]
     ctx.step(ids, 1, g.BATCHED)                       # upload + first step
     if args.autotune:
@@ -254,6 +256,7 @@ def run_ours(args):
     e2e = None
     if rank == 0:
         c2 = g.Context(local, budget)
+        c2.set_precision(prec)
         t0 = time.perf_counter()
         ids2 = [c2.load_vxa(c.vxa, name=f"c{i}") for i, c in enumerate(cs)]
         c2.step(ids2, args.steps, g.BATCHED)
@@ -283,6 +286,7 @@ def run_ours(args):
         "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded creatures, no dataset)",
         "config": dict(desc, simulations=len(cs) * ws, voxels=n_vox * ws, links=n_links * ws, mode="batched",
+                       kernel_build=args.precision,
                        l2="device state larger than L2; no flush needed", parallelism=f"replicas x{ws} (no collective)"),
         "e2e": e2e,
         "gpu_launches": launches,
@@ -340,6 +344,7 @@ def main():
     ap.add_argument("--plain-sims", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", default="exact", choices=["exact", "fma"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -336,6 +336,10 @@ public:
             x.sizef = (float)m.nom;
             x.nom = m.nom;
             x.measured = m.is_measured;
+            x.massInvD = x.massInv; x.IinvD = x.Iinv; x.gDampTD = x.gDampT; x.gDampRD = x.gDampR; x.cDampTD = x.cDampT;
+            x.gravForceD = x.gravForce;
+            x.halfNom = m.nom / 2;
+            x.halfMassInv = 0.5 * (double)x.massInv;
         }
         dev::LMat* lm = (dev::LMat*)P(o.lm);
         for (size_t i = 0; i < w.lmats.size(); i++) {
@@ -345,6 +349,8 @@ public:
             x.sqA1 = m.sqA1; x.sqA2xIp = m.sqA2xIp; x.sqB1 = m.sqB1; x.sqB2xFMp = m.sqB2xFMp; x.sqB3xIp = m.sqB3xIp;
             x.epsFail = m.epsFail; x.linear = m.linear; x.n = m.n;
             for (int k = 0; k < 18; k++) { x.strain[k] = k < kMaxModelPoints + 2 ? m.strain[k] : 0; x.stress[k] = k < kMaxModelPoints + 2 ? m.stress[k] : 0; }
+            x.a2D = x.a2; x.b1D = x.b1; x.b2D = x.b2; x.b3D = x.b3;
+            x.sqA1D = x.sqA1; x.sqA2xIpD = x.sqA2xIp; x.sqB1D = x.sqB1; x.sqB2xFMpD = x.sqB2xFMp; x.sqB3xIpD = x.sqB3xIp;
         }
         dev::Ext* ex = (dev::Ext*)P(o.ext);
         for (size_t i = 0; i < w.desc.externals.size(); i++) {

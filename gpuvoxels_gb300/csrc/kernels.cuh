@@ -29,7 +29,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     const VMat& vN = S.vm[__ldg(S.vmat + ng)];
     const VMat& vP = S.vm[__ldg(S.vmat + pv)];
     const float tN = S.temp[ng], tP = S.temp[pv];
-    const double restLen = 0.5 * (base_size(vN, tN) + base_size(vP, tP));   // CVX_Link::updateRestLength
+    const double restLen = half(base_size(vN, tN) + base_size(vP, tP));   // CVX_Link::updateRestLength
     const int nl = S.nl;
     double* st = S.lst;
     const d3 o2 = D3(st[l], st[nl + l], st[2 * nl + l]);
@@ -47,10 +47,15 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     pos2 = qrot(tr, pos2);
     angle2 = qmul(tr, angle2);
     angle1 = Q4(1, 0, 0, 0);
-    const float smallTurn = (float)((fabs(pos2.z) + fabs(pos2.y)) / pos2.x);
-    const float extendPerc = (float)(fabs(1 - pos2.x / restLen));
-    if (!small && smallTurn < 0.05f && extendPerc < 0.50f) { small = true; lvv = false; }
-    else if (small && (smallTurn > HB_TURN || extendPerc > HB_EXT)) { small = false; lvv = false; }
+    // SmallTurn = (float)((|z|+|y|)/x), ExtendPerc = (float)|1 - x/restLength|, compared with the
+    // hysteresis thresholds (VX_Link.cpp:85-94); decided without dividing unless near a threshold
+    const double turnNum = fabs(pos2.z) + fabs(pos2.y);
+    if (!small) {
+        if (quot_lt(turnNum, pos2.x, 0.05f) && ext_lt(pos2.x, restLen, 0.50f)) { small = true; lvv = false; }
+    } else if (quot_gt(turnNum, pos2.x, HB_TURN) || ext_gt(pos2.x, restLen, HB_EXT)) {
+        small = false;
+        lvv = false;
+    }
     d3 a1v;
     if (small) {
         pos2.x -= restLen;
@@ -106,23 +111,25 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     if (m.epsFail != -1.0f && maxStrain > m.epsFail) {
         fN = fP = mN = mP = D3(0, 0, 0);
     } else {
-        const float b1 = m.b1, b2 = m.b2, b3 = m.b3, a2 = m.a2;
+        // the float beam constants enter as exactly widened doubles (b1*pos2.y is float*double in the reference)
+        const double b1 = m.b1D, b2 = m.b2D, b3 = m.b3D, a2 = m.a2D;
         fN = D3((double)(stress * A), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
         fP = D3(-fN.x, -fN.y, -fN.z);
-        mN = D3(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (2 * a1v.y + a2v.y), b2 * pos2.y - b3 * (2 * a1v.z + a2v.z));
-        mP = D3(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + 2 * a2v.y), b2 * pos2.y - b3 * (a1v.z + 2 * a2v.z));
+        mN = D3(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (mul2(a1v.y) + a2v.y), b2 * pos2.y - b3 * (mul2(a1v.z) + a2v.z));
+        mP = D3(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + mul2(a2v.y)), b2 * pos2.y - b3 * (a1v.z + mul2(a2v.z)));
         if (lvv) {
-            const d3 dP = D3(0.5 * (pos2.x - o2.x), 0.5 * (pos2.y - o2.y), 0.5 * (pos2.z - o2.z));
-            const d3 d1 = D3(0.5 * (a1v.x - oa1.x), 0.5 * (a1v.y - oa1.y), 0.5 * (a1v.z - oa1.z));
-            const d3 d2 = D3(0.5 * (a2v.x - oa2.x), 0.5 * (a2v.y - oa2.y), 0.5 * (a2v.z - oa2.z));
-            const float sqA1 = m.sqA1, sqA2xIp = m.sqA2xIp, sqB1 = m.sqB1, sqB2xFMp = m.sqB2xFMp, sqB3xIp = m.sqB3xIp;
+            const d3 dP = D3(half(pos2.x - o2.x), half(pos2.y - o2.y), half(pos2.z - o2.z));
+            const d3 d1 = D3(half(a1v.x - oa1.x), half(a1v.y - oa1.y), half(a1v.z - oa1.z));
+            const d3 d2 = D3(half(a2v.x - oa2.x), half(a2v.y - oa2.y), half(a2v.z - oa2.z));
+            const double sqA1 = m.sqA1D, sqA2xIp = m.sqA2xIpD, sqB1 = m.sqB1D, sqB2xFMp = m.sqB2xFMpD, sqB3xIp = m.sqB3xIpD;
             const d3 pc = D3(sqA1 * dP.x, sqB1 * dP.y - sqB2xFMp * (d1.z + d2.z), sqB1 * dP.z + sqB2xFMp * (d1.y + d2.y));
-            const float dmN = vN.dampNum / dt, dmP = vP.dampNum / dt;   // CVX_Voxel::dampingMultiplier
+            const float dmNf = vN.dampNum / dt, dmPf = vP.dampNum / dt;   // CVX_Voxel::dampingMultiplier
+            const double dmN = dmNf, dmP = dmPf;
             fN = D3(fN.x + dmN * pc.x, fN.y + dmN * pc.y, fN.z + dmN * pc.z);
             fP = D3(fP.x - dmP * pc.x, fP.y - dmP * pc.y, fP.z - dmP * pc.z);
-            const double hN = 0.5 * dmN, hP = 0.5 * dmP;
-            const d3 tN = D3(-sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (2 * d1.y + d2.y), -sqB2xFMp * dP.y + sqB3xIp * (2 * d1.z + d2.z));
-            const d3 tP = D3(sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (d1.y + 2 * d2.y), -sqB2xFMp * dP.y + sqB3xIp * (d1.z + 2 * d2.z));
+            const double hN = half(dmN), hP = half(dmP);
+            const d3 tN = D3(-sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (mul2(d1.y) + d2.y), -sqB2xFMp * dP.y + sqB3xIp * (mul2(d1.z) + d2.z));
+            const d3 tP = D3(sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (d1.y + mul2(d2.y)), -sqB2xFMp * dP.y + sqB3xIp * (d1.z + mul2(d2.z)));
             mN = D3(mN.x - hN * tN.x, mN.y - hN * tN.y, mN.z - hN * tN.z);
             mP = D3(mP.x - hP * tP.x, mP.y - hP * tP.y, mP.z - hP * tP.z);
         } else {
@@ -319,9 +326,9 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
             if (fl & (1u << d)) F = D3(F.x + sf[(d * 3) * nv + v], F.y + sf[(d * 3 + 1) * nv + v], F.z + sf[(d * 3 + 2) * nv + v]);
         F = qrot(q, F);
         if (e) { F.x += e->f[0]; F.y += e->f[1]; F.z += e->f[2]; }
-        const double vx = m.massInv * lm.x, vy = m.massInv * lm.y, vz = m.massInv * lm.z;
-        F = D3(F.x - m.gDampT * vx, F.y - m.gDampT * vy, F.z - m.gDampT * vz);
-        F.z += m.gravForce;
+        const double vx = m.massInvD * lm.x, vy = m.massInvD * lm.y, vz = m.massInvD * lm.z;
+        F = D3(F.x - m.gDampTD * vx, F.y - m.gDampTD * vy, F.z - m.gDampTD * vz);
+        F.z += m.gravForceD;
         if (flags & SF_COLLIDE) {
             const int nc = S.ccount[v];
             const float* cf = S.cforce + (size_t)v * 3 * kContactCap;
@@ -330,11 +337,13 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         // floorForce()
         const d3 F0 = F;
         const bool floor = flags & SF_FLOOR;
+        // CVX_Voxel::floorPenetration; pos is unchanged until the translation below, so the
+        // reference's second evaluation (VX_Voxel.cpp:188) yields this same value
+        const float pen = floor ? (float)(half(base_size_avg(m, temp)) - m.halfNom - pos.z) : -1.0f;
         if (floor) {
-            const float pen = (float)(base_size_avg(m, temp) / 2 - m.nom / 2 - pos.z);
             if (pen >= 0) {
                 const float normal = m.penStiff * pen;
-                F.z += normal - m.cDampT * vz;
+                F.z += normal - m.cDampTD * vz;
                 if (fl & VF_STATIC) {
                     const float surf = (float)(F.x * F.x + F.y * F.y);
                     const float fr = (m.mus * normal) * (m.mus * normal);
@@ -354,9 +363,9 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         lm = D3(lm.x + dt * F.x, lm.y + dt * F.y, lm.z + dt * F.z);
         const float sdt = dt * m.massInv;
         d3 tr = D3(sdt * lm.x, sdt * lm.y, sdt * lm.z);
-        if (floor && (float)(base_size_avg(m, temp) / 2 - m.nom / 2 - pos.z) >= 0) {
+        if (floor && pen >= 0) {
             const double work = fric.x * tr.x + fric.y * tr.y;
-            const double hKe = 0.5 * m.massInv * (lm.x * lm.x + lm.y * lm.y);
+            const double hKe = m.halfMassInv * (lm.x * lm.x + lm.y * lm.y);
             if (hKe + work <= 0) fl |= VF_STATIC;
             if (fl & VF_STATIC) { lm.x = lm.y = 0; tr.x = tr.y = 0; }
         } else {
@@ -371,8 +380,8 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
             if (fl & (1u << d)) M = D3(M.x + sm[(d * 3) * nv + v], M.y + sm[(d * 3 + 1) * nv + v], M.z + sm[(d * 3 + 2) * nv + v]);
         M = qrot(q, M);
         if (e) { M.x += e->m[0]; M.y += e->m[1]; M.z += e->m[2]; }
-        const double wx = m.Iinv * am.x, wy = m.Iinv * am.y, wz = m.Iinv * am.z;
-        M = D3(M.x - m.gDampR * wx, M.y - m.gDampR * wy, M.z - m.gDampR * wz);
+        const double wx = m.IinvD * am.x, wy = m.IinvD * am.y, wz = m.IinvD * am.z;
+        M = D3(M.x - m.gDampRD * wx, M.y - m.gDampRD * wy, M.z - m.gDampRD * wz);
         am = D3(am.x + dt * M.x, am.y + dt * M.y, am.z + dt * M.z);
         const float sI = dt * m.Iinv;
         q = qmul(q_from_rotvec(D3(sI * am.x, sI * am.y, sI * am.z)), q);
@@ -454,7 +463,50 @@ __device__ __forceinline__ double block_sum(double x, double* red) {
     return r;
 }
 
-__global__ void __launch_bounds__(256) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items,
+// Per-simulation bookkeeping after its last voxel item of the step (one thread):
+// status on divergence/error, time and step count, cycle CoM sampling and the
+// recent-angle measure (VX3_VoxelyzeKernel.cu:314-334, 352), stop condition.
+// Kept out of line so the voxel loop does not carry its registers and stack.
+__device__ __noinline__ void sim_control(Ctl& c, bool div, double t_next, int64_t stepno, bool com_step, int flags, int nv,
+                                         const double* partials) {
+    c.done_items = 0;
+    if (div) { c.status = 3; return; }
+    if (c.error) { c.status = 4; return; }
+    c.t = t_next;
+    c.steps = stepno;
+    if (flags & SF_COLLIDE) c.hash_parity ^= 1;
+    if (com_step) {
+        double s4[4] = {0, 0, 0, 0};
+        for (int k = 0; k < c.n_vox_items; k++)
+            for (int j = 0; j < 4; j++) s4[j] += partials[(size_t)(c.item_begin + k) * 4 + j];
+        c.angle_samples++;
+        for (int j = 0; j < 3; j++) { c.com_hist[0][j] = c.com_hist[1][j]; c.com_hist[1][j] = c.com[j]; }
+        if (s4[3] == 0) { c.com[0] = c.com[1] = c.com[2] = 0; }
+        else for (int j = 0; j < 3; j++) c.com[j] = s4[j] / s4[3];
+        const double* A = c.com_hist[0];
+        const double* B = c.com_hist[1];
+        const double* C = c.com;
+        const bool eqBC = B[0] == C[0] && B[1] == C[1] && B[2] == C[2];
+        const bool eqAB = A[0] == B[0] && A[1] == B[1] && A[2] == B[2];
+        if (eqBC || eqAB || c.angle_samples < 3) c.recent_angle = 0;
+        else {
+            const double bax = B[0] - A[0], bay = B[1] - A[1], baz = B[2] - A[2];
+            const double cbx = C[0] - B[0], cby = C[1] - B[1], cbz = C[2] - B[2];
+            c.recent_angle = acos((bax * cbx + bay * cby + baz * cbz) /
+                                  (sqrt(bax * bax + bay * bay + baz * baz) * sqrt(cbx * cbx + cby * cby + cbz * cbz)));
+        }
+    }
+    bool stop = c.target > 0 && stepno >= c.target;
+    if (c.stop.n > 0) {
+        MathVars mv;
+        mv.x = c.com[0]; mv.y = c.com[1]; mv.z = c.com[2]; mv.hit = 0; mv.t = c.t; mv.angle = c.recent_angle;
+        mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = nv;
+        if (mathtree_eval(c.stop, mv) > 0) stop = true;
+    }
+    if (stop) c.status = 2;
+}
+
+__global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items,
                                                 int* tickets, double* partials) {
     __shared__ int s_item, s_last;
     __shared__ double red[256];
@@ -488,42 +540,7 @@ __global__ void __launch_bounds__(256) k_voxels(const Sim* __restrict__ sims, Ct
         __syncthreads();
         if (s_last && threadIdx.x == 0) {
             __threadfence();
-            c.done_items = 0;
-            if (div) { c.status = 3; continue; }
-            if (c.error) { c.status = 4; continue; }
-            c.t = t_next;
-            c.steps = stepno;
-            if (flags & SF_COLLIDE) c.hash_parity ^= 1;
-            if (com_step) {
-                double s4[4] = {0, 0, 0, 0};
-                for (int k = 0; k < c.n_vox_items; k++)
-                    for (int j = 0; j < 4; j++) s4[j] += partials[(size_t)(c.item_begin + k) * 4 + j];
-                // VX3_VoxelyzeKernel::doTimeStep cycle sampling (VX3_VoxelyzeKernel.cu:314-334)
-                c.angle_samples++;
-                for (int j = 0; j < 3; j++) { c.com_hist[0][j] = c.com_hist[1][j]; c.com_hist[1][j] = c.com[j]; }
-                if (s4[3] == 0) { c.com[0] = c.com[1] = c.com[2] = 0; }
-                else for (int j = 0; j < 3; j++) c.com[j] = s4[j] / s4[3];
-                const double* A = c.com_hist[0];
-                const double* B = c.com_hist[1];
-                const double* C = c.com;
-                const bool eqBC = B[0] == C[0] && B[1] == C[1] && B[2] == C[2];
-                const bool eqAB = A[0] == B[0] && A[1] == B[1] && A[2] == B[2];
-                if (eqBC || eqAB || c.angle_samples < 3) c.recent_angle = 0;
-                else {
-                    const double bax = B[0] - A[0], bay = B[1] - A[1], baz = B[2] - A[2];
-                    const double cbx = C[0] - B[0], cby = C[1] - B[1], cbz = C[2] - B[2];
-                    c.recent_angle = acos((bax * cbx + bay * cby + baz * cbz) /
-                                          (sqrt(bax * bax + bay * bay + baz * baz) * sqrt(cbx * cbx + cby * cby + cbz * cbz)));
-                }
-            }
-            bool stop = c.target > 0 && stepno >= c.target;
-            if (c.stop.n > 0) {
-                MathVars mv;
-                mv.x = c.com[0]; mv.y = c.com[1]; mv.z = c.com[2]; mv.hit = 0; mv.t = c.t; mv.angle = c.recent_angle;
-                mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = S.nv;
-                if (mathtree_eval(c.stop, mv) > 0) stop = true;
-            }
-            if (stop) c.status = 2;
+            sim_control(c, div, t_next, stepno, com_step, flags, S.nv, partials);
         }
     }
 }

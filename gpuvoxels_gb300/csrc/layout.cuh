@@ -37,12 +37,18 @@ struct VMat {
     double nom;
     int32_t measured;
     int32_t pad;
+    // the float constants above that enter FP64 expressions, widened once (exact)
+    double massInvD, IinvD, gDampTD, gDampRD, cDampTD, gravForceD;
+    double halfNom;       // nom/2
+    double halfMassInv;   // 0.5*(double)massInv
 };
 
 struct LMat {
     float E, nu, eHat, a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp, epsFail;
     int32_t linear, n;
     float strain[18], stress[18];
+    // beam and damping constants widened once (exact float -> double)
+    double a2D, b1D, b2D, b3D, sqA1D, sqA2xIpD, sqB1D, sqB2xFMpD, sqB3xIpD;
 };
 
 struct Ext {

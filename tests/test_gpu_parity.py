@@ -119,9 +119,13 @@ def test_gpu_batch_of_uneven_creatures_matches_oracle(pctx):
             ctx.free(s)
 
 
-def test_center_of_mass_over_full_horizon(pctx):
-    ctx = pctx
-    """CoM displacement within 1e-4 relative after a 0.25 s run to the stop condition (~8,000 steps)."""
+@pytest.mark.parametrize("precision,rtol", [(g.EXACT, 1e-4), (g.FMA, 1e-3)], ids=["exact", "fma"])
+def test_center_of_mass_over_full_horizon(ctx, precision, rtol):
+    """CoM displacement after a 0.25 s run to the stop condition (~8,000 steps): within 1e-4
+    relative for the exact build (the specification's bar).  The FMA build rounds every
+    multiply-add once instead of twice; over long horizons that drifts further (measured
+    ~5e-4), so it is held to 1e-3 and is not the default."""
+    ctx.set_precision(precision)
     c = synth.config0_creature(7, stop_time=0.25)
     d = desc_from_vxa(c.vxa)
     o = OracleSim(d)
@@ -135,8 +139,25 @@ def test_center_of_mass_over_full_horizon(pctx):
         init = np.array(r.initial_center_of_mass)
         disp_o = com_o - init
         disp_g = np.array(r.current_center_of_mass) - init
-        assert np.linalg.norm(disp_g - disp_o) <= 1e-4 * max(np.linalg.norm(disp_o), 1e-12)
+        assert np.linalg.norm(disp_g - disp_o) <= rtol * max(np.linalg.norm(disp_o), 1e-12)
         assert r.current_time > 0.25 and r.status == g.SIM_DONE
         assert r.fitness_score == pytest.approx(disp_g[0], abs=1e-12)
     finally:
         ctx.free(sim)
+        ctx.set_precision(g.EXACT)
+
+
+def test_exact_build_is_bit_identical_without_transcendentals(ctx):
+    """With no actuation (no sin) and small angles only, the exact build performs exactly the
+    reference's floating-point operations: positions and orientations equal bit for bit."""
+    from conftest import load_golden
+    for name in ("falling_blocks", "bilinear_cantilever"):
+        z, vxa, ext = load_golden(name)
+        sim = _load(ctx, vxa, ext, name)
+        try:
+            ctx.step(sim, int(z["snaps"][1]))
+            st = ctx.voxel_state(sim)
+            assert np.array_equal(st["pos"].view(np.uint64), z["s1_pos"].view(np.uint64)), name
+            assert np.array_equal(st["orient"].view(np.uint64), z["s1_orient"].view(np.uint64)), name
+        finally:
+            ctx.free(sim)
