@@ -21,7 +21,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgpuvoxels_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_exact.cu", "kernels_fast.cu", "engine.cu", "world.cpp", "xml_dom.cpp", "capi.cpp"]
+SOURCES = ["kernels_exact.cu", "kernels_fast.cu", "engine.cu", "noalloc.cu", "world.cpp", "xml_dom.cpp", "capi.cpp"]
 
 
 def nvcc() -> str:

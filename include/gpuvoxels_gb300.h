@@ -32,6 +32,7 @@ extern "C" {
 #define VX3_E_CUDA (-5)
 #define VX3_E_ARG (-6)
 #define VX3_E_STATE (-7)
+#define VX3_E_LIMIT (-8)      /* a size beyond a fixed, documented limit */
 
 /* vx3_result.status / vx3_sim_info.status */
 #define VX3_SIM_IDLE 0
@@ -143,6 +144,24 @@ int vx3_set_profiling(vx3_ctx* ctx, int on);
 #define VX3_EXACT 0
 #define VX3_FMA 1
 int vx3_set_precision(vx3_ctx* ctx, int mode);
+
+/* Mass-weighted centre of mass of n points already on the device, for callers that cannot
+ * allocate device memory: code recording a CUDA graph (stream capture forbids cudaMalloc),
+ * processes whose device memory belongs to another framework's allocator, real-time loops.
+ * This entry point has no counterpart in the reference.  It is the engine's centre-of-mass
+ * reduction (per-block partial sums, then one fixed-order fold) with its scratch in a fixed
+ * array compiled into the library, so it calls no cudaMalloc, cudaFree or allocating routine.
+ *   x, y, z[n] (double), mass[n] (float): device inputs; out4: device output (cx, cy, cz, total mass);
+ *   stream: a cudaStream_t, or NULL for the legacy default stream; the work is only enqueued.
+ * Limit: n <= VX3_NOALLOC_MAX_POINTS; larger n returns VX3_E_LIMIT without launching anything.
+ * The scratch (64 KiB) stays resident on every GPU that loads the library until the process exits.
+ * The first call on a device resolves the scratch array's device address with that device current;
+ * make that first call before any stream capture.  All calls share the scratch and it keeps the last
+ * call's contents (each call overwrites everything it reads); calls that overlap on the GPU race,
+ * so serialise them (one stream, or events between streams). */
+#define VX3_NOALLOC_MAX_POINTS 4194304
+int vx3_center_of_mass_noalloc(const double* x, const double* y, const double* z, const float* mass, int64_t n, double* out4,
+                               void* stream);
 /* Device bytes a loaded simulation needs when resident (for HBM-budget admission). */
 int64_t vx3_sim_bytes(vx3_ctx* ctx, vx3_sim_id id);
 size_t vx3_bytes_in_use(vx3_ctx* ctx);
