@@ -24,7 +24,7 @@ ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
 sys.path.insert(0, ROOT)
 
 from gpuvoxels_gb300 import synth  # noqa: E402
-from oracle.oracle import RefSim, desc_from_vxa  # noqa: E402
+from oracle.oracle import RefSim, desc_from_vxa, merge_vxd  # noqa: E402
 
 
 def grid_world(cells, materials, **kw):
@@ -76,6 +76,43 @@ def worlds():
     return w
 
 
+# The reference's own sample worlds (read from its source tree; the merged VXA text is stored in the fixture).
+REF = os.environ.get("VX_REFERENCE", "/root/reference")
+SAMPLES = {
+    "ref_zoo_basic": ("zoo/basic/base.vxa", "zoo/basic/robot.vxd", [1, 300, 1000]),
+    "ref_example": ("doc/misc/example.vxa", None, [1, 300, 1000]),
+    "ref_signaling": ("Experiments/xenobot/c.signaling/data1/base.vxa", "Experiments/xenobot/c.signaling/data1/rob.vxd",
+                      [1, 300, 1000]),
+    "ref_memleaking": ("Experiments/xenobot/d.memleaking/data/base.vxa", "Experiments/xenobot/d.memleaking/data/rob.vxd",
+                       [1, 300, 1000]),
+    "ref_circle_push": ("Experiments/xenobot/e.circle_push/data1/base.vxa",
+                        "Experiments/xenobot/e.circle_push/data1/bot_0017.vxd", [1, 300, 1000]),
+    "ref_target_only": ("Experiments/xenobot/h.target_only/data1/base.vxa",
+                        "Experiments/xenobot/h.target_only/data1/bot_0000.vxd", [1, 300]),
+}
+DAMPING_DEFAULTS = ("<Damping><BondDampingZ>0.1</BondDampingZ><ColDampingZ>1</ColDampingZ>"
+                    "<SlowDampingZ>1</SlowDampingZ></Damping>")
+
+
+def sample_worlds():
+    """The reference's sample worlds, VXD merged into the base.  A world without
+    <Damping> leaves the reference's damping members unset (VXA/VX_Sim.cpp:197-212
+    only assigns them inside that element), so the fixture states the documented
+    defaults 0.1/1.0/1.0 explicitly; nothing else is changed."""
+    w = {}
+    for name, (base, vxd, snaps) in SAMPLES.items():
+        with open(os.path.join(REF, base), encoding="latin-1") as f:
+            xml = f.read()
+        if vxd:
+            with open(os.path.join(REF, vxd), encoding="latin-1") as f:
+                xml = merge_vxd(xml, f.read())
+        if "<Damping>" not in xml:
+            i = xml.index("<Simulator>") + len("<Simulator>")
+            xml = xml[:i] + DAMPING_DEFAULTS + xml[i:]
+        w[name] = dict(vxa=xml, ext=[], snaps=snaps)
+    return w
+
+
 def run(name, spec):
     d = desc_from_vxa(spec["vxa"])
     r = RefSim(spec["vxa"], d)
@@ -105,5 +142,10 @@ def run(name, spec):
 if __name__ == "__main__":
     if not RefSim.available():
         sys.exit("oracle/_ref/libvxref.so missing: run `make -C oracle ref` where the reference sources exist")
-    for name, spec in worlds().items():
-        run(name, spec)
+    todo = dict(worlds())
+    if os.path.isdir(REF):
+        todo.update(sample_worlds())
+    only = sys.argv[1:]
+    for name, spec in todo.items():
+        if not only or name in only:
+            run(name, spec)
