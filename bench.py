@@ -304,6 +304,78 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_serve(args):
+    """Serving: requests arrive as a Poisson stream; each is parsed and loaded on arrival
+    (vx3_load_vxa), queued (vx3_submit) and advanced by vx3_poll in chunks of --chunk-steps
+    alongside every other admitted request, within the context's HBM budget.  Per offered
+    rate: completion latency p50/p99 (submit to finish) and served voxel-steps/s."""
+    import itertools
+    import numpy as np
+    import gpuvoxels_gb300 as g
+    from gpuvoxels_gb300 import synth
+    reqs = synth.serving_requests(args.serve_requests, seed=4)
+    ctx = g.Context(0, int(args.budget_gb * (1 << 30)))
+    ctx.set_precision(g.FMA if args.precision == "fma" else g.EXACT)
+    # warm the kernels and graphs with one small request
+    w = ctx.load_vxa(reqs[0][0].vxa, name="warm")
+    ctx.submit(w, 256)
+    while ctx.pending():
+        for r in ctx.poll(args.chunk_steps):
+            ctx.free(r.id)
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    rng = np.random.default_rng(5)
+    out = []
+    for rate in rates:
+        arrivals = list(itertools.accumulate(rng.exponential(1.0 / rate, size=len(reqs))))
+        lat, vsteps, k = [], 0, 0
+        t0 = time.perf_counter()
+        while k < len(reqs) or ctx.pending():
+            now = time.perf_counter() - t0
+            while k < len(reqs) and arrivals[k] <= now:
+                c, horizon = reqs[k]
+                sid = ctx.load_vxa(c.vxa, name=f"r{k}")
+                ctx.submit(sid, horizon)
+                k += 1
+            if ctx.pending():
+                for r in ctx.poll(args.chunk_steps):
+                    lat.append(r.finish_time_s - r.submit_time_s)
+                    vsteps += r.num_voxel * r.steps
+                    ctx.free(r.id)
+            elif k < len(reqs):
+                time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t0))))
+        span = time.perf_counter() - t0
+        lat.sort()
+        pct = lambda p: lat[min(len(lat) - 1, int(round(p / 100.0 * (len(lat) - 1))))]
+        out.append(dict(offered_req_per_s=rate, completed=len(lat), p50_latency_s=pct(50), p99_latency_s=pct(99),
+                        served_voxel_steps_per_s=vsteps / span, makespan_s=span))
+    ctx.close()
+    line = {"metric": "served voxel-steps/s and completion latency (Poisson arrivals)", "unit": "voxel-steps/s",
+            "value": max(o["served_voxel_steps_per_s"] for o in out), "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic (seeded creatures, no dataset)",
+            "config": {"workload": f"serving: {len(reqs)} requests per rate, V log-uniform [100, 1e4], horizon U[1e3, 5e3] "
+                                   f"steps, 20% with self-collision, chunk {args.chunk_steps} steps per poll",
+                       "kernel_build": args.precision},
+            "rates": out}
+    print(json.dumps(line))
+
+
+def profile_case(args):
+    """A short, self-terminating run for ncu: the workload's kernels, one launch each per step."""
+    import gpuvoxels_gb300 as g
+    cs, desc = make_workload(args.workload, 0, args.batch)
+    ctx = g.Context(0, int(args.budget_gb * (1 << 30)))
+    ctx.set_precision(g.FMA if args.precision == "fma" else g.EXACT)
+    ids = [ctx.load_vxa(c.vxa, name=f"c{i}") for i, c in enumerate(cs)]
+    ctx.set_profiling(True)
+    ctx.step(ids, args.profile_steps, g.BATCHED)
+    t = ctx.timing()
+    n_links = sum(ctx.info(i).num_link for i in ids)
+    n_vox = sum(ctx.info(i).num_voxel for i in ids)
+    print(json.dumps(dict(workload=desc["workload"], steps=args.profile_steps, voxels=n_vox, links=n_links,
+                          link_ms=t["link_ms"], voxel_ms=t["voxel_ms"], contact_ms=t["contact_ms"])))
+    ctx.close()
+
+
 def run_reference(args):
     rank, ws, dist = dist_init()
     if rank != 0:
@@ -313,9 +385,7 @@ def run_reference(args):
     cs, desc = make_workload(args.workload, 0, args.batch)
     threads = os.cpu_count() or 1
     vals = []
-    for _ in range(max(1, args.warmup // args.warmup if args.warmup else 1)):
-        pass
-    for _ in range(args.steps if args.steps <= 3 else 3):
+    for _ in range(min(args.steps, 3)):
         v, cores, kind, sample = cpu_sample(cs, args.cpu_seconds, threads)
         vals.append(v)
     v = statistics.median(vals)
@@ -336,7 +406,10 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "slab", "collide", "plain"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "slab", "collide", "plain", "serve"])
+    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-rates", default="5,10,20,40", help="offered request rates (req/s) for --workload serve")
+    ap.add_argument("--chunk-steps", type=int, default=64)
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--graph-steps", type=int, default=64)
@@ -345,10 +418,17 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--precision", default="exact", choices=["exact", "fma"])
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling case for ncu: load the workload, run this many batched steps with one launch per "
+                         "kernel (no graphs), print the per-kernel times and exit")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile_steps:
+        profile_case(args)
+    elif args.workload == "serve":
+        run_serve(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -34,7 +34,8 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_submit", "vx3_poll", "vx3_pending", "vx3_get_result", "vx3_sim_info_get", "vx3_get_state",
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
-           "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc"]
+           "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
+           "vx3_write_report_multi"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -89,6 +90,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_inspect_topology": (I, [S, S, P, P, P, P, P, P, P]),
         "vx3_inspect_formula": (I, [S, S, I, P, P]),
         "vx3_center_of_mass_noalloc": (I, [P, P, P, P, I64, P, P]),
+        "vx3_write_report_multi": (I, [P, P, P, I, S, S]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

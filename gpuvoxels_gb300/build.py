@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgpuvoxels_gb300.so")
+WORKER = os.path.join(OUT_DIR, "vx3_node_worker")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels_exact.cu", "kernels_fast.cu", "engine.cu", "noalloc.cu", "world.cpp", "xml_dom.cpp", "capi.cpp"]
 
@@ -41,9 +42,9 @@ def _flags(src: str):
 
 
 def needs_build() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(WORKER):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(WORKER))
     for d in (CSRC, os.path.join(HERE, "..", "include")):
         for f in os.listdir(d):
             if os.path.getmtime(os.path.join(d, f)) > t:
@@ -76,6 +77,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the worker executable (vx3_node_worker process contract) over the library
+    cmd = [exe, os.path.join(CSRC, "worker_main.cpp"), "-o", WORKER + ".tmp", "-O2", "-std=c++17", "-I", CSRC,
+           "-I", os.path.join(HERE, "..", "include"), "-L", OUT_DIR, "-lgpuvoxels_gb300", "-Xlinker", "-rpath,$ORIGIN",
+           "-cudart", "static"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"worker link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(WORKER + ".tmp", WORKER)
     return LIB
 
 

@@ -189,19 +189,44 @@ int vx3_get_link_state(vx3_ctx* c, vx3_sim_id id, double* d9, float* f3, int32_t
     return e ? fail(c, e, err) : VX3_OK;
 }
 
-int vx3_write_report(vx3_ctx* c, const vx3_sim_id* ids, int n, const char* input_dir, const char* path) {
-    if (!c || !path || (n > 0 && !ids)) return VX3_E_ARG;
-    std::vector<std::pair<vx3_result, std::string>> rs;
+}  // extern "C"
+
+namespace {
+// One simulation's report entry: its result, file name and (SavePositionOfAllVoxels) positions.
+struct ReportEntry {
+    vx3_result r;
+    std::string name;
+    int save = 0;
+    std::vector<double> init, cur;
+    std::vector<int> mats;
+};
+
+int collect_entries(vx3_ctx* c, const vx3_sim_id* ids, int n, std::vector<ReportEntry>* out) {
     for (int i = 0; i < n; i++) {
-        vx3_result r;
-        if (int e = vx3_get_result(c, ids[i], &r)) return e;
-        rs.emplace_back(r, c->names[ids[i]]);
+        ReportEntry e;
+        if (int rc = vx3_get_result(c, ids[i], &e.r)) return rc;
+        e.name = c->names[ids[i]];
+        if (int rc = c->eng->saved_positions(ids[i], &e.save, &e.init, &e.cur, &e.mats, &c->err)) return rc;
+        out->push_back(std::move(e));
     }
-    // VX3_SimulationResult::compareFitnessScore: diverged (NaN) last, then descending fitness
-    std::stable_sort(rs.begin(), rs.end(), [](const std::pair<vx3_result, std::string>& a, const std::pair<vx3_result, std::string>& b) {
-        if (std::isnan(b.first.fitness_score)) return !std::isnan(a.first.fitness_score);
-        if (std::isnan(a.first.fitness_score)) return false;
-        return a.first.fitness_score > b.first.fitness_score;
+    return VX3_OK;
+}
+
+// Positions as the worker prints them: std::to_string per coordinate, "x,y,z;" per voxel.
+std::string pos_list(const std::vector<double>& p) {
+    std::string s;
+    for (size_t i = 0; i + 2 < p.size(); i += 3)
+        s += std::to_string(p[i]) + "," + std::to_string(p[i + 1]) + "," + std::to_string(p[i + 2]) + ";";
+    return s;
+}
+
+// The worker's report (vx3_node_worker.cu:98-141), results sorted by VX3_SimulationResult::compareFitnessScore.
+int write_report_file(std::vector<ReportEntry>& rs, const char* input_dir, const char* path, std::string* err) {
+    // diverged (NaN) last, then descending fitness
+    std::stable_sort(rs.begin(), rs.end(), [](const ReportEntry& a, const ReportEntry& b) {
+        if (std::isnan(b.r.fitness_score)) return !std::isnan(a.r.fitness_score);
+        if (std::isnan(a.r.fitness_score)) return false;
+        return a.r.fitness_score > b.r.fitness_score;
     });
     std::string dir = input_dir ? input_dir : "";
     while (!dir.empty() && dir.back() == '/') dir.pop_back();
@@ -209,13 +234,13 @@ int vx3_write_report(vx3_ctx* c, const vx3_sim_id* ids, int n, const char* input
     if (slash != std::string::npos) dir = dir.substr(slash + 1);
     std::string o = "<?xml version=\"1.0\" encoding=\"utf-8\"?>\n<report><inputdir>" + gvx::xml_escape(dir) + "</inputdir>";
     if (!rs.empty())
-        o += "<bestfit><filename>" + gvx::xml_escape(rs[0].second) + "</filename><fitness_score>" + num(rs[0].first.fitness_score) +
+        o += "<bestfit><filename>" + gvx::xml_escape(rs[0].name) + "</filename><fitness_score>" + num(rs[0].r.fitness_score) +
              "</fitness_score></bestfit>";
     o += "<detail>";
     for (auto& p : rs) {
-        std::string nm = p.second.substr(0, p.second.find('.'));
-        if (nm.empty()) nm = "sim" + std::to_string(p.first.id);
-        const vx3_result& r = p.first;
+        std::string nm = p.name.substr(0, p.name.find('.'));
+        if (nm.empty()) nm = "sim" + std::to_string(p.r.id);
+        const vx3_result& r = p.r;
         o += "<" + nm + ">";
         o += "<currentTime>" + num(r.current_time) + "</currentTime>";
         o += "<fitness_score>" + num(r.fitness_score) + "</fitness_score>";
@@ -228,14 +253,42 @@ int vx3_write_report(vx3_ctx* c, const vx3_sim_id* ids, int n, const char* input
         o += "<currentCenterOfMass><x>" + num(r.current_center_of_mass[0]) + "</x><y>" + num(r.current_center_of_mass[1]) + "</y><z>" +
              num(r.current_center_of_mass[2]) + "</z></currentCenterOfMass>";
         o += "<total_distance_of_all_voxels>" + num(r.total_distance_of_all_voxels) + "</total_distance_of_all_voxels>";
+        if (p.save) {
+            o += "<init_pos>" + pos_list(p.init) + "</init_pos>";
+            o += "<pos>" + pos_list(p.cur) + "</pos>";
+            std::string m;
+            for (int id : p.mats) m += std::to_string(id) + ";";
+            o += "<mats>" + m + "</mats>";
+        }
         o += "</" + nm + ">";
     }
     o += "</detail></report>\n";
     FILE* f = fopen(path, "wb");
-    if (!f) return fail(c, VX3_E_ARG, std::string("cannot open ") + path);
+    if (!f) { *err = std::string("cannot open ") + path; return VX3_E_ARG; }
     fwrite(o.data(), 1, o.size(), f);
     fclose(f);
     return VX3_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int vx3_write_report(vx3_ctx* c, const vx3_sim_id* ids, int n, const char* input_dir, const char* path) {
+    if (!c || !path || (n > 0 && !ids)) return VX3_E_ARG;
+    std::vector<ReportEntry> rs;
+    if (int e = collect_entries(c, ids, n, &rs)) return e;
+    return write_report_file(rs, input_dir, path, &c->err);
+}
+
+int vx3_write_report_multi(vx3_ctx* const* ctxs, const vx3_sim_id* const* ids, const int* counts, int nctx, const char* input_dir,
+                           const char* path) {
+    if (!ctxs || !ids || !counts || nctx <= 0 || !path) return VX3_E_ARG;
+    std::vector<ReportEntry> rs;
+    for (int k = 0; k < nctx; k++) {
+        if (!ctxs[k] || (counts[k] > 0 && !ids[k])) return VX3_E_ARG;
+        if (int e = collect_entries(ctxs[k], ids[k], counts[k], &rs)) return e;
+    }
+    return write_report_file(rs, input_dir, path, &ctxs[0]->err);
 }
 
 int vx3_free_sim(vx3_ctx* c, vx3_sim_id id) {

@@ -86,6 +86,7 @@ struct SimRec {
     bool retired = false;
     SimResult result{};
     int n_vox_items = 0;
+    std::vector<double> final_pos;  // x block, y block, z block at finish (SavePositionOfAllVoxels only)
 };
 
 class EngineImpl final : public Engine {
@@ -811,6 +812,7 @@ public:
             tot += sqrt(dx * dx + dy * dy + dz * dz);
         }
         R.total_distance = tot;
+        if (r->w.desc.save_all_positions) r->final_pos = std::move(p);   // kept for the report's pos field
         R.submit_s = r->submit_s;
         R.start_s = r->start_s;
         r->finish_s = now_s() - t0_;
@@ -956,6 +958,38 @@ public:
             if (d9) for (int k = 0; k < 9; k++) d9[9 * (size_t)i + k] = st[(size_t)k * nl + i];
             if (f3) for (int k = 0; k < 3; k++) f3[3 * (size_t)i + k] = sf[(size_t)k * nl + i];
             if (flags) flags[i] = fl[i];
+        }
+        return 0;
+    }
+
+    int saved_positions(int64_t id, int* save, std::vector<double>* init, std::vector<double>* cur, std::vector<int>* matid,
+                        std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        *save = r->w.desc.save_all_positions;
+        if (!*save) return 0;
+        const int nv = r->w.nv;
+        // positions at finish for retired simulations, else the current device state (x block, y block, z block)
+        std::vector<double> p = r->final_pos;
+        if (p.empty()) {
+            if (!r->resident) if (int e = upload(r, err)) return e;
+            p.resize(3 * (size_t)nv);
+            CK(cudaMemcpyAsync(p.data(), r->dsim.px, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaMemcpyAsync(p.data() + nv, r->dsim.py, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaMemcpyAsync(p.data() + 2 * (size_t)nv, r->dsim.pz, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+        }
+        init->resize(3 * (size_t)nv);
+        cur->resize(3 * (size_t)nv);
+        matid->resize((size_t)nv);
+        for (int i = 0; i < nv; i++) {
+            const int mi = r->w.desc.voxels[4 * i + 3];
+            const double nom = r->w.vmats[mi].nom;
+            for (int k = 0; k < 3; k++) {
+                (*init)[3 * (size_t)i + k] = r->w.desc.voxels[4 * i + k] * nom;
+                (*cur)[3 * (size_t)i + k] = p[(size_t)k * nv + i];
+            }
+            (*matid)[i] = mi + 1;   // palette index 0 is the empty material (VX_Object.cpp:149-158, 486)
         }
         return 0;
     }

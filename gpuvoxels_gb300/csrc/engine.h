@@ -70,6 +70,10 @@ public:
     virtual int info(int64_t id, int* nv, int* nl, double* dt, double* t, int64_t* steps, int* status) = 0;
     virtual int voxel_state(int64_t id, double* d13, float* f4, int32_t* flags, std::string* err) = 0;
     virtual int link_state(int64_t id, double* d9, float* f3, int32_t* flags, std::string* err) = 0;
+    // Report extras of VXA Simulator/SavePositionOfAllVoxels: initial and current voxel positions
+    // (x,y,z per voxel) and palette material ids (1-based); *save = the VXA flag (vectors untouched if 0).
+    virtual int saved_positions(int64_t id, int* save, std::vector<double>* init, std::vector<double>* cur,
+                                std::vector<int>* matid, std::string* err) = 0;
     virtual int free_sim(int64_t id) = 0;
     virtual const Timing& timing() const = 0;
     virtual void set_profiling(int on) = 0;

@@ -89,7 +89,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     }
 
     // updateStrain
-    const float axial = (float)(pos2.x / restLen);
+    const float axial = d2f(pos2.x / restLen);
     float stress;
     strain = axial;
     if (m.linear) {
@@ -113,7 +113,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     } else {
         // the float beam constants enter as exactly widened doubles (b1*pos2.y is float*double in the reference)
         const double b1 = m.b1D, b2 = m.b2D, b3 = m.b3D, a2 = m.a2D;
-        fN = D3((double)(stress * A), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
+        fN = D3(f2d(stress * A), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
         fP = D3(-fN.x, -fN.y, -fN.z);
         mN = D3(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (mul2(a1v.y) + a2v.y), b2 * pos2.y - b3 * (mul2(a1v.z) + a2v.z));
         mP = D3(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + mul2(a2v.y)), b2 * pos2.y - b3 * (a1v.z + mul2(a2v.z)));
@@ -124,7 +124,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
             const double sqA1 = m.sqA1D, sqA2xIp = m.sqA2xIpD, sqB1 = m.sqB1D, sqB2xFMp = m.sqB2xFMpD, sqB3xIp = m.sqB3xIpD;
             const d3 pc = D3(sqA1 * dP.x, sqB1 * dP.y - sqB2xFMp * (d1.z + d2.z), sqB1 * dP.z + sqB2xFMp * (d1.y + d2.y));
             const float dmNf = vN.dampNum / dt, dmPf = vP.dampNum / dt;   // CVX_Voxel::dampingMultiplier
-            const double dmN = dmNf, dmP = dmPf;
+            const double dmN = f2d(dmNf), dmP = f2d(dmPf);
             fN = D3(fN.x + dmN * pc.x, fN.y + dmN * pc.y, fN.z + dmN * pc.z);
             fP = D3(fP.x - dmP * pc.x, fP.y - dmP * pc.y, fP.z - dmP * pc.z);
             const double hN = half(dmN), hP = half(dmP);
@@ -184,8 +184,8 @@ __global__ void __launch_bounds__(256) k_links(const Sim* __restrict__ sims, Ctl
 __device__ __forceinline__ bool pair_force(const Sim& S, int a, int b, float* f3) {
     const VMat& ma = S.vm[__ldg(S.vmat + a)];
     const VMat& mb = S.vm[__ldg(S.vmat + b)];
-    const float ox = (float)(S.px[b] - S.px[a]), oy = (float)(S.py[b] - S.py[a]), oz = (float)(S.pz[b] - S.pz[a]);
-    const float nomDist = (float)((base_size_avg(ma, S.temp[a]) + base_size_avg(mb, S.temp[b])) * S.env_radius);
+    const float ox = d2f(S.px[b] - S.px[a]), oy = d2f(S.py[b] - S.py[a]), oz = d2f(S.pz[b] - S.pz[a]);
+    const float nomDist = d2f((base_size_avg(ma, S.temp[a]) + base_size_avg(mb, S.temp[b])) * S.env_radius);
     const float len = sqrtf(ox * ox + oy * oy + oz * oz);
     const float relDist = nomDist - len;
     if (!(relDist > 0)) return false;
@@ -193,7 +193,8 @@ __device__ __forceinline__ bool pair_force(const Sim& S, int a, int b, float* f3
     if (len > 0) { const float inv = 1.0f / len; ux = inv * ox; uy = inv * oy; uz = inv * oz; }
     const double vax = S.mx[a] * ma.massInv, vay = S.my[a] * ma.massInv, vaz = S.mz[a] * ma.massInv;
     const double vbx = S.mx[b] * mb.massInv, vby = S.my[b] * mb.massInv, vbz = S.mz[b] * mb.massInv;
-    const float rv = (float)((vax * (double)ux + vay * (double)uy + vaz * (double)uz) - (vbx * (double)ux + vby * (double)uy + vbz * (double)uz));
+    const double dux = f2d(ux), duy = f2d(uy), duz = f2d(uz);
+    const float rv = d2f((vax * dux + vay * duy + vaz * duz) - (vbx * dux + vby * duy + vbz * duz));
     const float k = 2.0f / (1.0f / ma.penStiff + 1.0f / mb.penStiff);
     const float cd = 0.5f * (ma.cDampT + mb.cDampT);
     const float f = k * relDist + cd * rv;
@@ -301,7 +302,8 @@ __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, 
 // (Voxelyze3/src/old/VX_Voxel.cpp:163-297), then the Poisson strain the next
 // step's links will read (CVX_Voxel::strain(true), :299-333) and the next
 // step's actuation temperature (VX3_VoxelyzeKernel.cu:625-650).
-__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, double t_next, int flags, double* com4, int* hash_next_table) {
+// t_cycles = t_next / TempPeriod, the same quotient for every voxel of the simulation.
+__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, double t_cycles, int flags, double* com4, int* hash_next_table) {
     const int nv = S.nv;
     const VMat& m = S.vm[__ldg(S.vmat + v)];
     uint32_t fl = S.vfl[v];
@@ -339,20 +341,20 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         const bool floor = flags & SF_FLOOR;
         // CVX_Voxel::floorPenetration; pos is unchanged until the translation below, so the
         // reference's second evaluation (VX_Voxel.cpp:188) yields this same value
-        const float pen = floor ? (float)(half(base_size_avg(m, temp)) - m.halfNom - pos.z) : -1.0f;
+        const float pen = floor ? d2f(half(base_size_avg(m, temp)) - m.halfNom - pos.z) : -1.0f;
         if (floor) {
             if (pen >= 0) {
                 const float normal = m.penStiff * pen;
-                F.z += normal - m.cDampTD * vz;
+                F.z += f2d(normal) - m.cDampTD * vz;
                 if (fl & VF_STATIC) {
-                    const float surf = (float)(F.x * F.x + F.y * F.y);
+                    const float surf = d2f(F.x * F.x + F.y * F.y);
                     const float fr = (m.mus * normal) * (m.mus * normal);
                     if (surf > fr) fl &= ~VF_STATIC;
                 } else {
-                    const double hl = sqrt(vx * vx + vy * vy + 0.0 * 0.0);
+                    const double hl = sqrt(fp64i::plus_zero(vx * vx + vy * vy));   // + 0.0 * 0.0
                     double nx = vx, ny = vy, nz = 0.0;
-                    if (hl > 0) { const double inv = 1.0 / hl; nx = inv * vx; ny = inv * vy; nz = inv * 0.0; }
-                    const float k = m.muk * normal;
+                    if (fp64i::gt0(hl)) { const double inv = 1.0 / hl; nx = inv * vx; ny = inv * vy; nz = inv * 0.0; }
+                    const double k = f2d(m.muk * normal);
                     F = D3(F.x - k * nx, F.y - k * ny, F.z - k * nz);
                 }
             } else {
@@ -360,13 +362,14 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
             }
         }
         const d3 fric = D3(F.x - F0.x, F.y - F0.y, F.z - F0.z);
-        lm = D3(lm.x + dt * F.x, lm.y + dt * F.y, lm.z + dt * F.z);
-        const float sdt = dt * m.massInv;
+        const double dtd = f2d(dt);
+        lm = D3(lm.x + dtd * F.x, lm.y + dtd * F.y, lm.z + dtd * F.z);
+        const double sdt = f2d(dt * m.massInv);
         d3 tr = D3(sdt * lm.x, sdt * lm.y, sdt * lm.z);
         if (floor && pen >= 0) {
             const double work = fric.x * tr.x + fric.y * tr.y;
             const double hKe = m.halfMassInv * (lm.x * lm.x + lm.y * lm.y);
-            if (hKe + work <= 0) fl |= VF_STATIC;
+            if (fp64i::le(hKe + work, 0.0)) fl |= VF_STATIC;
             if (fl & VF_STATIC) { lm.x = lm.y = 0; tr.x = tr.y = 0; }
         } else {
             fl &= ~VF_STATIC;
@@ -382,8 +385,8 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         if (e) { M.x += e->m[0]; M.y += e->m[1]; M.z += e->m[2]; }
         const double wx = m.IinvD * am.x, wy = m.IinvD * am.y, wz = m.IinvD * am.z;
         M = D3(M.x - m.gDampRD * wx, M.y - m.gDampRD * wy, M.z - m.gDampRD * wz);
-        am = D3(am.x + dt * M.x, am.y + dt * M.y, am.z + dt * M.z);
-        const float sI = dt * m.Iinv;
+        am = D3(am.x + dtd * M.x, am.y + dtd * M.y, am.z + dtd * M.z);
+        const double sI = f2d(dt * m.Iinv);
         q = qmul(q_from_rotvec(D3(sI * am.x, sI * am.y, sI * am.z)), q);
         if (e) {
             const int d = e->dof;
@@ -429,7 +432,7 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         if (!(ten[0] && ten[1] && ten[2])) {
             float add = 0;
             for (int i = 0; i < 3; i++) if (ten[i]) add += s[i];
-            const float value = (float)pow((double)(1.0f + add), (double)(-m.nu)) - 1.0f;
+            const float value = d2f(pow(f2d(1.0f + add), f2d(-m.nu))) - 1.0f;
             for (int i = 0; i < 3; i++) if (!ten[i]) s[i] = value;
         }
         S.ps[v] = s[0]; S.ps[nv + v] = s[1]; S.ps[2 * nv + v] = s[2];
@@ -437,9 +440,9 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
     // actuation temperature for the next step
     if (flags & SF_VARY) {
         const float two_pi = 2 * 3.1415926f;
-        double T = S.temp_amp * sin((double)two_pi * (t_next / S.temp_period + __ldg(S.phase + v)));
-        if (!(flags & SF_EXPAND) && T > 0) T = 0;
-        S.temp[v] = (float)T;
+        double T = S.temp_amp * sin((double)two_pi * (t_cycles + __ldg(S.phase + v)));
+        if (!(flags & SF_EXPAND) && fp64i::gt0(T)) T = 0;
+        S.temp[v] = d2f(T);
     }
     if ((flags & SF_COLLIDE) && !(fl & VF_INTERIOR)) {
         // insert into the table the next step's contact pass reads
@@ -510,6 +513,7 @@ __global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims,
                                                 int* tickets, double* partials) {
     __shared__ int s_item, s_last;
     __shared__ double red[256];
+    __shared__ double s_cycles;
     if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
     for (;;) {
         const int it = claim(&tickets[2], &s_item);
@@ -521,13 +525,17 @@ __global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims,
         const bool div = c.diverged;
         const float dt = c.dt;
         const double t_next = c.t + dt;
+        // one FP64 division per item instead of one per voxel
+        if (threadIdx.x == 0) s_cycles = (S.flags & SF_VARY) ? t_next / S.temp_period : 0.0;
+        __syncthreads();
+        const double t_cycles = s_cycles;
         const int64_t stepno = c.steps + 1;
         const bool com_step = c.cycle_step > 0 && (stepno % c.cycle_step) == 0;
         const int flags = S.flags;
         int* hnext = (flags & SF_COLLIDE) ? S.hash_head + (size_t)(c.hash_parity ^ 1) * S.hash_size : nullptr;
         double acc[4] = {0, 0, 0, 0};
         if (!div && dt != 0.0f)
-            for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, t_next, flags, com_step ? acc : nullptr, hnext);
+            for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, t_cycles, flags, com_step ? acc : nullptr, hnext);
         if (com_step) {
             for (int k = 0; k < 4; k++) {
                 const double r = block_sum(acc[k], red);

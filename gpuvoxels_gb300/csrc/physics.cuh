@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fp64_int.cuh"
 #include "layout.cuh"
 
 #ifndef GVX_KNS
@@ -28,24 +29,12 @@ __device__ __forceinline__ d3 D3(double x, double y, double z) { d3 r; r.x = x; 
 __device__ __forceinline__ q4 Q4(double w, double x, double y, double z) { q4 r; r.w = w; r.x = x; r.y = y; r.z = z; return r; }
 
 // ---------------------------------------------------- exact FP64 shortcuts
-// GB300 issues FP64 arithmetic at 2 instructions/clock/SM, integer arithmetic at
-// 64.  Scaling by 2 or 1/2 only changes the exponent, so it is done on the
-// integer pipes when that is exact; the result is bit-identical to the FP64
-// multiply in every case (zero, subnormal, overflow fall back to it).
-__device__ __forceinline__ double mul2(double x) {
-    const long long b = __double_as_longlong(x);
-    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-    if (e - 1u < 0x7FDu) return __longlong_as_double(b + (1LL << 52));   // 1 <= e <= 0x7FD: normal, no overflow
-    if (e == 0u) return __longlong_as_double((b & (long long)0x8000000000000000ULL) | ((b & 0x7FFFFFFFFFFFFFFFLL) << 1));
-    return x * 2.0;
-}
-__device__ __forceinline__ double half(double x) {
-    const long long b = __double_as_longlong(x);
-    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-    if (e - 2u < 0x7FDu) return __longlong_as_double(b - (1LL << 52));   // 2 <= e <= 0x7FE: result stays normal
-    if ((b & 0x7FFFFFFFFFFFFFFFLL) == 0) return x;                       // +-0
-    return x * 0.5;
-}
+// Scaling by 2 or 1/2, float<->double conversions and FP64 comparisons run on the
+// integer pipes (fp64_int.cuh); results are bit-identical to the FP64 instructions.
+using fp64i::mul2;
+using fp64i::half;
+using fp64i::f2d;
+using fp64i::d2f;
 
 // (float)(n/d) compared with a float threshold T, deciding with one multiply
 // unless n/d lies within 2^-20 (relative) of T, where the quotient is formed
@@ -53,32 +42,32 @@ __device__ __forceinline__ double half(double x) {
 // decision equals the reference's (float)(n/d) < T (or > T).
 __device__ __forceinline__ bool quot_lt(double n, double d, float T) {
     const double t = T;
-    if (d > 0) {
-        if (n < (t * (1.0 - 0x1p-20)) * d) return true;
-        if (n > (t * (1.0 + 0x1p-20)) * d) return false;
+    if (fp64i::gt0(d)) {
+        if (fp64i::lt(n, (t * (1.0 - 0x1p-20)) * d)) return true;
+        if (fp64i::gt(n, (t * (1.0 + 0x1p-20)) * d)) return false;
     }
-    return (float)(n / d) < T;
+    return d2f(n / d) < T;
 }
 __device__ __forceinline__ bool quot_gt(double n, double d, float T) {
     const double t = T;
-    if (d > 0) {
-        if (n > (t * (1.0 + 0x1p-20)) * d) return true;
-        if (n < (t * (1.0 - 0x1p-20)) * d) return false;
+    if (fp64i::gt0(d)) {
+        if (fp64i::gt(n, (t * (1.0 + 0x1p-20)) * d)) return true;
+        if (fp64i::lt(n, (t * (1.0 - 0x1p-20)) * d)) return false;
     }
-    return (float)(n / d) > T;
+    return d2f(n / d) > T;
 }
 // (float)fabs(1 - x/r) < T and > T for r > 0, with the same band rule (T < 1).
 __device__ __forceinline__ bool ext_lt(double x, double r, float T) {
     const double t = T;
-    if (x > ((1.0 - t) * (1.0 + 0x1p-20)) * r && x < ((1.0 + t) * (1.0 - 0x1p-20)) * r) return true;
-    if (x < ((1.0 - t) * (1.0 - 0x1p-20)) * r || x > ((1.0 + t) * (1.0 + 0x1p-20)) * r) return false;
-    return (float)(fabs(1 - x / r)) < T;
+    if (fp64i::gt(x, ((1.0 - t) * (1.0 + 0x1p-20)) * r) && fp64i::lt(x, ((1.0 + t) * (1.0 - 0x1p-20)) * r)) return true;
+    if (fp64i::lt(x, ((1.0 - t) * (1.0 - 0x1p-20)) * r) || fp64i::gt(x, ((1.0 + t) * (1.0 + 0x1p-20)) * r)) return false;
+    return d2f(fabs(1 - x / r)) < T;
 }
 __device__ __forceinline__ bool ext_gt(double x, double r, float T) {
     const double t = T;
-    if (x > ((1.0 - t) * (1.0 + 0x1p-20)) * r && x < ((1.0 + t) * (1.0 - 0x1p-20)) * r) return false;
-    if (x < ((1.0 - t) * (1.0 - 0x1p-20)) * r || x > ((1.0 + t) * (1.0 + 0x1p-20)) * r) return true;
-    return (float)(fabs(1 - x / r)) > T;
+    if (fp64i::gt(x, ((1.0 - t) * (1.0 + 0x1p-20)) * r) && fp64i::lt(x, ((1.0 + t) * (1.0 - 0x1p-20)) * r)) return false;
+    if (fp64i::lt(x, ((1.0 - t) * (1.0 - 0x1p-20)) * r) || fp64i::gt(x, ((1.0 + t) * (1.0 + 0x1p-20)) * r)) return true;
+    return d2f(fabs(1 - x / r)) > T;
 }
 
 // Quat3D::operator*  Voxelyze3/src/old/Quat3D.h:87
@@ -110,9 +99,9 @@ __device__ __forceinline__ d3 qrotinv(const q4& q, const d3& f) {
 }
 // Quat3D::ToRotationVector  Quat3D.h:121-126
 __device__ __forceinline__ d3 q_to_rotvec(const q4& q) {
-    if (q.w >= 1.0 || q.w <= -1.0) return D3(0, 0, 0);
+    if (fp64i::ge(fabs(q.w), 1.0)) return D3(0, 0, 0);   // q.w >= 1 || q.w <= -1
     double sl = 1.0 - q.w * q.w;
-    if (sl < 2.4e-3) {
+    if (fp64i::lt(sl, 2.4e-3)) {
         double s = sqrt((2 - mul2(q.w)) / sl);
         return D3(mul2(q.x) * s, mul2(q.y) * s, mul2(q.z) * s);
     }
@@ -125,7 +114,7 @@ __device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
     double tx = half(v.x), ty = half(v.y), tz = half(v.z);
     double m2 = tx * tx + ty * ty + tz * tz;
     double w, s;
-    if (m2 * m2 < 5.328e-15) {
+    if (fp64i::lt(m2 * m2, 5.328e-15)) {
         w = 1.0 - half(m2);
         s = 1.0 - m2 / 6.0;
     } else {
@@ -139,17 +128,17 @@ __device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
 }
 // Quat3D::FromAngleToPosX  Quat3D.h:145-170; `cur` is returned for a zero vector
 __device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r) {
-    if (r.x == 0 && r.y == 0 && r.z == 0) return cur;
+    if (fp64i::eq0(r.x) && fp64i::eq0(r.y) && fp64i::eq0(r.z)) return cur;
     double yox = r.y / r.x, zox = r.z / r.x;
-    if (yox < 1.732e-2 && yox > -1.732e-2 && zox < 1.732e-2 && zox > -1.732e-2) {
+    if (fp64i::lt(fabs(yox), 1.732e-2) && fp64i::lt(fabs(zox), 1.732e-2)) {   // |yox|, |zox| < 1.732e-2
         double y = half(zox), z = -half(yox);
         return Q4(1 + half(-y * y - z * z), 0, y, z);
     }
     double l = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
     double nx = r.x, ny = r.y, nz = r.z;
-    if (l > 0) { double li = 1.0 / l; nx *= li; ny *= li; nz *= li; }
+    if (fp64i::gt0(l)) { double li = 1.0 / l; nx *= li; ny *= li; nz *= li; }
     double theta = acos(nx);
-    if (theta > 3.14159265358979 - 1e-7) return Q4(0, 0, 1, 0);
+    if (fp64i::gt(theta, 3.14159265358979 - 1e-7)) return Q4(0, 0, 1, 0);
     double ami = 1.0 / sqrt(nz * nz + ny * ny);
     double a = half(theta);
     double sn, cs;
@@ -197,7 +186,7 @@ __device__ __forceinline__ float mat_stress(const LMat& m, float strain, float t
 }
 
 // CVX_Voxel::baseSize(axis) and baseSizeAverage  Voxelyze3/src/old/VX_Voxel.h:91-92
-__device__ __forceinline__ double base_size(const VMat& m, float temp) { return m.nom * (double)(1 + temp * m.cte); }
+__device__ __forceinline__ double base_size(const VMat& m, float temp) { return m.nom * f2d(1 + temp * m.cte); }
 __device__ __forceinline__ double base_size_avg(const VMat& m, float temp) {
     double b = base_size(m, temp);
     return (b + b + b) / 3.0f;
@@ -206,7 +195,7 @@ __device__ __forceinline__ double base_size_avg(const VMat& m, float temp) {
 __device__ __forceinline__ float voxel_tarea(const VMat& m, float psa, float psb) {
     float size = m.sizef;
     if (m.nu == 0) return size * size;
-    return (float)(size * size * (1 + (double)psa) * (1 + (double)psb));
+    return d2f(f2d(size * size) * (1 + f2d(psa)) * (1 + f2d(psb)));
 }
 // CVX_Voxel::transverseStrainSum  VX_Voxel.cpp:345-358
 __device__ __forceinline__ float voxel_tss(const VMat& m, float psa, float psb) {

@@ -157,6 +157,25 @@ def config2_batch(n: int = 64, seed: int = 2, **kw) -> List[Creature]:
     return [random_creature(int(rng.integers(1 << 31)), (40, 40, 40), 0.5, mats, collision=True, **kw) for _ in range(n)]
 
 
+def serving_requests(n: int = 64, seed: int = 4, v_range=(100, 10000), horizon_range=(1000, 5000),
+                     collide_frac: float = 0.2) -> List[tuple]:
+    """Serving requests: (creature, horizon_steps) with the voxel count log-uniform in v_range,
+    the horizon uniform in horizon_range and a fraction with self-collision on (contraction-only
+    actuation for those).  Cubic lattices at fill U(0.5, 0.9), largest component kept."""
+    rng = np.random.default_rng(seed)
+    mats = [PASSIVE, ACTIVE]
+    out = []
+    for _ in range(n):
+        v = math.exp(rng.uniform(math.log(v_range[0]), math.log(v_range[1])))
+        fill = float(rng.uniform(0.5, 0.9))
+        s = max(2, int(round((v / fill) ** (1.0 / 3.0))))
+        collide = bool(rng.random() < collide_frac)
+        kw = dict(collision=True, expansion=False) if collide else {}
+        c = random_creature(int(rng.integers(1 << 31)), (s, s, s), fill, mats, **kw)
+        out.append((c, int(rng.integers(horizon_range[0], horizon_range[1] + 1))))
+    return out
+
+
 def slab(X: int = 200, Y: int = 200, Z: int = 100, seed: int = 3, **kw) -> Creature:
     """Single large body: a solid X x Y x Z slab of one actuated material (E=1e6), random phases."""
     rng = np.random.default_rng(seed)

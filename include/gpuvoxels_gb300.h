@@ -121,8 +121,14 @@ int vx3_get_link_state(vx3_ctx* ctx, vx3_sim_id id, double* d9, float* f3, int32
 
 /* Replaces the worker's report (Executables/vx3_node_worker.cu:98-141): report.inputdir,
  * report.bestfit.{filename,fitness_score}, report.detail.<name>.{...}; results sorted by
- * fitness with NaN last (VX3_SimulationResult.h:26-33). */
+ * fitness with NaN last (VX3_SimulationResult.h:26-33).  A simulation whose VXA sets
+ * Simulator/SavePositionOfAllVoxels also gets init_pos, pos and mats (vx3_node_worker.cu:123-139). */
 int vx3_write_report(vx3_ctx* ctx, const vx3_sim_id* ids, int n, const char* input_dir, const char* path);
+/* One report over the simulations of several contexts (one per GPU), as the worker writes a
+ * single report after dealing files across devices (vx3_node_worker.cu:88-98).  ids[k] lists
+ * counts[k] simulations of ctxs[k]; errors are left in ctxs[0]. */
+int vx3_write_report_multi(vx3_ctx* const* ctxs, const vx3_sim_id* const* ids, const int* counts, int nctx,
+                           const char* input_dir, const char* path);
 
 /* Releases a simulation's device memory and host state. */
 int vx3_free_sim(vx3_ctx* ctx, vx3_sim_id id);
