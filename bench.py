@@ -47,6 +47,38 @@ def measured_peaks():
     return HBM_PEAK_FALLBACK, "fallback"
 
 
+# FP64-pipe thread instructions (DADD/DMUL/DFMA, compares, conversions; predicated-on lanes)
+# per link and per voxel of one step of the batch workload, read by ncu at step 205
+# (sm__thread_inst_executed_pipe_fp64_pred_on.sum ÷ links or voxels; profiles/k_links_k_voxels_batch512_steady.md).
+FP64_INSTR_PER_LINK = 478.0
+FP64_INSTR_PER_VOXEL = 320.0
+# DRAM bytes per link of one k_links launch at the same step (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum = 388.2 MB + 336.6 MB for 1,627,115 links).
+LINK_TRAFFIC_PER_LINK = (388222720 + 336599040) / 1627115
+
+
+def fp64_peak_fma_per_s(device=0):
+    """FP64 FMA throughput of this GPU, measured live with a cuBLAS DGEMM (4096^3, best of 3):
+    the denominator of the FP64 roofline, as the HBM copy and the bf16 GEMM are for the others."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
+    b = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return n ** 3 / best
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
@@ -240,6 +272,20 @@ def run_ours(args):
     achieved = dom_b / (dom_ms / 1e3) / 1e9
     n_links = sum(ctx.info(i).num_link for i in ids)
     n_vox = sum(ctx.info(i).num_voxel for i in ids)
+    # ---- the FP64 roofline that actually bounds both step kernels
+    fp64 = None
+    if args.workload == "batch":
+        try:
+            peak64 = fp64_peak_fma_per_s(local)
+            ach_l = FP64_INSTR_PER_LINK * n_links / (link_ms / 1e3)
+            ach_v = FP64_INSTR_PER_VOXEL * n_vox / (vox_ms / 1e3)
+            fp64 = {"bound": "fp64", "kernel": "k_links", "achieved": ach_l / 1e9, "peak": peak64 / 1e9,
+                    "unit": "G FP64 thread-instructions/s", "frac": ach_l / peak64,
+                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FMA/s)",
+                    "instr_per_link": FP64_INSTR_PER_LINK, "k_voxels_achieved": ach_v / 1e9, "k_voxels_frac": ach_v / peak64,
+                    "instr_per_voxel": FP64_INSTR_PER_VOXEL}
+        except Exception as e:   # the FP64 roofline is reported beside the HBM one; its absence is not fatal
+            fp64 = {"unavailable": str(e)[:200]}
     # ---- plain one-simulation-per-launch form of the same kernels, on a sample of the batch
     plain = None
     if args.workload == "batch" and rank == 0:
@@ -258,7 +304,7 @@ def run_ours(args):
         c2 = g.Context(local, budget)
         c2.set_precision(prec)
         t0 = time.perf_counter()
-        ids2 = [c2.load_vxa(c.vxa, name=f"c{i}") for i, c in enumerate(cs)]
+        ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
         c2.step(ids2, args.steps, g.BATCHED)
         d2h = 0
         for i in ids2:
@@ -292,9 +338,13 @@ def run_ours(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                     "traffic": None, "algorithmic_bytes_per_launch": dom_b, "kernel_ms": dom_ms,
+                     "algorithmic_bytes_per_launch": dom_b, "kernel_ms": dom_ms,
                      "link_kernel_ms": link_ms, "voxel_kernel_ms": vox_ms, "contact_kernel_ms": con_ms,
-                     "note": "the step is FP64-issue bound on GB300 (measured 505.8 G FP64 instr/s); see fp64 and DESIGN.md"},
+                     "traffic": LINK_TRAFFIC_PER_LINK * n_links if dom == "k_links" else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per k_links launch at step 205, "
+                                       "per link, times this run's links",
+                     "fp64": fp64,
+                     "note": "the step kernels are bound by GB300's FP64 pipe, not by HBM: see roofline.fp64"},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "wall_s_timed": wall,

@@ -35,7 +35,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
-           "vx3_write_report_multi"]
+           "vx3_write_report_multi", "vx3_load_vxa_many"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -91,6 +91,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_inspect_formula": (I, [S, S, I, P, P]),
         "vx3_center_of_mass_noalloc": (I, [P, P, P, P, I64, P, P]),
         "vx3_write_report_multi": (I, [P, P, P, I, S, S]),
+        "vx3_load_vxa_many": (I, [P, S, P, P, I, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -177,6 +178,23 @@ class Context:
         self._check(self.L.vx3_load_vxa(self.h, _b(base_xml), _b(vxd_xml), name.encode(), ctypes.byref(out)))
         self.names[out.value] = name
         return out.value
+
+    def load_many(self, docs: Sequence[str], base: Optional[str] = None, names: Optional[Sequence[str]] = None) -> List[int]:
+        """Loads many simulations, parsed and built on host threads: each of `docs` is a VXD
+        merged into `base`, or a whole VXA when `base` is None."""
+        n = len(docs)
+        names = list(names) if names is not None else [""] * n
+        enc = [d.encode() for d in docs]
+        cdocs = (ctypes.c_char_p * n)(*enc)
+        cnames = (ctypes.c_char_p * n)(*[s.encode() for s in names])
+        ids = np.full(n, -1, np.int64)
+        st = np.zeros(n, np.int32)
+        self._check(self.L.vx3_load_vxa_many(self.h, _b(base), ctypes.cast(cdocs, ctypes.c_void_p),
+                                             ctypes.cast(cnames, ctypes.c_void_p), n, _p(ids), _p(st)))
+        out = [int(i) for i in ids]
+        for i, nm in zip(out, names):
+            self.names[i] = nm
+        return out
 
     def set_external(self, sim: int, voxel: int, dof_fixed: int = 0, force=(0, 0, 0), moment=(0, 0, 0),
                      translate=(0, 0, 0), rotate=(0, 0, 0)):

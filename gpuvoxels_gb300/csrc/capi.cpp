@@ -2,11 +2,13 @@
 #include "../../include/gpuvoxels_gb300.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -79,6 +81,54 @@ int vx3_load_vxa(vx3_ctx* c, const char* base, const char* vxd, const char* name
     c->names[id] = d.name;
     *out = id;
     return VX3_OK;
+}
+
+int vx3_load_vxa_many(vx3_ctx* c, const char* base, const char* const* vxds, const char* const* names, int n, vx3_sim_id* ids,
+                      int* status) {
+    if (!c || !ids || n < 0 || (!base && !vxds)) return fail(c, VX3_E_ARG, "null argument");
+    if (!base)
+        for (int i = 0; i < n; i++)
+            if (!vxds[i]) return fail(c, VX3_E_ARG, "without a base every entry must be a whole VXA");
+    std::vector<gvx::SimDesc> descs((size_t)n);
+    std::vector<std::string> errs((size_t)n);
+    std::vector<int> rc((size_t)n, VX3_OK);
+    // parse on host threads: each VXD merged into its own copy of the base
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        for (int i = next++; i < n; i = next++) {
+            const bool ok = base ? gvx::parse_vxa(base, vxds ? vxds[i] : nullptr, &descs[i], &errs[i])
+                                 : gvx::parse_vxa(vxds[i], nullptr, &descs[i], &errs[i]);
+            if (!ok) rc[i] = VX3_E_PARSE;
+            descs[i].name = (names && names[i]) ? names[i] : "";
+        }
+    };
+    const int nt = std::max(1, std::min(n, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    std::vector<const gvx::SimDesc*> ok;
+    std::vector<int> where;
+    for (int i = 0; i < n; i++)
+        if (rc[i] == VX3_OK) { ok.push_back(&descs[i]); where.push_back(i); }
+    std::vector<int64_t> got(ok.size());
+    std::vector<std::string> berr(ok.size());
+    c->eng->add_sims(ok.data(), (int)ok.size(), got.data(), berr.data());
+    for (size_t k = 0; k < ok.size(); k++) {
+        const int i = where[k];
+        if (got[k] < 0) { rc[i] = VX3_E_PARSE; errs[i] = berr[k]; continue; }
+        ids[i] = got[k];
+        c->names[got[k]] = descs[i].name;
+    }
+    int first = VX3_OK;
+    for (int i = 0; i < n; i++) {
+        if (rc[i] != VX3_OK) {
+            ids[i] = -1;
+            if (first == VX3_OK) { first = rc[i]; c->err = "simulation " + std::to_string(i) + ": " + errs[i]; }
+        }
+        if (status) status[i] = rc[i];
+    }
+    return first;
 }
 
 int vx3_set_external(vx3_ctx* c, vx3_sim_id id, int voxel, int dof, const float force[3], const float moment[3],

@@ -5,10 +5,12 @@
 #include "layout.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <thread>
 
 namespace gvx {
 
@@ -207,7 +209,7 @@ public:
 
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
-        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext;
+        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos;
         int hash_size;
     };
     static void compute_layout(const SimWorld& w, Layout* L, Offs* o) {
@@ -249,15 +251,51 @@ public:
             t.cforce = L->add(4 * 3 * dev::kContactCap * nv);
             t.hhead = L->add(4 * 2 * (size_t)hs);
             t.hnext = L->add(4 * nv);
+            t.cpos = L->add(16 * nv);
         }
         if (o) *o = t;
     }
 
     int add_sim(const SimDesc& d, int64_t* id, std::string* err) override {
         auto r = std::make_unique<SimRec>();
-        if (!build_world(d, &r->w, err)) return -1;
+        if (!prepare(d, r.get(), err)) return -1;
         r->id = next_id_++;
         *id = r->id;
+        r->submit_s = now_s() - t0_;
+        sims_[r->id] = std::move(r);
+        return 0;
+    }
+
+    int add_sims(const SimDesc* const* descs, int n, int64_t* ids, std::string* errs) override {
+        std::vector<std::unique_ptr<SimRec>> recs((size_t)std::max(n, 0));
+        std::vector<char> ok((size_t)std::max(n, 0), 0);
+        std::atomic<int> next{0};
+        auto work = [&]() {
+            for (int i = next++; i < n; i = next++) {
+                recs[i] = std::make_unique<SimRec>();
+                ok[i] = prepare(*descs[i], recs[i].get(), &errs[i]) ? 1 : 0;
+            }
+        };
+        const int nt = std::max(1, std::min(n, (int)std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; t++) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+        int rejected = 0;
+        const double now = now_s() - t0_;
+        for (int i = 0; i < n; i++) {
+            if (!ok[i]) { ids[i] = -1; rejected++; continue; }
+            recs[i]->id = next_id_++;
+            recs[i]->submit_s = now;
+            ids[i] = recs[i]->id;
+            sims_[ids[i]] = std::move(recs[i]);
+        }
+        return rejected;
+    }
+
+    // Host part of loading one simulation (thread-safe): topology, materials, initial centre of mass.
+    static bool prepare(const SimDesc& d, SimRec* r, std::string* err) {
+        if (!build_world(d, &r->w, err)) return false;
         // initial centre of mass from the lattice positions
         double sx = 0, sy = 0, sz = 0, tm = 0;
         for (int i = 0; i < r->w.nv; i++) {
@@ -269,9 +307,7 @@ public:
             tm += wgt;
         }
         if (tm != 0) { r->init_com[0] = sx / tm; r->init_com[1] = sy / tm; r->init_com[2] = sz / tm; }
-        r->submit_s = now_s() - t0_;
-        sims_[r->id] = std::move(r);
-        return 0;
+        return true;
     }
 
     SimRec* find(int64_t id) {
@@ -438,6 +474,8 @@ public:
             S.surf = (const int32_t*)D(o.surf); S.reach = (const uint32_t*)D(o.reach);
             S.ccount = (int32_t*)D(o.ccount); S.cforce = (float*)D(o.cforce);
             S.hash_head = (int32_t*)D(o.hhead); S.hash_next = (int32_t*)D(o.hnext);
+            S.cpos = (float4*)D(o.cpos);
+            S.inv_cell = (float)(1.0 / S.cell_size);
         }
         CK(cudaMemcpyAsync(base, h.data(), L.total, cudaMemcpyHostToDevice, stream_));
         CK(cudaMemcpyAsync(d_sims_ + slot, &S, sizeof(S), cudaMemcpyHostToDevice, stream_));

@@ -56,6 +56,9 @@ class Engine {
 public:
     virtual ~Engine() = default;
     virtual int add_sim(const SimDesc& d, int64_t* id, std::string* err) = 0;
+    // Many at once: topology and materials are built on host threads; ids[i] = -1 and
+    // errs[i] set where descs[i] is rejected.  Returns the number rejected.
+    virtual int add_sims(const SimDesc* const* descs, int n, int64_t* ids, std::string* errs) = 0;
     virtual int set_external(int64_t id, const External& x, std::string* err) = 0;
     // Advance the given simulations by exactly `steps` steps each (fewer if they stop).
     virtual int step(const int64_t* ids, int n, int mode, int64_t steps, std::string* err) = 0;

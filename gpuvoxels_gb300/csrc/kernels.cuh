@@ -162,8 +162,53 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     S.ss[dp * nv + pv] = 2.0f * strain * ratio / (1.0f + ratio);
 }
 
+// Links of one work item in an order that keeps warps on one path: the large-angle
+// links of the previous step first, then the small-angle ones (stable within each
+// group).  The two paths differ by ~40% of the FP64 work and GB300's FP64 pipe
+// spends the same cycles on a warp instruction whatever its active lanes, so
+// mixed warps would pay for both.  The flag is last step's; links that switch
+// mode this step are rare (hysteresis).  Order of evaluation does not change
+// results: every link writes only its own state and its two direction slots.
+constexpr int kLinkOrderMax = 1024;   // links per item that are reordered (larger items run in index order)
+
+__device__ __forceinline__ int order_links(const Sim& S, const Item& w, int* perm, int* warp_sums) {
+    const int n = w.end - w.begin;
+    if (n > kLinkOrderMax) return 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int base_large = 0, base_small = 0;
+    int n_large = 0;
+    // count the large-angle links first, so that the small ones can start after them
+    for (int j0 = 0; j0 < n; j0 += blockDim.x) {
+        const int j = j0 + threadIdx.x;
+        const bool large = j < n && !(S.lfl[w.begin + j] & LF_SMALL);
+        const unsigned bl = __ballot_sync(0xffffffffu, large);
+        if (lane == 0) warp_sums[wid] = __popc(bl);
+        __syncthreads();
+        for (int k = 0; k < nw; k++) n_large += warp_sums[k];
+        __syncthreads();
+    }
+    for (int j0 = 0; j0 < n; j0 += blockDim.x) {
+        const int j = j0 + threadIdx.x;
+        const bool in = j < n;
+        const bool large = in && !(S.lfl[w.begin + j] & LF_SMALL);
+        const unsigned bl = __ballot_sync(0xffffffffu, large), bs = __ballot_sync(0xffffffffu, in && !large);
+        if (lane == 0) { warp_sums[wid] = __popc(bl); warp_sums[32 + wid] = __popc(bs); }
+        __syncthreads();
+        int pl = base_large, ps = base_small;
+        for (int k = 0; k < wid; k++) { pl += warp_sums[k]; ps += warp_sums[32 + k]; }
+        const unsigned below = (1u << lane) - 1u;
+        if (large) perm[pl + __popc(bl & below)] = j;
+        else if (in) perm[n_large + ps + __popc(bs & below)] = j;
+        for (int k = 0; k < nw; k++) { base_large += warp_sums[k]; base_small += warp_sums[32 + k]; }
+        __syncthreads();
+    }
+    return 1;
+}
+
 __global__ void __launch_bounds__(256) k_links(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
     __shared__ int s_item;
+    __shared__ int s_perm[kLinkOrderMax];
+    __shared__ int s_warp[64];
     if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; }
     for (;;) {
         const int it = claim(&tickets[0], &s_item);
@@ -174,7 +219,12 @@ __global__ void __launch_bounds__(256) k_links(const Sim* __restrict__ sims, Ctl
         const Sim& S = sims[w.sim];
         const float dt = c.dt;
         bool div = false;
-        for (int l = w.begin + threadIdx.x; l < w.end; l += blockDim.x) link_update(S, l, dt, &div);
+        if (order_links(S, w, s_perm, s_warp)) {
+            const int n = w.end - w.begin;
+            for (int k = threadIdx.x; k < n; k += blockDim.x) link_update(S, w.begin + s_perm[k], dt, &div);
+        } else {
+            for (int l = w.begin + threadIdx.x; l < w.end; l += blockDim.x) link_update(S, l, dt, &div);
+        }
         if (div) c.diverged = 1;
     }
 }
@@ -205,13 +255,29 @@ __device__ __forceinline__ bool pair_force(const Sim& S, int a, int b, float* f3
 __device__ __forceinline__ uint32_t cell_hash(int cx, int cy, int cz, int mask) {
     return ((uint32_t)cx * 73856093u ^ (uint32_t)cy * 19349663u ^ (uint32_t)cz * 83492791u) & (uint32_t)mask;
 }
-__device__ __forceinline__ int cell_of(double p, double cs) { return (int)floor(p / cs); }
+// The broadphase runs in FP32 on positions rounded to float: it only has to be
+// conservative (every pair the exact FP64 test accepts must be found), and the
+// same float values give the same cell at insertion and lookup.
+__device__ __forceinline__ int cell_of(float p, float inv_cell) { return (int)floorf(p * inv_cell); }
 
-__device__ __forceinline__ void hash_insert(const Sim& S, int v, int parity) {
-    const double cs = S.cell_size;
-    const uint32_t h = cell_hash(cell_of(S.px[v], cs), cell_of(S.py[v], cs), cell_of(S.pz[v], cs), S.hash_size - 1);
-    int* head = S.hash_head + (size_t)parity * S.hash_size;
+// Records voxel v (position pos, temperature temp) in hash table `head` and its
+// float position and base size in cpos for the next contact pass.
+__device__ __forceinline__ void hash_insert(const Sim& S, int v, const d3& pos, float temp, int* head) {
+    const VMat& m = S.vm[__ldg(S.vmat + v)];
+    const float4 p = make_float4(d2f(pos.x), d2f(pos.y), d2f(pos.z), m.sizef * (1.0f + temp * m.cte));
+    S.cpos[v] = p;
+    const uint32_t h = cell_hash(cell_of(p.x, S.inv_cell), cell_of(p.y, S.inv_cell), cell_of(p.z, S.inv_cell), S.hash_size - 1);
     S.hash_next[v] = atomicExch(head + h, v);
+}
+
+// Conservative FP32 overlap test: false only when the exact test (pair_force) cannot
+// accept the pair.  2% of the contact distance plus 4 float ulps of every coordinate
+// cover the float rounding of positions and base sizes.
+__device__ __forceinline__ bool maybe_touching(float4 a, float4 b, float env_radius) {
+    const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    const float lim = env_radius * (a.w + b.w) * 1.02f +
+                      2.4e-7f * (fabsf(a.x) + fabsf(a.y) + fabsf(a.z) + fabsf(b.x) + fabsf(b.y) + fabsf(b.z));
+    return dx * dx + dy * dy + dz * dz <= lim * lim;
 }
 
 // Spatial-hash broadphase + exact contact forces for one surface voxel.  The
@@ -221,8 +287,9 @@ __device__ __forceinline__ void hash_insert(const Sim& S, int v, int parity) {
 // pairs that do not overlap contribute exactly zero, so summing the
 // overlapping pairs in partner order reproduces it.
 __device__ void voxel_contacts(const Sim& S, int v, int parity, int* err) {
-    const double cs = S.cell_size;
-    const int cx = cell_of(S.px[v], cs), cy = cell_of(S.py[v], cs), cz = cell_of(S.pz[v], cs);
+    const float4 pv = S.cpos[v];
+    const float ic = S.inv_cell;
+    const int cx = cell_of(pv.x, ic), cy = cell_of(pv.y, ic), cz = cell_of(pv.z, ic);
     const int nv = S.nv;
     const int vx = S.ijk[v], vy = S.ijk[nv + v], vz = S.ijk[2 * nv + v];
     const int* head = S.hash_head + (size_t)parity * S.hash_size;
@@ -237,7 +304,9 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, int* err) {
                 int guard = 0;
                 while (q >= 0 && guard++ < nv) {
                     const int nq = S.hash_next[q];
-                    if (q != v && cell_of(S.px[q], cs) == tx && cell_of(S.py[q], cs) == ty && cell_of(S.pz[q], cs) == tz) {
+                    const float4 pq = S.cpos[q];
+                    if (q != v && cell_of(pq.x, ic) == tx && cell_of(pq.y, ic) == ty && cell_of(pq.z, ic) == tz &&
+                        maybe_touching(pv, pq, S.env_radius)) {
                         // lattice exclusion: within 5 links of each other
                         const int ox = S.ijk[q] - vx, oy = S.ijk[nv + q] - vy, oz = S.ijk[2 * nv + q] - vz;
                         const int l1 = abs(ox) + abs(oy) + abs(oz);
@@ -438,18 +507,16 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         S.ps[v] = s[0]; S.ps[nv + v] = s[1]; S.ps[2 * nv + v] = s[2];
     }
     // actuation temperature for the next step
+    float temp_next = temp;
     if (flags & SF_VARY) {
         const float two_pi = 2 * 3.1415926f;
         double T = S.temp_amp * sin((double)two_pi * (t_cycles + __ldg(S.phase + v)));
         if (!(flags & SF_EXPAND) && fp64i::gt0(T)) T = 0;
-        S.temp[v] = d2f(T);
+        temp_next = d2f(T);
+        S.temp[v] = temp_next;
     }
-    if ((flags & SF_COLLIDE) && !(fl & VF_INTERIOR)) {
-        // insert into the table the next step's contact pass reads
-        const double cs = S.cell_size;
-        const uint32_t h = cell_hash(cell_of(pos.x, cs), cell_of(pos.y, cs), cell_of(pos.z, cs), S.hash_size - 1);
-        S.hash_next[v] = atomicExch(hash_next_table + h, v);
-    }
+    // insert into the table the next step's contact pass reads
+    if ((flags & SF_COLLIDE) && !(fl & VF_INTERIOR)) hash_insert(S, v, pos, temp_next, hash_next_table);
 }
 
 __device__ __forceinline__ double block_sum(double x, double* red) {
@@ -594,8 +661,11 @@ __global__ void k_init_temp(const Sim* __restrict__ sims, int sim, float initial
 
 __global__ void k_hash_build(const Sim* __restrict__ sims, Ctl* ctl, int sim) {
     const Sim& S = sims[sim];
-    const int parity = ctl[sim].hash_parity;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nsurf; i += gridDim.x * blockDim.x) hash_insert(S, S.surf[i], parity);
+    int* head = S.hash_head + (size_t)ctl[sim].hash_parity * S.hash_size;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nsurf; i += gridDim.x * blockDim.x) {
+        const int v = S.surf[i];
+        hash_insert(S, v, D3(S.px[v], S.py[v], S.pz[v]), S.temp[v], head);
+    }
 }
 
 // Mass-weighted centre of mass of measured voxels (VX3_VoxelyzeKernel::updateCurrentCenterOfMass,

@@ -94,6 +94,8 @@ struct Sim {
     float* cforce;              // 3*kContactCap per voxel
     int32_t* hash_head;         // 2 tables of hash_size
     int32_t* hash_next;         // per voxel
+    float4* cpos;               // per hashed voxel: position rounded to float, float base size (broadphase only)
+    float inv_cell;             // 1 / cell_size, for the float cell index
 };
 
 // Mutable per-simulation control block.

@@ -68,18 +68,24 @@ struct DeviceJob {
 void run_device(DeviceJob* job, const std::string* base_xml, const std::string* input_dir) {
     job->ctx = vx3_create(job->device, 0);
     if (!job->ctx) { job->rc = VX3_E_CUDA; return; }
+    std::vector<std::string> texts, names;
     for (const std::string& f : job->files) {
         std::string vxd;
         if (!slurp(join(*input_dir, f), &vxd)) {
             fprintf(stderr, "%s: cannot read\n", f.c_str());
             continue;
         }
-        vx3_sim_id id;
-        if (vx3_load_vxa(job->ctx, base_xml->c_str(), vxd.c_str(), base_name(f).c_str(), &id) != VX3_OK) {
-            fprintf(stderr, "%s: %s\n", f.c_str(), vx3_last_error(job->ctx));
-            continue;
-        }
-        job->ids.push_back(id);
+        texts.push_back(std::move(vxd));
+        names.push_back(base_name(f));
+    }
+    std::vector<const char*> tp, np;
+    for (size_t i = 0; i < texts.size(); i++) { tp.push_back(texts[i].c_str()); np.push_back(names[i].c_str()); }
+    std::vector<vx3_sim_id> ids(texts.size());
+    std::vector<int> st(texts.size());
+    vx3_load_vxa_many(job->ctx, base_xml->c_str(), tp.data(), np.data(), (int)texts.size(), ids.data(), st.data());
+    for (size_t i = 0; i < ids.size(); i++) {
+        if (st[i] != VX3_OK) fprintf(stderr, "%s: rejected (error %d)\n", names[i].c_str(), st[i]);
+        else job->ids.push_back(ids[i]);
     }
     if (!job->ids.empty()) {
         job->rc = vx3_run(job->ctx, job->ids.data(), (int)job->ids.size(), VX3_BATCHED, 0);

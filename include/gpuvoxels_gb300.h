@@ -87,6 +87,13 @@ const char* vx3_last_error(vx3_ctx* ctx);
  * merges the VXD into the base VXA (Utils/ctool.h:49-57), reads it, builds the
  * voxel/link topology.  Host only; device memory is taken when the simulation first runs. */
 int vx3_load_vxa(vx3_ctx* ctx, const char* base_vxa_xml, const char* vxd_xml_or_null, const char* name, vx3_sim_id* out);
+/* A whole generation at once (the loop of VX3_SimulationManager::readVXD over its files,
+ * VX3_SimulationManager.cu:285-380): n VXDs merged into the base (vxds NULL or an entry NULL =
+ * the base alone; base NULL = every entry is a whole VXA), parsed and built on host threads.
+ * ids[i] = -1 and status[i] (optional) = the error code where file i is rejected; the others
+ * load.  Returns VX3_OK, or the first error code with its message in vx3_last_error. */
+int vx3_load_vxa_many(vx3_ctx* ctx, const char* base_vxa_xml_or_null, const char* const* vxds, const char* const* names, int n,
+                      vx3_sim_id* ids, int* status_or_null);
 
 /* Replaces CVX_Voxel::external() fixes/forces (Voxelyze3/src/old/VX_External.h:58-79):
  * dof_fixed bits 0-2 fix x/y/z translation, 3-5 fix x/y/z rotation.  Before the first step only. */

@@ -17,6 +17,28 @@ def _bits(a):
     return np.ascontiguousarray(a).view(np.uint64)
 
 
+def test_load_many_matches_one_by_one(ctx):
+    """vx3_load_vxa_many (host threads) loads exactly what vx3_load_vxa loads, in both its
+    forms (whole VXAs; base + VXDs), and rejects a malformed VXD without dropping the rest."""
+    cs = synth.config1_batch(5, seed=21)
+    a = [ctx.load_vxa(c.vxa, name=f"a{i}") for i, c in enumerate(cs)]
+    b = ctx.load_many([c.vxa for c in cs], names=[f"b{i}" for i in range(len(cs))])
+    base = cs[0].vxa
+    vxd = ("<VXD><Structure replace=\"VXA.VXC.Structure\" Compression=\"ASCII_READABLE\"><X_Voxels>2</X_Voxels>"
+           "<Y_Voxels>1</Y_Voxels><Z_Voxels>1</Z_Voxels><Data><Layer><![CDATA[12]]></Layer></Data></Structure></VXD>")
+    c = ctx.load_many([vxd, vxd], base=base)
+    with pytest.raises(g.VX3Error):
+        ctx.load_many([vxd, "<VXD><Structure"], base=base)
+    try:
+        assert [ctx.info(i).num_voxel for i in c] == [2, 2]
+        ctx.step(a + b, 100, g.BATCHED)
+        for x, y in zip(a, b):
+            assert np.array_equal(_bits(ctx.voxel_state(x)["pos"]), _bits(ctx.voxel_state(y)["pos"]))
+    finally:
+        for s in a + b + c:
+            ctx.free(s)
+
+
 def test_plain_and_batched_are_bit_identical(ctx):
     cs = synth.config1_batch(4, seed=9)
     a = [ctx.load_vxa(c.vxa, name=f"p{i}") for i, c in enumerate(cs)]
