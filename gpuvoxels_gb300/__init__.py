@@ -35,7 +35,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
-           "vx3_write_report_multi", "vx3_load_vxa_many"]
+           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -92,6 +92,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_center_of_mass_noalloc": (I, [P, P, P, P, I64, P, P]),
         "vx3_write_report_multi": (I, [P, P, P, I, S, S]),
         "vx3_load_vxa_many": (I, [P, S, P, P, I, P, P]),
+        "vx3_record_history": (I, [P, I64, S]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -195,6 +196,10 @@ class Context:
         for i, nm in zip(out, names):
             self.names[i] = nm
         return out
+
+    def record_history(self, sim: int, path: Optional[str]):
+        """Writes the simulation's .history stream to `path` during later step/run calls (None stops)."""
+        self._check(self.L.vx3_record_history(self.h, sim, _b(path)))
 
     def set_external(self, sim: int, voxel: int, dof_fixed: int = 0, force=(0, 0, 0), moment=(0, 0, 0),
                      translate=(0, 0, 0), rotate=(0, 0, 0)):

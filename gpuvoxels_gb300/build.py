@@ -22,7 +22,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgpuvoxels_gb300.so")
 WORKER = os.path.join(OUT_DIR, "vx3_node_worker")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels_exact.cu", "kernels_fast.cu", "engine.cu", "noalloc.cu", "world.cpp", "xml_dom.cpp", "capi.cpp"]
+SOURCES = ["kernels_exact.cu", "kernels_fast.cu", "engine.cu", "noalloc.cu", "world.cpp", "xml_dom.cpp", "capi.cpp", "history.cpp"]
 
 
 def nvcc() -> str:

@@ -12,12 +12,22 @@
 #include <vector>
 
 #include "engine.h"
+#include "history.h"
 #include "world.h"
+
+// A simulation whose steps are written to a .history file.
+struct HistoryState {
+    FILE* f = nullptr;
+    bool header = false;
+    int interval = 1;
+    int64_t last_j = -1;
+};
 
 struct vx3_ctx {
     gvx::Engine* eng = nullptr;
     std::string err;
     std::map<int64_t, std::string> names;
+    std::map<int64_t, HistoryState> hist;
 };
 
 namespace {
@@ -64,6 +74,8 @@ vx3_ctx* vx3_create(int device, size_t budget) {
 
 void vx3_destroy(vx3_ctx* c) {
     if (!c) return;
+    for (auto& kv : c->hist)
+        if (kv.second.f) fclose(kv.second.f);
     gvx::engine_destroy(c->eng);
     delete c;
 }
@@ -148,8 +160,91 @@ int vx3_set_external(vx3_ctx* c, vx3_sim_id id, int voxel, int dof, const float 
     return e ? fail(c, e, err) : VX3_OK;
 }
 
+}  // extern "C"
+
+namespace {
+bool any_history(vx3_ctx* c, const vx3_sim_id* ids, int n) {
+    for (int i = 0; i < n; i++)
+        if (c->hist.count(ids[i])) return true;
+    return false;
+}
+
+// Writes the header (once the first step has fixed the time step) and a record for every
+// recording simulation that has just completed a recorded loop step.
+int history_after_chunk(vx3_ctx* c, const vx3_sim_id* ids, int n) {
+    for (int i = 0; i < n; i++) {
+        auto it = c->hist.find(ids[i]);
+        if (it == c->hist.end()) continue;
+        HistoryState& h = it->second;
+        int nv, nl, status;
+        double dt, t;
+        int64_t steps;
+        if (c->eng->info(ids[i], &nv, &nl, &dt, &t, &steps, &status)) continue;
+        const gvx::SimWorld* w = c->eng->world(ids[i]);
+        if (!w || steps == 0) continue;
+        if (!h.header) {
+            const double opt = c->eng->optimal_dt(ids[i]);
+            h.interval = gvx::history_step_interval(*w, opt);
+            const std::string hd = gvx::history_header(*w, opt);
+            fwrite(hd.data(), 1, hd.size(), h.f);
+            h.header = true;
+        }
+        const int64_t j = steps - 1;                 // the reference's loop index of the last step
+        if (j % h.interval != 0 || j == h.last_j) continue;
+        std::vector<double> d13(13 * (size_t)nv);
+        std::vector<float> f4(4 * (size_t)nv), lsf(3 * (size_t)std::max(nl, 1));
+        std::vector<int32_t> vf((size_t)nv), lf((size_t)std::max(nl, 1));
+        std::string err;
+        if (int e = c->eng->voxel_state(ids[i], d13.data(), f4.data(), vf.data(), &err)) return fail(c, e, err);
+        std::vector<double> ld(9 * (size_t)std::max(nl, 1));
+        if (nl > 0)
+            if (int e = c->eng->link_state(ids[i], ld.data(), lsf.data(), lf.data(), &err)) return fail(c, e, err);
+        const std::string rec = gvx::history_record(*w, j, t, d13.data(), f4.data(), lsf.data());
+        fwrite(rec.data(), 1, rec.size(), h.f);
+        fflush(h.f);
+        h.last_j = j;
+    }
+    return VX3_OK;
+}
+
+// Steps in chunks that end on every recorded step of every recording simulation.
+// steps < 0: until every listed simulation has stopped (or max_steps).
+int drive_with_history(vx3_ctx* c, const vx3_sim_id* ids, int n, int mode, int64_t steps, int64_t max_steps) {
+    int64_t done = 0;
+    const int64_t limit = steps >= 0 ? steps : (max_steps > 0 ? max_steps : INT64_MAX);
+    while (done < limit) {
+        int64_t chunk = std::min<int64_t>(limit - done, 4096);
+        bool running = false;
+        for (int i = 0; i < n; i++) {
+            int nv, nl, status;
+            double dt, t;
+            int64_t s;
+            if (c->eng->info(ids[i], &nv, &nl, &dt, &t, &s, &status)) continue;
+            if (status == gvx::SIM_IDLE || status == gvx::SIM_RUNNING) running = true;
+            else continue;
+            auto it = c->hist.find(ids[i]);
+            if (it == c->hist.end()) continue;
+            const HistoryState& h = it->second;
+            if (!h.header) { chunk = 1; continue; }
+            // next loop index j > s - 1 with j % interval == 0, completed after step j + 1
+            const int64_t jn = ((s - 1) / h.interval + 1) * h.interval;
+            chunk = std::min(chunk, std::max<int64_t>(1, jn + 1 - s));
+        }
+        if (!running) break;
+        std::string err;
+        if (int e = c->eng->step(ids, n, mode, chunk, &err)) return fail(c, e, err);
+        done += chunk;
+        if (int e = history_after_chunk(c, ids, n)) return e;
+    }
+    return VX3_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int vx3_run(vx3_ctx* c, const vx3_sim_id* ids, int n, int mode, int64_t max_steps) {
     if (!c || (!ids && n > 0) || n < 0) return fail(c, VX3_E_ARG, "bad arguments");
+    if (any_history(c, ids, n)) return drive_with_history(c, ids, n, mode, -1, max_steps);
     std::string err;
     int e = c->eng->run(ids, n, mode, max_steps, &err);
     return e ? fail(c, e, err) : VX3_OK;
@@ -157,9 +252,29 @@ int vx3_run(vx3_ctx* c, const vx3_sim_id* ids, int n, int mode, int64_t max_step
 
 int vx3_step(vx3_ctx* c, const vx3_sim_id* ids, int n, int mode, int64_t steps) {
     if (!c || (!ids && n > 0) || n < 0 || steps < 0) return fail(c, VX3_E_ARG, "bad arguments");
+    if (any_history(c, ids, n)) return drive_with_history(c, ids, n, mode, steps, 0);
     std::string err;
     int e = c->eng->step(ids, n, mode, steps, &err);
     return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_record_history(vx3_ctx* c, vx3_sim_id id, const char* path) {
+    if (!c) return VX3_E_ARG;
+    auto it = c->hist.find(id);
+    if (it != c->hist.end()) {
+        if (it->second.f) fclose(it->second.f);
+        c->hist.erase(it);
+    }
+    if (!path) return VX3_OK;
+    const gvx::SimWorld* w = c->eng->world(id);
+    if (!w) return fail(c, VX3_E_ARG, "unknown simulation id");
+    if (w->desc.record_step_size <= 0) return fail(c, VX3_E_ARG, "the VXA sets no Simulator/RecordHistory/RecordStepSize");
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(c, VX3_E_ARG, std::string("cannot open ") + path);
+    HistoryState h;
+    h.f = f;
+    c->hist[id] = h;
+    return VX3_OK;
 }
 
 int vx3_submit(vx3_ctx* c, vx3_sim_id id, int64_t horizon) {
@@ -344,6 +459,11 @@ int vx3_write_report_multi(vx3_ctx* const* ctxs, const vx3_sim_id* const* ids, c
 int vx3_free_sim(vx3_ctx* c, vx3_sim_id id) {
     if (!c) return VX3_E_ARG;
     c->names.erase(id);
+    auto h = c->hist.find(id);
+    if (h != c->hist.end()) {
+        if (h->second.f) fclose(h->second.f);
+        c->hist.erase(h);
+    }
     return c->eng->free_sim(id) ? fail(c, VX3_E_ARG, "unknown simulation id") : VX3_OK;
 }
 

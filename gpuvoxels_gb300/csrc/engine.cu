@@ -1000,6 +1000,16 @@ public:
         return 0;
     }
 
+    const SimWorld* world(int64_t id) override {
+        SimRec* r = find(id);
+        return r ? &r->w : nullptr;
+    }
+
+    double optimal_dt(int64_t id) override {
+        SimRec* r = find(id);
+        return r ? (double)r->optdt : 0.0;
+    }
+
     int saved_positions(int64_t id, int* save, std::vector<double>* init, std::vector<double>* cur, std::vector<int>* matid,
                         std::string* err) override {
         SimRec* r = find(id);

@@ -78,6 +78,10 @@ public:
     virtual int saved_positions(int64_t id, int* save, std::vector<double>* init, std::vector<double>* cur,
                                 std::vector<int>* matid, std::string* err) = 0;
     virtual int free_sim(int64_t id) = 0;
+    // Host-side description of a loaded simulation (topology, materials, VXA settings); null if unknown.
+    virtual const SimWorld* world(int64_t id) = 0;
+    // recommendedTimeStep of the simulation (0 until its first step).
+    virtual double optimal_dt(int64_t id) = 0;
     virtual const Timing& timing() const = 0;
     virtual void set_profiling(int on) = 0;
     virtual size_t bytes_in_use() const = 0;

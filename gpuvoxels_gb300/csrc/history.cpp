@@ -1,0 +1,114 @@
+// .history stream writer (see history.h).  Number formats are the reference's printf
+// formats; values are formed in the reference's types (float corner offsets, double
+// positions).
+#include "history.h"
+
+#include <cmath>
+#include <cstdio>
+
+namespace gvx {
+
+namespace {
+
+void appendf(std::string* s, const char* fmt, double a) {
+    char b[64];
+    snprintf(b, sizeof(b), fmt, a);
+    *s += b;
+}
+
+// (int)(colour * 255) clamped to 0..255 (CVXC_Material::GetRedi, VXA/VX_Object.h:419;
+// CVX_Material::setRed, old/VX_Material.cpp:253-258)
+int color_byte(float c) {
+    int v = (int)(c * 255);
+    return v > 255 ? 255 : (v < 0 ? 0 : v);
+}
+
+// VX3_Link::axialStrain(positiveEnd), VX3/VX3_Link.cu:72-74
+float axial_strain(const SimWorld& w, int l, float strain, bool positive_end) {
+    const float ratio = w.vmats[w.desc.voxels[4 * w.link_pos[l] + 3]].E / w.vmats[w.desc.voxels[4 * w.link_neg[l] + 3]].E;
+    return positive_end ? 2.0f * strain * ratio / (1.0f + ratio) : 2.0f * strain / (1.0f + ratio);
+}
+
+}  // namespace
+
+int history_step_interval(const SimWorld& w, double optimal_dt) {
+    return (int)(w.desc.record_step_size / (10000 * optimal_dt * w.desc.dt_frac)) + 1;
+}
+
+std::string history_header(const SimWorld& w, double optimal_dt) {
+    std::string s = "\n{{{setting}}}<rescale>0.001</rescale>\n";
+    for (size_t i = 0; i < w.desc.mats.size(); i++) {
+        const float* c = w.desc.mats[i].rgba;
+        char b[256];
+        snprintf(b, sizeof(b), "{{{setting}}}<matcolor><id>%d</id><r>%.2f</r><g>%.2f</g><b>%.2f</b><a>%.2f</a></matcolor>\n",
+                 (int)i + 1, color_byte(c[0]) / 255., color_byte(c[1]) / 255., color_byte(c[2]) / 255., color_byte(c[3]) / 255.);
+        s += b;
+    }
+    appendf(&s, "\n{{{setting}}}<voxel_size>%f</voxel_size>\n", w.desc.vox_size);
+    char b[256];
+    snprintf(b, sizeof(b), "real_stepsize: %d ; recommendedTimeStep %f; d_v3->DtFrac %f . \n", history_step_interval(w, optimal_dt),
+             optimal_dt, w.desc.dt_frac);
+    s += b;
+    return s;
+}
+
+std::string history_record(const SimWorld& w, int64_t j, double t, const double* d13, const float* f4, const float* lsf3) {
+    const double vs = 1 / 0.001;
+    std::string s;
+    char b[512];
+    const int nl = w.nl;
+    if (w.desc.record_voxel) {
+        snprintf(b, sizeof(b), "<<<Step%lld Time:%f>>>", (long long)j, t);
+        s += b;
+        for (int v = 0; v < w.nv; v++) {
+            if (w.vox_interior[v]) continue;                       // surface voxels only, in voxel order
+            const double* p = d13 + 13 * (size_t)v;
+            const double qw = p[6], qx = p[7], qy = p[8], qz = p[9];
+            snprintf(b, sizeof(b), "%.1f,%.1f,%.1f,", p[0] * vs, p[1] * vs, p[2] * vs);
+            s += b;
+            const double angle = 2.0 * acos(qw > 1 ? 1 : qw) * 57.29577951308232;   // Quat3D::AngleDegrees
+            snprintf(b, sizeof(b), "%.1f,%.2f,%.2f,%.2f,", angle, qx, qy, qz);
+            s += b;
+            // VX3_Voxel::cornerOffset(NNN) and (PPP), VX3/VX3_Voxel.cu:147-159
+            const int mi = w.desc.voxels[4 * v + 3];
+            const VoxelMaterial& m = w.vmats[mi];
+            const double half_size = 0.5 * (m.nom * (1 + f4[4 * (size_t)v] * m.cte));
+            float nnn[3], ppp[3];
+            for (int i = 0; i < 3; i++) {
+                for (int corner = 0; corner < 2; corner++) {
+                    const bool pos_link = corner == 1;
+                    const int l = w.vox_links[6 * (size_t)v + 2 * i + (pos_link ? 0 : 1)];
+                    double st = pos_link ? 1.0 : -1.0;
+                    if (l >= 0) {
+                        const LinkMaterial& lm = w.lmats[w.link_mat[l]];
+                        const bool failed = lm.epsFail != -1.0f && lsf3[3 * (size_t)l + 1] > lm.epsFail;
+                        if (!failed) st = (1 + axial_strain(w, l, lsf3[3 * (size_t)l], pos_link)) * (pos_link ? 1 : -1);
+                    }
+                    (pos_link ? ppp : nnn)[i] = (float)(half_size * st);
+                }
+            }
+            snprintf(b, sizeof(b), "%.1f,%.1f,%.1f,%.1f,%.1f,%.1f,", nnn[0] * vs, nnn[1] * vs, nnn[2] * vs, ppp[0] * vs, ppp[1] * vs,
+                     ppp[2] * vs);
+            s += b;
+            snprintf(b, sizeof(b), "%d,", mi + 1);
+            s += b;
+            s += "0.0,;";                                          // localSignal (signals are not simulated)
+        }
+        s += "<<<>>>";
+    }
+    if (w.desc.record_link) {
+        snprintf(b, sizeof(b), "|[[[%lld]]]", (long long)j);
+        s += b;
+        for (int l = 0; l < nl; l++) {
+            const double* a = d13 + 13 * (size_t)w.link_pos[l];
+            const double* c = d13 + 13 * (size_t)w.link_neg[l];
+            snprintf(b, sizeof(b), "%.4f,%.4f,%.4f,%.4f,%.4f,%.4f,;", a[0], a[1], a[2], c[0], c[1], c[2]);
+            s += b;
+        }
+        s += "[[[]]]";
+    }
+    s += "\n";
+    return s;
+}
+
+}  // namespace gvx

@@ -1,0 +1,24 @@
+// The .history text stream of VX3_SimulationManager's simulation loop
+// (Voxelyze3/src/VX3/VX3_SimulationManager.cu:40-114): a settings header, then one
+// line per recorded step with every surface voxel's pose and deformed corners
+// (RecordVoxel) and every link's end positions (RecordLink).
+#pragma once
+#include <cstdint>
+#include <string>
+
+#include "world.h"
+
+namespace gvx {
+
+// Steps between records: int(RecordStepSize / (10000 * recommendedTimeStep * DtFrac)) + 1 (:56).
+int history_step_interval(const SimWorld& w, double optimal_dt);
+
+// Header: rescale, material colours, voxel size (:40-50) and the step-interval line (:56-58).
+std::string history_header(const SimWorld& w, double optimal_dt);
+
+// One record after loop step `j` (0-based; the reference records when j % interval == 0), at
+// simulation time `t`.  d13 = pos3 linMom3 orient4 angMom3 per voxel, f4 = temperature and
+// Poisson strains per voxel, lsf3 = strain, maxStrain, strainOffset per link.
+std::string history_record(const SimWorld& w, int64_t j, double t, const double* d13, const float* f4, const float* lsf3);
+
+}  // namespace gvx

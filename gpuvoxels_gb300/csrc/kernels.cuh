@@ -57,16 +57,17 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         lvv = false;
     }
     d3 a1v;
+    bool wide1 = false, wide2 = false;      // branches taken, kept as the next step's ordering key
     if (small) {
         pos2.x -= restLen;
         a1v = D3(0, 0, 0);                  // ToRotationVector of the identity
     } else {
-        angle1 = q_from_angle_to_posx(angle1, pos2);
+        angle1 = q_from_angle_to_posx(angle1, pos2, &wide1);
         angle2 = qmul(angle1, angle2);
         pos2 = D3(sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z) - restLen, 0, 0);
-        a1v = q_to_rotvec(angle1);
+        a1v = q_to_rotvec(angle1, &wide1);
     }
-    const d3 a2v = q_to_rotvec(angle2);
+    const d3 a2v = q_to_rotvec(angle2, &wide2);
     st[l] = pos2.x; st[nl + l] = pos2.y; st[2 * nl + l] = pos2.z;
     st[3 * nl + l] = a1v.x; st[4 * nl + l] = a1v.y; st[5 * nl + l] = a1v.z;
     st[6 * nl + l] = a2v.x; st[7 * nl + l] = a2v.y; st[8 * nl + l] = a2v.z;
@@ -144,7 +145,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         fN = to_axis_orig(axis, fN); fP = to_axis_orig(axis, fP);
         mN = to_axis_orig(axis, mN); mP = to_axis_orig(axis, mP);
     }
-    S.lfl[l] = (uint8_t)((small ? LF_SMALL : 0) | (lvv ? LF_LVV : 0));
+    S.lfl[l] = (uint8_t)((small ? LF_SMALL : 0) | (lvv ? LF_LVV : 0) | (wide1 ? LF_WIDE1 : 0) | (wide2 ? LF_WIDE2 : 0));
 
     // direction slots: the negative-end voxel sees this link in direction 2*axis,
     // the positive-end voxel in direction 2*axis+1 (CVX_Voxel::force, VX_Voxel.cpp:236-238)
@@ -162,53 +163,78 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     S.ss[dp * nv + pv] = 2.0f * strain * ratio / (1.0f + ratio);
 }
 
-// Links of one work item in an order that keeps warps on one path: the large-angle
-// links of the previous step first, then the small-angle ones (stable within each
-// group).  The two paths differ by ~40% of the FP64 work and GB300's FP64 pipe
-// spends the same cycles on a warp instruction whatever its active lanes, so
-// mixed warps would pay for both.  The flag is last step's; links that switch
-// mode this step are rare (hysteresis).  Order of evaluation does not change
-// results: every link writes only its own state and its two direction slots.
-constexpr int kLinkOrderMax = 1024;   // links per item that are reordered (larger items run in index order)
+// Work-item elements in an order that keeps warps on one code path.  GB300's FP64
+// pipe spends the same cycles on a warp instruction whatever its active lanes, so a
+// warp whose lanes take different branches pays for every branch.  Elements are
+// grouped by a small key describing the branches they took in the previous step
+// (paths change rarely from one step to the next); the partition is stable and
+// deterministic.  The order never changes results: every link writes only its own
+// state and its two direction slots, and voxel work is per voxel.
+constexpr int kOrderMax = 1024;   // elements per item that are reordered (larger items run in index order)
+constexpr int kOrderKeys = 8;
 
-__device__ __forceinline__ int order_links(const Sim& S, const Item& w, int* perm, int* warp_sums) {
-    const int n = w.end - w.begin;
-    if (n > kLinkOrderMax) return 0;
+// perm[0..n) = element indices grouped by key(j) in increasing key order; wc holds
+// kOrderKeys x 8 warp counts.  Every thread of the block must call it.
+template <typename KeyFn>
+__device__ __forceinline__ void order_by_key(int n, KeyFn key, int* perm, int* wc) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int base_large = 0, base_small = 0;
-    int n_large = 0;
-    // count the large-angle links first, so that the small ones can start after them
+    const unsigned below = (1u << lane) - 1u;
+    int start[kOrderKeys];
+    for (int k = 0; k < kOrderKeys; k++) start[k] = 0;
+    // pass 1: group sizes
     for (int j0 = 0; j0 < n; j0 += blockDim.x) {
         const int j = j0 + threadIdx.x;
-        const bool large = j < n && !(S.lfl[w.begin + j] & LF_SMALL);
-        const unsigned bl = __ballot_sync(0xffffffffu, large);
-        if (lane == 0) warp_sums[wid] = __popc(bl);
+        const int kj = j < n ? key(j) : -1;
+#pragma unroll
+        for (int k = 0; k < kOrderKeys; k++) {
+            const unsigned b = __ballot_sync(0xffffffffu, kj == k);
+            if (lane == 0) wc[k * 8 + wid] = __popc(b);
+        }
         __syncthreads();
-        for (int k = 0; k < nw; k++) n_large += warp_sums[k];
+        for (int k = 0; k < kOrderKeys; k++)
+            for (int q = 0; q < nw; q++) start[k] += wc[k * 8 + q];
         __syncthreads();
     }
+    // group starts
+    int acc = 0;
+    for (int k = 0; k < kOrderKeys; k++) { const int c = start[k]; start[k] = acc; acc += c; }
+    // pass 2: place
     for (int j0 = 0; j0 < n; j0 += blockDim.x) {
         const int j = j0 + threadIdx.x;
-        const bool in = j < n;
-        const bool large = in && !(S.lfl[w.begin + j] & LF_SMALL);
-        const unsigned bl = __ballot_sync(0xffffffffu, large), bs = __ballot_sync(0xffffffffu, in && !large);
-        if (lane == 0) { warp_sums[wid] = __popc(bl); warp_sums[32 + wid] = __popc(bs); }
+        const int kj = j < n ? key(j) : -1;
+        unsigned mine = 0;
+#pragma unroll
+        for (int k = 0; k < kOrderKeys; k++) {
+            const unsigned b = __ballot_sync(0xffffffffu, kj == k);
+            if (kj == k) mine = b;
+            if (lane == 0) wc[k * 8 + wid] = __popc(b);
+        }
         __syncthreads();
-        int pl = base_large, ps = base_small;
-        for (int k = 0; k < wid; k++) { pl += warp_sums[k]; ps += warp_sums[32 + k]; }
-        const unsigned below = (1u << lane) - 1u;
-        if (large) perm[pl + __popc(bl & below)] = j;
-        else if (in) perm[n_large + ps + __popc(bs & below)] = j;
-        for (int k = 0; k < nw; k++) { base_large += warp_sums[k]; base_small += warp_sums[32 + k]; }
+        if (kj >= 0) {
+            int p = start[kj] + __popc(mine & below);
+            for (int q = 0; q < wid; q++) p += wc[kj * 8 + q];
+            perm[p] = j;
+        }
+        for (int k = 0; k < kOrderKeys; k++)
+            for (int q = 0; q < nw; q++) start[k] += wc[k * 8 + q];
         __syncthreads();
     }
-    return 1;
 }
+
+// Link key: small-angle mode, then within each mode which rotation branches were taken.
+struct LinkKey {
+    const uint8_t* lfl;
+    int begin;
+    __device__ int operator()(int j) const {
+        const uint8_t f = lfl[begin + j];
+        return ((f & LF_SMALL) ? 4 : 0) | ((f & LF_WIDE1) ? 2 : 0) | ((f & LF_WIDE2) ? 1 : 0);
+    }
+};
 
 __global__ void __launch_bounds__(256) k_links(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
     __shared__ int s_item;
-    __shared__ int s_perm[kLinkOrderMax];
-    __shared__ int s_warp[64];
+    __shared__ int s_perm[kOrderMax];
+    __shared__ int s_warp[kOrderKeys * 8];
     if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; }
     for (;;) {
         const int it = claim(&tickets[0], &s_item);
@@ -219,8 +245,9 @@ __global__ void __launch_bounds__(256) k_links(const Sim* __restrict__ sims, Ctl
         const Sim& S = sims[w.sim];
         const float dt = c.dt;
         bool div = false;
-        if (order_links(S, w, s_perm, s_warp)) {
-            const int n = w.end - w.begin;
+        const int n = w.end - w.begin;
+        if (n <= kOrderMax) {
+            order_by_key(n, LinkKey{S.lfl, w.begin}, s_perm, s_warp);
             for (int k = threadIdx.x; k < n; k += blockDim.x) link_update(S, w.begin + s_perm[k], dt, &div);
         } else {
             for (int l = w.begin + threadIdx.x; l < w.end; l += blockDim.x) link_update(S, l, dt, &div);
@@ -412,6 +439,7 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
         // reference's second evaluation (VX_Voxel.cpp:188) yields this same value
         const float pen = floor ? d2f(half(base_size_avg(m, temp)) - m.halfNom - pos.z) : -1.0f;
         if (floor) {
+            fl = (pen >= 0) ? (fl | VF_FLOORC) : (fl & ~VF_FLOORC);
             if (pen >= 0) {
                 const float normal = m.penStiff * pen;
                 F.z += f2d(normal) - m.cDampTD * vz;
@@ -576,11 +604,24 @@ __device__ __noinline__ void sim_control(Ctl& c, bool div, double t_next, int64_
     if (stop) c.status = 2;
 }
 
+// Voxel key: touched the floor last step (contact and friction branches), then
+// surface voxels (Poisson strain by pow) apart from interior ones.
+struct VoxelKey {
+    const uint32_t* vfl;
+    int begin;
+    __device__ int operator()(int j) const {
+        const uint32_t f = vfl[begin + j];
+        return ((f & VF_FLOORC) ? 2 : 0) | ((f & VF_INTERIOR) ? 1 : 0);
+    }
+};
+
 __global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items,
                                                 int* tickets, double* partials) {
     __shared__ int s_item, s_last;
     __shared__ double red[256];
     __shared__ double s_cycles;
+    __shared__ int s_perm[kOrderMax];
+    __shared__ int s_warp[kOrderKeys * 8];
     if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
     for (;;) {
         const int it = claim(&tickets[2], &s_item);
@@ -601,8 +642,16 @@ __global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims,
         const int flags = S.flags;
         int* hnext = (flags & SF_COLLIDE) ? S.hash_head + (size_t)(c.hash_parity ^ 1) * S.hash_size : nullptr;
         double acc[4] = {0, 0, 0, 0};
-        if (!div && dt != 0.0f)
-            for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, t_cycles, flags, com_step ? acc : nullptr, hnext);
+        if (!div && dt != 0.0f) {
+            const int n = w.end - w.begin;
+            if (n <= kOrderMax) {
+                order_by_key(n, VoxelKey{S.vfl, w.begin}, s_perm, s_warp);
+                for (int k = threadIdx.x; k < n; k += blockDim.x)
+                    voxel_update(S, w.begin + s_perm[k], dt, t_cycles, flags, com_step ? acc : nullptr, hnext);
+            } else {
+                for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, t_cycles, flags, com_step ? acc : nullptr, hnext);
+            }
+        }
         if (com_step) {
             for (int k = 0; k < 4; k++) {
                 const double r = block_sum(acc[k], red);

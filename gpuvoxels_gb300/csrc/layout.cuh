@@ -22,6 +22,9 @@ constexpr uint32_t VF_MEASURED = 1u << 9;
 // link flag bits
 constexpr uint8_t LF_SMALL = 1;           // small-angle mode
 constexpr uint8_t LF_LVV = 2;             // LOCAL_VELOCITY_VALID
+constexpr uint8_t LF_WIDE1 = 4;           // last step: angle1 took the general (acos/sincos) branches
+constexpr uint8_t LF_WIDE2 = 8;           // last step: angle2's rotation vector took the acos branch
+constexpr uint32_t VF_FLOORC = 1u << 10;  // last step: the voxel touched the floor
 
 // sim flag bits
 constexpr int SF_FLOOR = 1, SF_COLLIDE = 2, SF_VARY = 4, SF_EXPAND = 8;

@@ -97,14 +97,15 @@ __device__ __forceinline__ d3 qrotinv(const q4& q, const d3& f) {
               tw * q.y - tx * q.z + ty * q.w + tz * q.x,
               tw * q.z + tx * q.y - ty * q.x + tz * q.w);
 }
-// Quat3D::ToRotationVector  Quat3D.h:121-126
-__device__ __forceinline__ d3 q_to_rotvec(const q4& q) {
+// Quat3D::ToRotationVector  Quat3D.h:121-126; *wide = the acos branch was taken
+__device__ __forceinline__ d3 q_to_rotvec(const q4& q, bool* wide = nullptr) {
     if (fp64i::ge(fabs(q.w), 1.0)) return D3(0, 0, 0);   // q.w >= 1 || q.w <= -1
     double sl = 1.0 - q.w * q.w;
     if (fp64i::lt(sl, 2.4e-3)) {
         double s = sqrt((2 - mul2(q.w)) / sl);
         return D3(mul2(q.x) * s, mul2(q.y) * s, mul2(q.z) * s);
     }
+    if (wide) *wide = true;
     double a = acos(q.w);
     double inv = 1.0 / sqrt(sl);
     return D3((mul2(q.x) * a) * inv, (mul2(q.y) * a) * inv, (mul2(q.z) * a) * inv);
@@ -126,14 +127,16 @@ __device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
     }
     return Q4(w, tx * s, ty * s, tz * s);
 }
-// Quat3D::FromAngleToPosX  Quat3D.h:145-170; `cur` is returned for a zero vector
-__device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r) {
+// Quat3D::FromAngleToPosX  Quat3D.h:145-170; `cur` is returned for a zero vector;
+// *wide = the general (acos, sincos) branch was taken
+__device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r, bool* wide = nullptr) {
     if (fp64i::eq0(r.x) && fp64i::eq0(r.y) && fp64i::eq0(r.z)) return cur;
     double yox = r.y / r.x, zox = r.z / r.x;
     if (fp64i::lt(fabs(yox), 1.732e-2) && fp64i::lt(fabs(zox), 1.732e-2)) {   // |yox|, |zox| < 1.732e-2
         double y = half(zox), z = -half(yox);
         return Q4(1 + half(-y * y - z * z), 0, y, z);
     }
+    if (wide) *wide = true;
     double l = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
     double nx = r.x, ny = r.y, nz = r.z;
     if (fp64i::gt0(l)) { double li = 1.0 / l; nx *= li; ny *= li; nz *= li; }

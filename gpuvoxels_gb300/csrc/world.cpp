@@ -229,6 +229,13 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
             int mt = get_i(m, "MatType", 0);
             if (mt != 0) { *err = "only basic (SINGLE) materials are supported"; return false; }
             pm.name = m->child("Name") ? m->child("Name")->text : "Default";
+            // Display colour, 0..1 floats, defaults as CVXC_Material::ReadXML (VXA/VX_Object.cpp:1385-1390)
+            if (const XmlNode* disp = m->child("Display")) {
+                pm.rgba[0] = (float)get_d(disp, "Red", 0.5);
+                pm.rgba[1] = (float)get_d(disp, "Green", 0.5);
+                pm.rgba[2] = (float)get_d(disp, "Blue", 0.5);
+                pm.rgba[3] = (float)get_d(disp, "Alpha", 1.0);
+            }
             const XmlNode* mech = m->child("Mechanical");
             pm.model = get_i(mech, "MatModel", 0);
             pm.E = get_d(mech, "Elastic_Mod", 0);
@@ -315,6 +322,8 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     d->save_all_positions = (int)ptree_num(*root, "VXA.Simulator.SavePositionOfAllVoxels", 0);
     d->max_dist_pairs = ptree_num(*root, "VXA.Simulator.MaxDistInVoxelLengthsToCountAsPair", 0);
     d->record_step_size = (int)ptree_num(*root, "VXA.Simulator.RecordHistory.RecordStepSize", 0);
+    d->record_voxel = (int)ptree_num(*root, "VXA.Simulator.RecordHistory.RecordVoxel", 1);
+    d->record_link = (int)ptree_num(*root, "VXA.Simulator.RecordHistory.RecordLink", 0);
     parse_mathtree(root->path("VXA.Simulator.StopCondition.StopConditionFormula"), &d->stop_formula);
     parse_mathtree(root->path("VXA.Simulator.FitnessFunction"), &d->fitness);
     return true;

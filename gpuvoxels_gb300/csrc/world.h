@@ -21,6 +21,7 @@ struct PaletteMaterial {
     double rho = 0, nu = 0, cte = 0, mu_static = 0, mu_kinetic = 0;
     int is_measured = 1;
     std::string name;
+    float rgba[4] = {0.5f, 0.5f, 0.5f, 1.0f};   // Display colour (history recorder)
 };
 
 struct External {
@@ -52,7 +53,8 @@ struct SimDesc {
     MathTree stop_formula, fitness;
     int save_all_positions = 0;
     double max_dist_pairs = 0;     // MaxDistInVoxelLengthsToCountAsPair
-    int record_step_size = 0;
+    int record_step_size = 0;      // VXA.Simulator.RecordHistory.* (VX3_SimulationManager.cu:344-346)
+    int record_voxel = 1, record_link = 0;
 };
 
 // Parses a base VXA plus an optional VXD (whose children carrying replace="VXA.a.b"

@@ -126,6 +126,14 @@ int vx3_get_voxel_state(vx3_ctx* ctx, vx3_sim_id id, double* d13, float* f4, int
 /* Link state (CVX_Link, VX_Link.h:68-99): d9 = pos2 angle1v angle2v, f3 = strain maxStrain strainOffset, flags. */
 int vx3_get_link_state(vx3_ctx* ctx, vx3_sim_id id, double* d9, float* f3, int32_t* flags);
 
+/* Replaces the .history stream the reference prints from its simulation loop when the VXA
+ * sets Simulator/RecordHistory/RecordStepSize (VX3/VX3_SimulationManager.cu:40-114): settings
+ * header, then every int(RecordStepSize/(10000*recommendedTimeStep*DtFrac))+1 loop steps a
+ * line with the surface voxels (RecordVoxel, default 1) and links (RecordLink).  Writes to
+ * `path` during the following vx3_run / vx3_step calls (which then advance in chunks that end
+ * on recorded steps); NULL stops recording.  VX3_E_ARG if the VXA has no RecordStepSize. */
+int vx3_record_history(vx3_ctx* ctx, vx3_sim_id id, const char* path_or_null);
+
 /* Replaces the worker's report (Executables/vx3_node_worker.cu:98-141): report.inputdir,
  * report.bestfit.{filename,fitness_score}, report.detail.<name>.{...}; results sorted by
  * fitness with NaN last (VX3_SimulationResult.h:26-33).  A simulation whose VXA sets
