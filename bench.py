@@ -242,7 +242,11 @@ def run_ours(args):
     ctx.step(ids, 1, g.BATCHED)                       # upload + first step
     if args.autotune:
         ctx.autotune(ids)
-    ctx.set_tuning(graph_steps=args.graph_steps)
+    if args.tuning:
+        bl, bv, il, iv = (int(x) for x in args.tuning.split(","))
+        ctx.set_tuning(bl, bv, il, iv, args.graph_steps)
+    else:
+        ctx.set_tuning(graph_steps=args.graph_steps)
     ctx.step(ids, args.warmup, g.BATCHED)
     if dist:
         dist.barrier()
@@ -463,6 +467,7 @@ def main():
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--graph-steps", type=int, default=64)
+    ap.add_argument("--tuning", default="", help="block_links,block_voxels,items_links,items_voxels (0 = keep)")
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--plain-sims", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

@@ -35,7 +35,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
-           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history"]
+           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -93,6 +93,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_write_report_multi": (I, [P, P, P, I, S, S]),
         "vx3_load_vxa_many": (I, [P, S, P, P, I, P, P]),
         "vx3_record_history": (I, [P, I64, S]),
+        "vx3_inspect_externals": (I, [S, S, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -130,6 +131,17 @@ def inspect_vxa(base_xml: str, vxd_xml: Optional[str] = None) -> dict:
                             externals=int(counts[5])),
                 env=dict(zip(keys, env.tolist())), voxels=vox, links=lnk[:nl], phase=ph, voxmat=vm, nom=vnom,
                 linkmat_idx=lidx[:nlm], linkmat=lm[:nlm])
+
+
+def inspect_externals(base_xml: str, vxd_xml: Optional[str] = None) -> dict:
+    """Host-only: per-voxel externals from the VXA's boundary-condition regions."""
+    L = library()
+    nv = inspect_vxa(base_xml, vxd_xml)["counts"]["voxels"]
+    dof = np.zeros(nv, np.int32); fm = np.zeros((nv, 6), np.float32); tr = np.zeros((nv, 6))
+    rc = L.vx3_inspect_externals(_b(base_xml), _b(vxd_xml), _p(dof), _p(fm), _p(tr))
+    if rc:
+        raise VX3Error(ERRORS.get(rc, str(rc)))
+    return dict(dof=dof, force=fm[:, :3], moment=fm[:, 3:], translate=tr[:, :3], rotate=tr[:, 3:])
 
 
 def eval_formula(base_xml: str, which: str, vars9: Sequence[float], vxd_xml: Optional[str] = None) -> float:

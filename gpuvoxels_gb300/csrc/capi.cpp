@@ -199,7 +199,7 @@ int history_after_chunk(vx3_ctx* c, const vx3_sim_id* ids, int n) {
         std::vector<double> ld(9 * (size_t)std::max(nl, 1));
         if (nl > 0)
             if (int e = c->eng->link_state(ids[i], ld.data(), lsf.data(), lf.data(), &err)) return fail(c, e, err);
-        const std::string rec = gvx::history_record(*w, j, t, d13.data(), f4.data(), lsf.data());
+        const std::string rec = gvx::history_record(*w, j, t, (float)dt, d13.data(), f4.data(), lsf.data());
         fwrite(rec.data(), 1, rec.size(), h.f);
         fflush(h.f);
         h.last_j = j;
@@ -563,6 +563,28 @@ int vx3_inspect_topology(const char* base, const char* vxd, int32_t* vox4, int32
         float v[20] = {m.E, m.nu, m.eHat, m.a1, m.a2, m.b1, m.b2, m.b3, m.sqA1, m.sqA2xIp, m.sqB1, m.sqB2xFMp, m.sqB3xIp,
                        m.sigmaYield, m.sigmaFail, m.epsYield, m.epsFail, m.linear ? 1.0f : 0.0f, (float)m.nom, m.rho};
         if (lmat20) memcpy(lmat20 + 20 * k, v, sizeof(v));
+    }
+    return VX3_OK;
+}
+
+int vx3_inspect_externals(const char* base, const char* vxd, int32_t* dof, float* fm6, double* tr6) {
+    gvx::SimWorld w;
+    std::string err;
+    if (int e = inspect_world(base, vxd, &w, &err)) return e;
+    for (int i = 0; i < w.nv; i++) {
+        if (dof) dof[i] = 0;
+        for (int k = 0; k < 6; k++) {
+            if (fm6) fm6[6 * i + k] = 0.0f;
+            if (tr6) tr6[6 * i + k] = 0.0;
+        }
+    }
+    for (const gvx::External& x : w.desc.externals) {
+        const int i = x.voxel;
+        if (dof) dof[i] = x.dof_fixed;
+        for (int k = 0; k < 3; k++) {
+            if (fm6) { fm6[6 * i + k] = x.force[k]; fm6[6 * i + 3 + k] = x.moment[k]; }
+            if (tr6) { tr6[6 * i + k] = x.translate[k]; tr6[6 * i + 3 + k] = x.rotate[k]; }
+        }
     }
     return VX3_OK;
 }

@@ -1061,7 +1061,7 @@ public:
         return 0;
     }
     int set_tuning(int bl, int bv, int il, int iv, int gs) override {
-        if (bl > 0) block_links_ = std::min(256, bl);
+        if (bl > 0) block_links_ = std::min(256, std::max(32, bl & ~31));   // whole warps (the link ordering uses ballots)
         if (bv > 0) block_voxels_ = std::min(256, std::max(32, bv & ~31));
         if (il > 0) items_links_ = il;
         if (iv > 0) items_voxels_ = iv;

@@ -52,7 +52,19 @@ std::string history_header(const SimWorld& w, double optimal_dt) {
     return s;
 }
 
-std::string history_record(const SimWorld& w, int64_t j, double t, const double* d13, const float* f4, const float* lsf3) {
+// Temperature voxel v had during the step that ended at time t: the reference sets it from the
+// time at the start of the step (VX3_VoxelyzeKernel.cu:625-650).  The engine already holds the
+// next step's value, so varying temperatures are formed again from t - dt.
+float step_temperature(const SimWorld& w, int v, double t, float dt, const float* f4) {
+    const SimDesc& d = w.desc;
+    if (!(d.vary_temp && d.temp_period > 0)) return f4[4 * (size_t)v];
+    const float two_pi = 2 * 3.1415926f;
+    double T = d.temp_amplitude * sin((double)two_pi * ((t - dt) / d.temp_period + d.phase[v]));
+    if (!d.enable_expansion && T > 0) T = 0;
+    return (float)T;
+}
+
+std::string history_record(const SimWorld& w, int64_t j, double t, float dt, const double* d13, const float* f4, const float* lsf3) {
     const double vs = 1 / 0.001;
     std::string s;
     char b[512];
@@ -72,7 +84,7 @@ std::string history_record(const SimWorld& w, int64_t j, double t, const double*
             // VX3_Voxel::cornerOffset(NNN) and (PPP), VX3/VX3_Voxel.cu:147-159
             const int mi = w.desc.voxels[4 * v + 3];
             const VoxelMaterial& m = w.vmats[mi];
-            const double half_size = 0.5 * (m.nom * (1 + f4[4 * (size_t)v] * m.cte));
+            const double half_size = 0.5 * (m.nom * (1 + step_temperature(w, v, t, dt, f4) * m.cte));
             float nnn[3], ppp[3];
             for (int i = 0; i < 3; i++) {
                 for (int corner = 0; corner < 2; corner++) {

@@ -17,8 +17,9 @@ int history_step_interval(const SimWorld& w, double optimal_dt);
 std::string history_header(const SimWorld& w, double optimal_dt);
 
 // One record after loop step `j` (0-based; the reference records when j % interval == 0), at
-// simulation time `t`.  d13 = pos3 linMom3 orient4 angMom3 per voxel, f4 = temperature and
-// Poisson strains per voxel, lsf3 = strain, maxStrain, strainOffset per link.
-std::string history_record(const SimWorld& w, int64_t j, double t, const double* d13, const float* f4, const float* lsf3);
+// simulation time `t` (after the step; `dt` is the step).  d13 = pos3 linMom3 orient4 angMom3 per
+// voxel, f4 = temperature and Poisson strains per voxel as the engine holds them after the step
+// (the next step's temperature), lsf3 = strain, maxStrain, strainOffset per link.
+std::string history_record(const SimWorld& w, int64_t j, double t, float dt, const double* d13, const float* f4, const float* lsf3);
 
 }  // namespace gvx

@@ -133,6 +133,152 @@ void parse_mathtree(const XmlNode* node, MathTree* m) {
     m->n = k + 1;
 }
 
+// ------------------------------------------------------------ boundary conditions
+// A region of the environment (CVX_FRegion, Voxelyze3/src/old/VX_FRegion.h:40-120) in
+// workspace-relative units, with what it does to the voxels it touches.
+struct BCRegion {
+    int prim = 0;                                  // PRIM_BOX 0, PRIM_CYLINDER 1, PRIM_SPHERE 2 (VX_FRegion.h:25-28)
+    double X = 0, Y = 0, Z = 0, dX = 0, dY = 0, dZ = 0, radius = 0;
+    int dof = 0;                                   // DOF_X 0x01 .. DOF_TZ 0x20
+    double force[3] = {0, 0, 0}, torque[3] = {0, 0, 0}, disp[3] = {0, 0, 0}, ang[3] = {0, 0, 0};
+};
+
+// CVX_FRegion::ReadXML (VX_FRegion.cpp:165-216)
+bool read_region(const XmlNode* fr, BCRegion* r, std::string* err) {
+    int prim;
+    if (!load_i(fr, "PrimType", &prim)) { *err = "boundary condition region without PrimType"; return false; }
+    if (prim == 3) { *err = "mesh boundary-condition regions are not supported"; return false; }
+    if (prim < 0 || prim > 3) { *err = "unknown boundary-condition PrimType"; return false; }
+    r->prim = prim;
+    r->X = get_d(fr, "X", 0); r->Y = get_d(fr, "Y", 0); r->Z = get_d(fr, "Z", 0);
+    r->dX = get_d(fr, "dX", 0); r->dY = get_d(fr, "dY", 0); r->dZ = get_d(fr, "dZ", 0);
+    r->radius = get_d(fr, "Radius", 0);
+    int dof;
+    if (load_i(fr, "DofFixed", &dof)) r->dof = (int)(char)dof;
+    else r->dof = get_b(fr, "Fixed", false) ? 0x3F : 0;   // older files: a binary Fixed tag
+    const char* f[3] = {"ForceX", "ForceY", "ForceZ"}, *t[3] = {"TorqueX", "TorqueY", "TorqueZ"};
+    const char* dd[3] = {"DisplaceX", "DisplaceY", "DisplaceZ"}, *a[3] = {"AngDisplaceX", "AngDisplaceY", "AngDisplaceZ"};
+    for (int k = 0; k < 3; k++) {
+        r->force[k] = get_d(fr, f[k], 0); r->torque[k] = get_d(fr, t[k], 0);
+        r->disp[k] = get_d(fr, dd[k], 0); r->ang[k] = get_d(fr, a[k], 0);
+    }
+    return true;
+}
+
+// CPrimitive::IsTouching(P, Dist vector, Envelope) for box, cylinder and sphere
+// (VX_FRegion.cpp:420-429, 495-534, 591-604); P and Dist in meters, Env = workspace size.
+bool region_touching(const BCRegion& r, const double P[3], const double D[3], const double E[3]) {
+    if (r.prim == 0) {
+        const double ps[3] = {P[0] / E[0], P[1] / E[1], P[2] / E[2]}, ds[3] = {D[0] / E[0], D[1] / E[1], D[2] / E[2]};
+        return ps[0] + ds[0] > r.X && ps[0] - ds[0] < r.X + r.dX && ps[1] + ds[1] > r.Y && ps[1] - ds[1] < r.Y + r.dY &&
+               ps[2] + ds[2] > r.Z && ps[2] - ds[2] < r.Z + r.dZ;
+    }
+    const double pos[3] = {r.X * E[0], r.Y * E[1], r.Z * E[2]};
+    const double size[3] = {r.dX * E[0], r.dY * E[1], r.dZ * E[2]};
+    const double emax = std::max(E[0], std::max(E[1], E[2]));
+    const double rad = r.radius * emax;
+    if (r.prim == 1) {   // cylinder: IsIn only, along the first nonzero axis
+        if (r.dX != 0)
+            return P[0] > pos[0] && P[0] < pos[0] + size[0] && sqrt((P[1] - pos[1]) * (P[1] - pos[1]) + (P[2] - pos[2]) * (P[2] - pos[2])) < rad;
+        if (r.dY != 0)
+            return P[1] > pos[1] && P[1] < pos[1] + size[1] && sqrt((P[0] - pos[0]) * (P[0] - pos[0]) + (P[2] - pos[2]) * (P[2] - pos[2])) < rad;
+        if (r.dZ != 0)
+            return P[2] > pos[2] && P[2] < pos[2] + size[2] && sqrt((P[0] - pos[0]) * (P[0] - pos[0]) + (P[1] - pos[1]) * (P[1] - pos[1])) < rad;
+        return false;
+    }
+    // sphere: against |Dist| around the point
+    const double dist = sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
+    return sqrt((P[0] - pos[0]) * (P[0] - pos[0]) + (P[1] - pos[1]) * (P[1] - pos[1]) + (P[2] - pos[2]) * (P[2] - pos[2])) < rad + dist;
+}
+
+// Boundary conditions of <Environment>: regions that fix, displace, force or torque the voxels
+// they touch (CVX_Environment::ReadXML, VX_Environment.cpp:101-146), applied as CVX_Sim::Import
+// does (VXA/VX_Sim.cpp:109-144): a region's force and torque are split over the number of
+// structure cells it touches (CVX_Environment::GetNumTouching, VX_Environment.cpp:215-232, which
+// tests the cell centres with CVX_Object::GetXYZ's 1e-6 lattice-unit offset), and each touched
+// voxel's external force becomes f + (float)(f + F/n) as Import writes it.
+bool apply_boundary_conditions(const XmlNode* root, const XmlNode* vxc, int NX, int NY, int NZ, const std::vector<uint8_t>& cells,
+                               SimDesc* d, std::string* err) {
+    std::vector<BCRegion> regions;
+    const XmlNode* env = root->child("Environment");
+    auto read_list = [&](const XmlNode* parent, const char* count_tag) {
+        int n = get_i(parent, count_tag, 0);
+        std::vector<const XmlNode*> frs = parent->children_named("FRegion");
+        if (n > (int)frs.size()) { *err = std::string("fewer FRegion elements than ") + count_tag; return false; }
+        for (int i = 0; i < n; i++) {
+            BCRegion r;
+            if (!read_region(frs[i], &r, err)) return false;
+            regions.push_back(r);
+        }
+        return true;
+    };
+    if (env) {
+        if (const XmlNode* bc = env->child("Boundary_Conditions")) {
+            if (!read_list(bc, "NumBCs")) return false;
+        } else {
+            if (const XmlNode* fx = env->child("Fixed_Regions"))
+                if (!read_list(fx, "NumFixed")) return false;
+            if (const XmlNode* fo = env->child("Forced_Regions"))
+                if (!read_list(fo, "NumForced")) return false;
+        }
+    }
+    if (regions.empty()) return true;
+    const XmlNode* lat = vxc->child("Lattice");
+    const double ld = get_d(lat, "Lattice_Dim", 0.001);
+    const double adj[3] = {get_d(lat, "X_Dim_Adj", 1.0), get_d(lat, "Y_Dim_Adj", 1.0), get_d(lat, "Z_Dim_Adj", 1.0)};
+    if (get_d(lat, "X_Line_Offset", 0) != 0 || get_d(lat, "Y_Line_Offset", 0) != 0 || get_d(lat, "X_Layer_Offset", 0) != 0 ||
+        get_d(lat, "Y_Layer_Offset", 0) != 0) {
+        *err = "boundary conditions on offset lattices are not supported";
+        return false;
+    }
+    const double latenv[3] = {ld * adj[0], ld * adj[1], ld * adj[2]};                    // GetLatDimEnv
+    const double ws[3] = {ld * adj[0] * NX, ld * adj[1] * NY, ld * adj[2] * NZ};         // GetWorkSpace
+    const double half[3] = {latenv[0] / 2.0, latenv[1] / 2.0, latenv[2] / 2.0};
+    // cells touched per region (GetXYZ with its offset hack: Eps = 1e-6 lattice units in x and y)
+    const double eps = 0.000001;
+    std::vector<int> touching(regions.size(), 0);
+    for (long i = 0; i < (long)NX * NY * NZ; i++) {
+        if (cells[i] == 0) continue;
+        const int ix = (int)(i % NX), iy = (int)((i / NX) % NY), iz = (int)(i / ((long)NX * NY));
+        const double offx = eps - (int)(eps / adj[0]) * adj[0], offy = eps - (int)(eps / adj[1]) * adj[1];
+        const double p[3] = {ld * (adj[0] * (0.5 + ix) + offx), ld * (adj[1] * (0.5 + iy) + offy), ld * adj[2] * (0.5 + iz)};
+        for (size_t j = 0; j < regions.size(); j++)
+            if (region_touching(regions[j], p, half, ws)) touching[j]++;
+    }
+    // apply to the voxels in list order
+    const int nv = (int)d->voxels.size() / 4;
+    std::vector<int> ext_of(nv, -1);
+    for (size_t k = 0; k < d->externals.size(); k++) ext_of[d->externals[k].voxel] = (int)k;
+    const double s = d->vox_size;                                                        // CVX_Voxel::originalPosition
+    for (int v = 0; v < nv; v++) {
+        const double p[3] = {d->voxels[4 * v] * s + latenv[0] / 2, d->voxels[4 * v + 1] * s + latenv[1] / 2,
+                             d->voxels[4 * v + 2] * s + latenv[2] / 2};
+        for (size_t j = 0; j < regions.size(); j++) {
+            const BCRegion& r = regions[j];
+            if (!region_touching(r, p, half, ws)) continue;
+            if (ext_of[v] < 0) {
+                External e;
+                e.voxel = v;
+                ext_of[v] = (int)d->externals.size();
+                d->externals.push_back(e);
+            }
+            External& e = d->externals[ext_of[v]];
+            // CVX_External::setDisplacement: fixes the DOF, sets the value when nonzero (VX_External.cpp:53-66)
+            const double vals[6] = {r.disp[0], r.disp[1], r.disp[2], r.ang[0], r.ang[1], r.ang[2]};
+            for (int k = 0; k < 6; k++) {
+                if (!(r.dof & (1 << k))) continue;
+                e.dof_fixed |= 1 << k;
+                if (vals[k] != 0.0f) (k < 3 ? e.translate[k] : e.rotate[k - 3]) = vals[k];
+            }
+            for (int k = 0; k < 3; k++) {
+                e.force[k] += (float)(e.force[k] + r.force[k] / touching[j]);
+                e.moment[k] += (float)(e.moment[k] + r.torque[k] / touching[j]);
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace
 
 void merge_vxd(XmlNode* base, const XmlNode& vxd) {
@@ -314,6 +460,7 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
         d->phase.push_back(have_phase ? phase_by_voxel[n] : 0.0);
         n++;
     }
+    if (!apply_boundary_conditions(root.get(), vxc, X, Y, Z, cells, d, err)) return false;
     /* VX3 keys, Voxelyze3/src/VX3/VX3_SimulationManager.cu:326-367 */
     d->collisions = ptree_bool(*root, "VXA.Simulator.AttachDetach.EnableCollision", true);
     d->bounding_radius = (float)ptree_num(*root, "VXA.Simulator.AttachDetach.boundingRadius", 0.75);

@@ -202,6 +202,11 @@ int vx3_inspect_vxa(const char* base_vxa_xml, const char* vxd_xml_or_null, int32
  *   2sqrt(mEs), 2sqrt(IEs^3), gravity); lidx2[2*nlm] constituent voxel materials;
  *   lmat20[20*nlm] = E, nu, eHat, a1, a2, b1, b2, b3, sqA1, sqA2xIp, sqB1, sqB2xFMp, sqB3xIp,
  *   sigmaYield, sigmaFail, epsYield, epsFail, linear, nomSize, rho. */
+/* Host-only: the externals the VXA's boundary-condition regions put on each voxel, as
+ * CVX_Sim::Import applies them (VXA/VX_Sim.cpp:109-144): dof[nv] fixed-DOF bits (1,2,4 translate
+ * x,y,z; 8,16,32 rotate), fm6[6*nv] force xyz + moment xyz, tr6[6*nv] prescribed translation xyz +
+ * rotation xyz; zeros for voxels no region touches. */
+int vx3_inspect_externals(const char* base_vxa_xml, const char* vxd_xml_or_null, int32_t* dof, float* fm6, double* tr6);
 int vx3_inspect_topology(const char* base_vxa_xml, const char* vxd_xml_or_null, int32_t* vox4, int32_t* lnk4, double* phase,
                          float* vmat18, double* vnom, int32_t* lidx2, float* lmat20);
 /* Stop/fitness formula evaluation as the engine performs it (Utils/VX3_MathTree.h:50-192);

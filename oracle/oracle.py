@@ -309,8 +309,116 @@ def desc_from_vxa(xml_text):
                vary_temp=int(vary), temp_amplitude=temp_amp, temp_period=temp_period,
                enable_expansion=int(_ptree_num(root, "VXA.Simulator.EnableExpansion", 0)), initial_temp=init,
                zeta_internal=bond, zeta_global=slow, zeta_collision=colz)
-    return dict(env=env, mats=mats, voxels=np.array(voxels, np.int32).reshape(-1, 4),
-                phase=np.array(phase, np.float64), externals=[])
+    voxels = np.array(voxels, np.int32).reshape(-1, 4)
+    externals = _boundary_conditions(env_el, lat, X, Y, Z, cells, voxels, vox_size)
+    return dict(env=env, mats=mats, voxels=voxels, phase=np.array(phase, np.float64), externals=externals)
+
+
+def _read_region(fr):
+    """CVX_FRegion::ReadXML (Voxelyze3/src/old/VX_FRegion.cpp:165-216)."""
+    prim = _load_int(fr, "PrimType", -1)
+    if prim not in (0, 1, 2):
+        raise ValueError("unsupported boundary-condition PrimType %d" % prim)
+    r = dict(prim=prim, X=_load_double(fr, "X", 0.0), Y=_load_double(fr, "Y", 0.0), Z=_load_double(fr, "Z", 0.0),
+             dX=_load_double(fr, "dX", 0.0), dY=_load_double(fr, "dY", 0.0), dZ=_load_double(fr, "dZ", 0.0),
+             radius=_load_double(fr, "Radius", 0.0))
+    if _text(fr, "DofFixed") is not None:
+        r["dof"] = _load_int(fr, "DofFixed", 0) & 0xFF
+        if r["dof"] >= 0x80:
+            r["dof"] -= 0x100                      # (char) cast
+    else:
+        r["dof"] = 0x3F if _load_bool(fr, "Fixed", False) else 0
+    r["force"] = [_load_double(fr, t, 0.0) for t in ("ForceX", "ForceY", "ForceZ")]
+    r["torque"] = [_load_double(fr, t, 0.0) for t in ("TorqueX", "TorqueY", "TorqueZ")]
+    r["disp"] = [_load_double(fr, t, 0.0) for t in ("DisplaceX", "DisplaceY", "DisplaceZ")]
+    r["ang"] = [_load_double(fr, t, 0.0) for t in ("AngDisplaceX", "AngDisplaceY", "AngDisplaceZ")]
+    return r
+
+
+def _touching(r, P, D, E):
+    """CPrimitive::IsTouching(P, Dist, Envelope) for box, cylinder, sphere (VX_FRegion.cpp:420-429, 495-534, 591-604)."""
+    if r["prim"] == 0:
+        ps = [P[k] / E[k] for k in range(3)]
+        ds = [D[k] / E[k] for k in range(3)]
+        lo, dd = (r["X"], r["Y"], r["Z"]), (r["dX"], r["dY"], r["dZ"])
+        return all(ps[k] + ds[k] > lo[k] and ps[k] - ds[k] < lo[k] + dd[k] for k in range(3))
+    pos = [r["X"] * E[0], r["Y"] * E[1], r["Z"] * E[2]]
+    size = [r["dX"] * E[0], r["dY"] * E[1], r["dZ"] * E[2]]
+    rad = r["radius"] * max(E)
+    if r["prim"] == 1:
+        for a, (b, c) in ((0, (1, 2)), (1, (0, 2)), (2, (0, 1))):
+            if (r["dX"], r["dY"], r["dZ"])[a] != 0:
+                return (P[a] > pos[a] and P[a] < pos[a] + size[a] and
+                        math.sqrt((P[b] - pos[b]) * (P[b] - pos[b]) + (P[c] - pos[c]) * (P[c] - pos[c])) < rad)
+        return False
+    dist = math.sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2])
+    return math.sqrt((P[0] - pos[0]) * (P[0] - pos[0]) + (P[1] - pos[1]) * (P[1] - pos[1]) +
+                     (P[2] - pos[2]) * (P[2] - pos[2])) < rad + dist
+
+
+def _boundary_conditions(env_el, lat, NX, NY, NZ, cells, voxels, vox_size):
+    """Externals from <Environment> boundary-condition regions as CVX_Sim::Import applies them
+    (VXA/VX_Sim.cpp:109-144; regions read by CVX_Environment::ReadXML, VX_Environment.cpp:101-146;
+    counts by CVX_Environment::GetNumTouching, VX_Environment.cpp:215-232 on CVX_Object::GetXYZ
+    cell points, VXA/VX_Object.cpp:525-558)."""
+    regions = []
+    if env_el is not None:
+        lists = []
+        bc = _child(env_el, "Boundary_Conditions")
+        if bc is not None:
+            lists.append((bc, "NumBCs"))
+        else:
+            for tag, cnt in (("Fixed_Regions", "NumFixed"), ("Forced_Regions", "NumForced")):
+                el = _child(env_el, tag)
+                if el is not None:
+                    lists.append((el, cnt))
+        for el, cnt in lists:
+            n = _load_int(el, cnt, 0)
+            frs = [c for c in el if c.tag == "FRegion"]
+            if n > len(frs):
+                raise ValueError("fewer FRegion elements than " + cnt)
+            regions += [_read_region(fr) for fr in frs[:n]]
+    if not regions:
+        return []
+    ld = _load_double(lat, "Lattice_Dim", 0.001)
+    adj = [_load_double(lat, t, 1.0) for t in ("X_Dim_Adj", "Y_Dim_Adj", "Z_Dim_Adj")]
+    latenv = [ld * a for a in adj]
+    ws = [ld * adj[0] * NX, ld * adj[1] * NY, ld * adj[2] * NZ]
+    half = [x / 2.0 for x in latenv]
+    eps = 0.000001
+    offx = eps - int(eps / adj[0]) * adj[0]
+    offy = eps - int(eps / adj[1]) * adj[1]
+    touching = [0] * len(regions)
+    for i in range(NX * NY * NZ):
+        if cells[i] == 0:
+            continue
+        ix, iy, iz = i % NX, (i // NX) % NY, i // (NX * NY)
+        p = [ld * (adj[0] * (0.5 + ix) + offx), ld * (adj[1] * (0.5 + iy) + offy), ld * adj[2] * (0.5 + iz)]
+        for j, r in enumerate(regions):
+            if _touching(r, p, half, ws):
+                touching[j] += 1
+    ext = {}
+    for v, (ix, iy, iz, _) in enumerate(voxels):
+        p = [ix * vox_size + latenv[0] / 2, iy * vox_size + latenv[1] / 2, iz * vox_size + latenv[2] / 2]
+        for j, r in enumerate(regions):
+            if not _touching(r, p, half, ws):
+                continue
+            e = ext.setdefault(v, dict(voxel=v, dof_fixed=0, force=np.zeros(3, np.float32), moment=np.zeros(3, np.float32),
+                                       translate=[0.0, 0.0, 0.0], rotate=[0.0, 0.0, 0.0]))
+            vals = r["disp"] + r["ang"]
+            for k in range(6):
+                if r["dof"] & (1 << k):
+                    e["dof_fixed"] |= 1 << k
+                    if vals[k] != 0.0:
+                        (e["translate"] if k < 3 else e["rotate"])[k % 3] = vals[k]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                for k in range(3):
+                    f_add = np.float32(float(e["force"][k]) + np.float64(r["force"][k]) / np.float64(touching[j]))
+                    m_add = np.float32(float(e["moment"][k]) + np.float64(r["torque"][k]) / np.float64(touching[j]))
+                    e["force"][k] = np.float32(e["force"][k] + f_add)
+                    e["moment"][k] = np.float32(e["moment"][k] + m_add)
+    return [dict(x, force=tuple(float(f) for f in x["force"]), moment=tuple(float(m) for m in x["moment"]))
+            for _, x in sorted(ext.items())]
 
 
 # ----------------------------------------------------------------------------
@@ -486,6 +594,12 @@ class RefSim:
         v = np.zeros((self.nvox, 4), np.int32); l = np.zeros((self.nlink, 4), np.int32); ph = np.zeros(self.nvox)
         RefSim._lib.vxref_topology(self.h, _p(v), _p(l), _p(ph))
         return dict(voxels=v, links=l, phase=ph)
+
+    def externals(self):
+        """Per voxel: fixed-DOF bits and force3, moment3, translation3, rotation3 (zeros without an external)."""
+        dof = np.zeros(self.nvox, np.int32); vals = np.zeros((self.nvox, 12))
+        RefSim._lib.vxref_externals(self.h, _p(dof), _p(vals))
+        return dict(dof=dof, vals=vals)
 
     def materials(self):
         f = np.zeros((self.nvmat, 18), np.float32); nom = np.zeros(self.nvmat)

@@ -10,7 +10,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-GOLDEN_WORLDS = ["c0_seed0", "c1_poisson", "falling_blocks", "bilinear_cantilever", "large_angle", "partial_fix",
+GOLDEN_WORLDS = ["c0_seed0", "c1_poisson", "falling_blocks", "bilinear_cantilever", "large_angle", "partial_fix", "bc_regions",
                  "ref_zoo_basic", "ref_example", "ref_signaling", "ref_memleaking", "ref_circle_push", "ref_target_only"]
 
 

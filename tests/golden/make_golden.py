@@ -73,6 +73,15 @@ def worlds():
     w["partial_fix"] = dict(vxa=vxa, ext=[dict(voxel=0, dof_fixed=0x07), dict(voxel=8, dof_fixed=0x07, translate=(0.0, 0.0, 0.001)),
                                           dict(voxel=2, dof_fixed=0x18), dict(voxel=4, moment=(0.01, 0.0, 0.0), force=(0.0, 0.5, 0.0))],
                             snaps=[1, 200, 400])
+    # boundary-condition regions in the VXA: a fixed box, a forced/torqued sphere, a displaced cylinder
+    bc = ("<Boundary_Conditions><NumBCs>3</NumBCs>"
+          "<FRegion><PrimType>0</PrimType><X>0</X><Y>0</Y><Z>0</Z><dX>0.3</dX><dY>1</dY><dZ>1</dZ><DofFixed>63</DofFixed></FRegion>"
+          "<FRegion><PrimType>2</PrimType><X>0.8</X><Y>0.5</Y><Z>0.5</Z><Radius>0.25</Radius><DofFixed>0</DofFixed>"
+          "<ForceX>0.3</ForceX><ForceZ>-0.7</ForceZ><TorqueY>0.001</TorqueY></FRegion>"
+          "<FRegion><PrimType>1</PrimType><X>0.5</X><Y>0.5</Y><Z>0</Z><dZ>1</dZ><Radius>0.2</Radius><DofFixed>5</DofFixed>"
+          "<DisplaceZ>0.002</DisplaceZ><ForceY>0.1</ForceY></FRegion></Boundary_Conditions>")
+    vxa = synth.config0_creature(0).vxa.replace("<Boundary_Conditions><NumBCs>0</NumBCs></Boundary_Conditions>", bc)
+    w["bc_regions"] = dict(vxa=vxa, ext=[], snaps=[1, 300, 1000])
     return w
 
 
@@ -121,8 +130,10 @@ def run(name, spec):
                        e.get("translate", (0, 0, 0)), e.get("rotate", (0, 0, 0)))
     topo = r.topology()
     mats = r.materials()
+    exts = r.externals()
     out = dict(vxa=np.array(spec["vxa"]), ext=np.array(repr(spec["ext"])), snaps=np.array(spec["snaps"], np.int64),
                voxels=topo["voxels"], links=topo["links"], phase=topo["phase"],
+               ext_dof=exts["dof"], ext_vals=exts["vals"],
                voxmat_bits=mats["voxmat"].view(np.uint32), nom=mats["nom"],
                linkmat_idx=mats["linkmat_idx"], linkmat_bits=mats["linkmat"].view(np.uint32))
     done = 0

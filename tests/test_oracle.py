@@ -12,7 +12,7 @@ from gpuvoxels_gb300 import synth
 
 def _oracle_for(vxa, ext):
     d = desc_from_vxa(vxa)
-    d["externals"] = ext
+    d["externals"] = d["externals"] + list(ext)    # boundary-condition regions of the VXA, then the API externals
     return OracleSim(d)
 
 

@@ -43,6 +43,22 @@ def test_reader_matches_reference(name):
     assert np.array_equal(p["voxmat"].view(np.uint32), z["voxmat_bits"])
     assert np.array_equal(p["linkmat"].view(np.uint32), z["linkmat_bits"])
     assert np.array_equal(p["linkmat_idx"], z["linkmat_idx"])
+    # externals from the VXA's boundary-condition regions (none where the fixture sets them by API)
+    if not load_golden(name)[2]:
+        x = g.inspect_externals(vxa)
+        assert np.array_equal(x["dof"], z["ext_dof"])
+        fm = np.concatenate([x["force"], x["moment"]], 1)
+        assert np.array_equal(fm.view(np.uint32), z["ext_vals"][:, :6].astype(np.float32).view(np.uint32))
+        assert np.array_equal(np.concatenate([x["translate"], x["rotate"]], 1), z["ext_vals"][:, 6:])
+
+
+def test_bc_regions_cover_every_primitive():
+    z, vxa, _ = load_golden("bc_regions")
+    dof = z["ext_dof"]
+    assert (dof == 0x3F).sum() > 0 and (dof == 0x05).sum() > 0            # fixed box, displaced cylinder
+    assert (np.abs(z["ext_vals"][:, 0]) > 0).sum() > 0                      # forced sphere
+    assert (z["ext_vals"][:, 8] == 0.002).sum() > 0                        # prescribed z translation
+    assert ((z["ext_vals"][:, 8] == 0.002) <= ((dof & 0x04) != 0)).all()    # only where z is fixed
 
 
 def test_reader_counts_and_environment():
