@@ -209,7 +209,7 @@ public:
 
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
-        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos;
+        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos, cilia, ffield;
         int hash_size;
     };
     static void compute_layout(const SimWorld& w, Layout* L, Offs* o) {
@@ -253,6 +253,8 @@ public:
             t.hnext = L->add(4 * nv);
             t.cpos = L->add(16 * nv);
         }
+        if (w.desc.enable_cilia) t.cilia = L->add(8 * 3 * nv);
+        if (w.desc.has_force_field) t.ffield = L->add(sizeof(MathTree) * 3);
         if (o) *o = t;
     }
 
@@ -377,6 +379,10 @@ public:
             x.gravForceD = x.gravForce;
             x.halfNom = m.nom / 2;
             x.halfMassInv = 0.5 * (double)x.massInv;
+            const PaletteMaterial& pm = w.desc.mats[i];
+            x.cilia = pm.cilia;
+            x.ciliaOn = pm.cilia_on_after;
+            x.thermalOn = pm.thermal_on_after;
         }
         dev::LMat* lm = (dev::LMat*)P(o.lm);
         for (size_t i = 0; i < w.lmats.size(); i++) {
@@ -438,6 +444,16 @@ public:
         if (w.desc.collisions) flags |= dev::SF_COLLIDE;
         if (w.desc.vary_temp && w.desc.temp_period > 0) flags |= dev::SF_VARY;
         if (w.desc.enable_expansion) flags |= dev::SF_EXPAND;
+        if (w.desc.enable_cilia) {
+            flags |= dev::SF_CILIA;
+            double* c = (double*)P(o.cilia);   // 3 blocks of nv; zeros where the VXA gives none
+            for (size_t i = 0; i < nv && 3 * i + 2 < w.desc.base_cilia.size(); i++)
+                for (int k = 0; k < 3; k++) c[k * nv + i] = w.desc.base_cilia[3 * i + k];
+        }
+        if (w.desc.has_force_field) {
+            flags |= dev::SF_FFIELD;
+            memcpy(P(o.ffield), w.desc.force_field, sizeof(MathTree) * 3);
+        }
         double max_bsa = 0;
         if (w.desc.collisions) {
             int32_t* surf = (int32_t*)P(o.surf);
@@ -477,6 +493,8 @@ public:
             S.cpos = (float4*)D(o.cpos);
             S.inv_cell = (float)(1.0 / S.cell_size);
         }
+        if (w.desc.enable_cilia) S.cilia = (const double*)D(o.cilia);
+        if (w.desc.has_force_field) S.ffield = (const MathTree*)D(o.ffield);
         CK(cudaMemcpyAsync(base, h.data(), L.total, cudaMemcpyHostToDevice, stream_));
         CK(cudaMemcpyAsync(d_sims_ + slot, &S, sizeof(S), cudaMemcpyHostToDevice, stream_));
         dev::Ctl c{};

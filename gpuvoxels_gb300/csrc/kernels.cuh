@@ -398,8 +398,16 @@ __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, 
 // (Voxelyze3/src/old/VX_Voxel.cpp:163-297), then the Poisson strain the next
 // step's links will read (CVX_Voxel::strain(true), :299-333) and the next
 // step's actuation temperature (VX3_VoxelyzeKernel.cu:625-650).
-// t_cycles = t_next / TempPeriod, the same quotient for every voxel of the simulation.
-__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, double t_cycles, int flags, double* com4, int* hash_next_table) {
+// Per-step values shared by every voxel of a simulation.
+struct StepTimes {
+    double t_now;      // currentTime during this step
+    double t_next;     // after it
+    double t_cycles;   // t_next / TempPeriod
+    double angle;      // recentAngle (force-field variable)
+};
+
+__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, const StepTimes& st, int flags, double* com4, int* hash_next_table) {
+    const double t_cycles = st.t_cycles;
     const int nv = S.nv;
     const VMat& m = S.vm[__ldg(S.vmat + v)];
     uint32_t fl = S.vfl[v];
@@ -431,6 +439,24 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
             const int nc = S.ccount[v];
             const float* cf = S.cforce + (size_t)v * 3 * kContactCap;
             for (int k = 0; k < nc; k++) { F.x -= cf[3 * k]; F.y -= cf[3 * k + 1]; F.z -= cf[3 * k + 2]; }
+        }
+        // VX3 cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859; VX3_Voxel::force,
+        // VX3_Voxel.cu:376): surface voxels of a cilia material, once it is switched on, are
+        // pushed along their base cilia force rotated into the world frame (no signals: the
+        // signal-scaled shift term is zero)
+        if ((flags & SF_CILIA) && !(fl & VF_INTERIOR) && m.cilia != 0 && !fp64i::gt(m.ciliaOn, st.t_now)) {
+            const d3 cf = qrot(q, D3(S.cilia[v], S.cilia[nv + v], S.cilia[2 * nv + v]));
+            F = D3(F.x + cf.x * m.cilia, F.y + cf.y * m.cilia, F.z + cf.z * m.cilia);
+        }
+        // VX3 force field (VX3_Voxel::timeStep, VX3_Voxel.cu:178-184): formulas of the voxel's
+        // position and the simulation's time, recent angle and voxel count
+        if (flags & SF_FFIELD) {
+            MathVars mv;
+            mv.x = pos.x; mv.y = pos.y; mv.z = pos.z; mv.hit = 0; mv.t = st.t_now; mv.angle = st.angle;
+            mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = nv;
+            F.x += mathtree_eval(S.ffield[0], mv);
+            F.y += mathtree_eval(S.ffield[1], mv);
+            F.z += mathtree_eval(S.ffield[2], mv);
         }
         // floorForce()
         const d3 F0 = F;
@@ -536,7 +562,8 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, doub
     }
     // actuation temperature for the next step
     float temp_next = temp;
-    if (flags & SF_VARY) {
+    // (VX3: no update before the material's TurnOnThermalExpansionAfterThisManySeconds)
+    if ((flags & SF_VARY) && !fp64i::gt(m.thermalOn, st.t_next)) {
         const float two_pi = 2 * 3.1415926f;
         double T = S.temp_amp * sin((double)two_pi * (t_cycles + __ldg(S.phase + v)));
         if (!(flags & SF_EXPAND) && fp64i::gt0(T)) T = 0;
@@ -636,7 +663,8 @@ __global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims,
         // one FP64 division per item instead of one per voxel
         if (threadIdx.x == 0) s_cycles = (S.flags & SF_VARY) ? t_next / S.temp_period : 0.0;
         __syncthreads();
-        const double t_cycles = s_cycles;
+        StepTimes st;
+        st.t_now = c.t; st.t_next = t_next; st.t_cycles = s_cycles; st.angle = c.recent_angle;
         const int64_t stepno = c.steps + 1;
         const bool com_step = c.cycle_step > 0 && (stepno % c.cycle_step) == 0;
         const int flags = S.flags;
@@ -647,9 +675,9 @@ __global__ void __launch_bounds__(256, 2) k_voxels(const Sim* __restrict__ sims,
             if (n <= kOrderMax) {
                 order_by_key(n, VoxelKey{S.vfl, w.begin}, s_perm, s_warp);
                 for (int k = threadIdx.x; k < n; k += blockDim.x)
-                    voxel_update(S, w.begin + s_perm[k], dt, t_cycles, flags, com_step ? acc : nullptr, hnext);
+                    voxel_update(S, w.begin + s_perm[k], dt, st, flags, com_step ? acc : nullptr, hnext);
             } else {
-                for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, t_cycles, flags, com_step ? acc : nullptr, hnext);
+                for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, st, flags, com_step ? acc : nullptr, hnext);
             }
         }
         if (com_step) {
@@ -698,7 +726,7 @@ __global__ void k_init_temp(const Sim* __restrict__ sims, int sim, float initial
     const Sim& S = sims[sim];
     const float two_pi = 2 * 3.1415926f;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < S.nv; v += gridDim.x * blockDim.x) {
-        if (S.flags & SF_VARY) {
+        if ((S.flags & SF_VARY) && !fp64i::gt(S.vm[S.vmat[v]].thermalOn, 0.0)) {
             double T = S.temp_amp * sin((double)two_pi * (0.0 / S.temp_period + S.phase[v]));
             if (!(S.flags & SF_EXPAND) && T > 0) T = 0;
             S.temp[v] = (float)T;

@@ -28,6 +28,7 @@ constexpr uint32_t VF_FLOORC = 1u << 10;  // last step: the voxel touched the fl
 
 // sim flag bits
 constexpr int SF_FLOOR = 1, SF_COLLIDE = 2, SF_VARY = 4, SF_EXPAND = 8;
+constexpr int SF_CILIA = 16, SF_FFIELD = 32;   // VX3 extras: cilia forces, force-field formulas
 
 struct VMat {
     float E, nu, cte, mus, muk, eHat;
@@ -44,6 +45,8 @@ struct VMat {
     double massInvD, IinvD, gDampTD, gDampRD, cDampTD, gravForceD;
     double halfNom;       // nom/2
     double halfMassInv;   // 0.5*(double)massInv
+    // VX3 material extras: cilia force scale and start time, thermal actuation start time
+    double cilia, ciliaOn, thermalOn;
 };
 
 struct LMat {
@@ -99,6 +102,9 @@ struct Sim {
     int32_t* hash_next;         // per voxel
     float4* cpos;               // per hashed voxel: position rounded to float, float base size (broadphase only)
     float inv_cell;             // 1 / cell_size, for the float cell index
+    // VX3 extras
+    const double* cilia;        // BaseCiliaForce, 3 blocks of nv (SF_CILIA)
+    const MathTree* ffield;     // x, y, z force-field formulas (SF_FFIELD)
 };
 
 // Mutable per-simulation control block.

@@ -394,6 +394,9 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
             pm.mu_static = get_d(mech, "uStatic", 0);
             pm.mu_kinetic = get_d(mech, "uDynamic", 0);
             pm.is_measured = get_i(mech, "isMeasured", 1);
+            pm.cilia = get_d(mech, "Cilia", 0);
+            pm.cilia_on_after = get_d(mech, "TurnOnCiliaAfterThisManySeconds", 0);
+            pm.thermal_on_after = get_d(mech, "TurnOnThermalExpansionAfterThisManySeconds", 0);
             if (const XmlNode* ss = mech ? mech->child("SSData") : nullptr) {
                 if (const XmlNode* se = ss->child("StrainData"))
                     for (auto* c : se->children_named("Strain")) pm.strain_data.push_back(atof_s(c->text));
@@ -448,6 +451,29 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
                 if (cells[(size_t)k * X * Y + j] > 0) phase_by_voxel.push_back(j < (int)arr.size() ? atof_s(arr[j]) : 0.0);
         }
     }
+    /* BaseCiliaForce: per filled cell an x,y,z triple, layer by layer; a short layer pads with
+       zeros (VXA/VX_Object.cpp:1886-1921) */
+    if (const XmlNode* bcf = st->child("BaseCiliaForce")) {
+        auto pl = bcf->children_named("Layer");
+        for (int k = 0; k < Z; k++) {
+            std::vector<std::string> arr;
+            if (k < (int)pl.size()) {
+                const std::string& raw = pl[k]->text;
+                size_t s = 0;
+                for (;;) {
+                    size_t c = raw.find(',', s);
+                    arr.push_back(raw.substr(s, c == std::string::npos ? std::string::npos : c - s));
+                    if (c == std::string::npos) break;
+                    s = c + 1;
+                }
+            }
+            for (int j = 0; j < X * Y; j++) {
+                if (cells[(size_t)k * X * Y + j] == 0) continue;
+                for (int c = 0; c < 3; c++)
+                    d->base_cilia.push_back(arr.size() > (size_t)(3 * j + c) && arr.size() > (size_t)(3 * j) ? atof_s(arr[3 * j + c]) : 0.0);
+            }
+        }
+    }
     int n = 0;
     for (long i = 0; i < (long)X * Y * Z; i++) {
         int mi = (int)(signed char)cells[i] - 1;
@@ -471,6 +497,24 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     d->record_step_size = (int)ptree_num(*root, "VXA.Simulator.RecordHistory.RecordStepSize", 0);
     d->record_voxel = (int)ptree_num(*root, "VXA.Simulator.RecordHistory.RecordVoxel", 1);
     d->record_link = (int)ptree_num(*root, "VXA.Simulator.RecordHistory.RecordLink", 0);
+    /* VX3 extras: cilia switch and force field; an absent force-field component is the constant 0
+       (VX3_ForceField's default, Utils/VX3_ForceField.h:10-19) */
+    d->enable_cilia = (int)ptree_num(*root, "VXA.Simulator.EnableCilia", 0);
+    const char* ff_paths[3] = {"VXA.Simulator.ForceField.x_forcefield", "VXA.Simulator.ForceField.y_forcefield",
+                               "VXA.Simulator.ForceField.z_forcefield"};
+    for (int k = 0; k < 3; k++) {
+        MathTree& m = d->force_field[k];
+        if (const XmlNode* n = root->path(ff_paths[k])) {
+            parse_mathtree(n, &m);
+            if (!m.valid) { *err = "invalid force-field formula"; return false; }
+            const bool zero = m.n == 2 && m.tok[0].op == mtCONST && m.tok[0].value == 0.0;
+            if (!zero) d->has_force_field = true;
+        } else {
+            m.n = 2; m.valid = 1;
+            m.tok[0].op = mtCONST; m.tok[0].value = 0.0;
+            m.tok[1].op = mtEND; m.tok[1].value = 0.0;
+        }
+    }
     parse_mathtree(root->path("VXA.Simulator.StopCondition.StopConditionFormula"), &d->stop_formula);
     parse_mathtree(root->path("VXA.Simulator.FitnessFunction"), &d->fitness);
     return true;

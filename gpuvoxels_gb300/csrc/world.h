@@ -22,6 +22,9 @@ struct PaletteMaterial {
     int is_measured = 1;
     std::string name;
     float rgba[4] = {0.5f, 0.5f, 0.5f, 1.0f};   // Display colour (history recorder)
+    // VX3 material keys (VXA/VX_Object.cpp:1425-1437): cilia force scale and start time,
+    // thermal actuation start time
+    double cilia = 0, cilia_on_after = 0, thermal_on_after = 0;
 };
 
 struct External {
@@ -55,6 +58,12 @@ struct SimDesc {
     double max_dist_pairs = 0;     // MaxDistInVoxelLengthsToCountAsPair
     int record_step_size = 0;      // VXA.Simulator.RecordHistory.* (VX3_SimulationManager.cu:344-346)
     int record_voxel = 1, record_link = 0;
+    // VX3 extras: cilia (VXA.Simulator.EnableCilia; per-voxel BaseCiliaForce, 3 per voxel, empty
+    // when absent) and the force field (VXA.Simulator.ForceField.{x,y,z}_forcefield)
+    int enable_cilia = 0;
+    std::vector<double> base_cilia;
+    MathTree force_field[3];
+    bool has_force_field = false;
 };
 
 // Parses a base VXA plus an optional VXD (whose children carrying replace="VXA.a.b"
