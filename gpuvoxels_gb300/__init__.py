@@ -340,9 +340,11 @@ class SimulationManager:
     def start(self):
         base_xml = open(self.base).read()
         self.ctx = Context(0, self.budget)
+        vxds = []
         for f in self.files:
-            vxd = open(os.path.join(self.input_dir, f)).read()
-            self.ids.append(self.ctx.load_vxa(base_xml, vxd, os.path.basename(f)))
+            with open(os.path.join(self.input_dir, f)) as fh:
+                vxds.append(fh.read())
+        self.ids = self.ctx.load_many(vxds, base=base_xml, names=[os.path.basename(f) for f in self.files])
         self.ctx.run(self.ids, self.mode)
         res = []
         for f, i in zip(self.files, self.ids):

@@ -37,7 +37,9 @@ def _flags(src: str):
               "-I", os.path.join(HERE, "..", "include")]
     if src.endswith(".cu"):
         fmad = "-fmad=true" if src == "kernels_fast.cu" else "-fmad=false"
-        return common + ARCH + ["-lineinfo", fmad, "-Xptxas", "-warn-spills"]
+        # GVX_NVCC_DEFINES: extra -D tuning knobs for the kernels, e.g. "GVX_LINKS_MIN_BLOCKS=3"
+        defs = ["-D" + x for x in os.environ.get("GVX_NVCC_DEFINES", "").split()]
+        return common + ARCH + ["-lineinfo", fmad, "-Xptxas", "-warn-spills"] + defs
     return common
 
 

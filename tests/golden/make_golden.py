@@ -121,7 +121,7 @@ def sample_worlds():
             xml = xml[:i] + DAMPING_DEFAULTS + xml[i:]
         # cilia are a VX3-only force the reference's CPU path does not apply: switched off so that the
         # reference's output is the expected one (the cilia themselves are tested on their own)
-        xml = re.sub(r"<EnableCilia>\s*1\s*</EnableCilia>", "<EnableCilia>0</EnableCilia>", xml)
+        xml = re.sub(r"(<EnableCilia(?:\s[^>]*)?>)\s*1\s*(</EnableCilia>)", r"\g<1>0\g<2>", xml)
         w[name] = dict(vxa=xml, ext=[], snaps=snaps)
     return w
 

@@ -92,7 +92,7 @@ def test_cilia_only_on_surface_voxels(ctx):
 def test_thermal_expansion_start_time(ctx):
     c = synth.config0_creature(1)
     delayed = c.vxa.replace("<Mechanical>", "<Mechanical><TurnOnThermalExpansionAfterThisManySeconds>0.01"
-                                            "</TurnOnThermalExpansionAfterThisManySeconds>")
+                                            "</TurnOnThermalExpansionAfterThisManySeconds>", 1)
     sim = ctx.load_vxa(delayed)
     try:
         info = g.inspect_vxa(delayed)

@@ -57,6 +57,35 @@ def _structure_vxd(seed):
 
 
 @pytest.mark.gpu
+def test_simulation_manager_python_mirror(tmp_path):
+    """SimulationManager(sub_batches, base, input_dir).start() (the VX3_SimulationManager
+    mirror) runs the files as one batch; h_results are sorted by fitness and equal the
+    per-file results of the C ABI; write_report gives the worker's keys."""
+    base = synth.config0_creature(0, stop_time=0.01).vxa
+    (tmp_path / "base.vxa").write_text(base)
+    gen = tmp_path / "gen"
+    gen.mkdir()
+    names = [f"bot_{i:04d}.vxd" for i in range(3)]
+    for i, n in enumerate(names):
+        (gen / n).write_text(_structure_vxd(60 + i))
+    sm = g.SimulationManager([names[:2], names[2:]], base=str(tmp_path / "base.vxa"), input_dir=str(gen))
+    res = sm.start()
+    assert sorted(r.vxa_filename for r in res) == names
+    fits = [r.fitness_score for r in res]
+    assert fits == sorted(fits, reverse=True)
+    with g.Context(0, 1 << 30) as ctx:
+        for n in names:
+            sid = ctx.load_vxa(base, (gen / n).read_text(), name=n)
+            ctx.run([sid])
+            r = ctx.result(sid)
+            mine = [x for x in res if x.vxa_filename == n][0]
+            assert mine.fitness_score == r.fitness_score and mine.current_time == r.current_time
+    sm.write_report(str(tmp_path / "report.xml"))
+    rep = ET.parse(tmp_path / "report.xml").getroot()
+    assert rep.find("bestfit/filename").text == res[0].vxa_filename
+
+
+@pytest.mark.gpu
 def test_worker_generation_report(worker, tmp_path):
     base = synth.config0_creature(0, stop_time=0.01).vxa
     base = base.replace("<Simulator>", "<Simulator><SavePositionOfAllVoxels>1</SavePositionOfAllVoxels>", 1)
