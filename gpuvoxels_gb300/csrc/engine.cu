@@ -111,8 +111,7 @@ public:
     double* d_partials_ = nullptr;
     double* d_com4_ = nullptr;
     // tuning
-    // link work items are claimed per warp (items_links_ links each), voxel items per block
-    int block_links_ = 256, block_voxels_ = 256, items_links_ = 128, items_voxels_ = 256, graph_steps_ = 64;
+    int block_links_ = 256, block_voxels_ = 256, items_links_ = 256, items_voxels_ = 256, graph_steps_ = 64;
     int sm_count_ = 152;
     int profiling_ = 0;
     KernelSet ks_ = kernelset_exact();
@@ -1095,8 +1094,8 @@ public:
         if (int e = prepare(ids, n, &rs, err)) return e;
         std::vector<int> slots;
         for (auto* r : rs) slots.push_back(r->slot);
-        struct Cand { int bl, bv, il, iv; };   // link items are per warp, voxel items per block
-        const Cand cands[] = {{128, 128, 64, 128}, {128, 256, 128, 256}, {256, 256, 128, 256}, {256, 256, 256, 512}, {256, 256, 64, 256}};
+        struct Cand { int bl, bv, il, iv; };
+        const Cand cands[] = {{128, 128, 256, 128}, {128, 256, 512, 256}, {256, 256, 256, 256}, {256, 256, 512, 256}, {256, 256, 1024, 512}};
         double best = 1e30;
         Cand bc = cands[2];
         // snapshot the simulations' device regions so tuning does not advance them

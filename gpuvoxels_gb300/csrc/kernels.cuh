@@ -221,36 +221,6 @@ __device__ __forceinline__ void order_by_key(int n, KeyFn key, int* perm, int* w
     }
 }
 
-// The same grouping done by one warp over its own work item (n <= kWarpOrderMax), with
-// ballots only: no block barrier, so warps of a block never wait for one another.
-constexpr int kWarpOrderMax = 256;
-
-template <typename KeyFn>
-__device__ __forceinline__ void warp_order_by_key(int n, KeyFn key, int* perm) {
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    int start[kOrderKeys];
-    for (int k = 0; k < kOrderKeys; k++) start[k] = 0;
-    for (int j0 = 0; j0 < n; j0 += 32) {
-        const int kj = j0 + lane < n ? key(j0 + lane) : -1;
-#pragma unroll
-        for (int k = 0; k < kOrderKeys; k++) start[k] += __popc(__ballot_sync(0xffffffffu, kj == k));
-    }
-    int acc = 0;
-    for (int k = 0; k < kOrderKeys; k++) { const int c = start[k]; start[k] = acc; acc += c; }
-    for (int j0 = 0; j0 < n; j0 += 32) {
-        const int j = j0 + lane;
-        const int kj = j < n ? key(j) : -1;
-#pragma unroll
-        for (int k = 0; k < kOrderKeys; k++) {
-            const unsigned b = __ballot_sync(0xffffffffu, kj == k);
-            if (kj == k) perm[start[k] + __popc(b & below)] = j;
-            start[k] += __popc(b);
-        }
-    }
-    __syncwarp();
-}
-
 // Link key: small-angle mode, then within each mode which rotation branches were taken.
 struct LinkKey {
     const uint8_t* lfl;
@@ -270,17 +240,17 @@ struct LinkKey {
 #define GVX_VOXELS_MIN_BLOCKS 2
 #endif
 
-// Each warp claims its own work items (a link range of one simulation) from the queue and
-// orders them by key on its own: warps never wait at a block barrier for slower warps.
+// Blocks claim work items (a link range of one simulation) and order each by key
+// across all of the block's warps.  (Per-warp items without block barriers were
+// measured slower: ordering 128 links per warp groups the paths less well than
+// 256 per block, and FP64 lane use fell from 84 % to 80 %.)
 __global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
-    __shared__ int s_perm[8][kWarpOrderMax];
-    const int lane = threadIdx.x & 31;
-    int* perm = s_perm[(threadIdx.x >> 5) & 7];
+    __shared__ int s_item;
+    __shared__ int s_perm[kOrderMax];
+    __shared__ int s_warp[kOrderKeys * 8];
     if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; }
     for (;;) {
-        int it = 0;
-        if (lane == 0) it = atomicAdd(&tickets[0], 1);
-        it = __shfl_sync(0xffffffffu, it, 0);
+        const int it = claim(&tickets[0], &s_item);
         if (it >= n_items) break;
         const Item w = items[it];
         Ctl& c = ctl[w.sim];
@@ -289,14 +259,13 @@ __global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* 
         const float dt = c.dt;
         bool div = false;
         const int n = w.end - w.begin;
-        if (n <= kWarpOrderMax) {
-            warp_order_by_key(n, LinkKey{S.lfl, w.begin}, perm);
-            for (int k = lane; k < n; k += 32) link_update(S, w.begin + perm[k], dt, &div);
+        if (n <= kOrderMax) {
+            order_by_key(n, LinkKey{S.lfl, w.begin}, s_perm, s_warp);
+            for (int k = threadIdx.x; k < n; k += blockDim.x) link_update(S, w.begin + s_perm[k], dt, &div);
         } else {
-            for (int l = w.begin + lane; l < w.end; l += 32) link_update(S, l, dt, &div);
+            for (int l = w.begin + threadIdx.x; l < w.end; l += blockDim.x) link_update(S, l, dt, &div);
         }
-        if (__any_sync(0xffffffffu, div) && lane == 0) c.diverged = 1;
-        __syncwarp();
+        if (div) c.diverged = 1;
     }
 }
 

@@ -79,7 +79,7 @@ def test_simulation_manager_python_mirror(tmp_path):
             ctx.run([sid])
             r = ctx.result(sid)
             mine = [x for x in res if x.vxa_filename == n][0]
-            assert mine.fitness_score == r.fitness_score and mine.current_time == r.current_time
+            assert mine.fitness_score == r.fitness_score and mine.currentTime == r.current_time
     sm.write_report(str(tmp_path / "report.xml"))
     rep = ET.parse(tmp_path / "report.xml").getroot()
     assert rep.find("bestfit/filename").text == res[0].vxa_filename
