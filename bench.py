@@ -313,17 +313,17 @@ def run_ours(args):
         ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
         c2.step(ids2, args.steps, g.BATCHED)
         d2h = 0
-        for i in ids2:
-            pos, q, fl = c2.get_state(i)
-            d2h += pos.nbytes + q.nbytes + fl.nbytes
+        pos, q, fl, _ = c2.get_states(ids2)      # every creature's pose, one device pass and one copy
+        d2h += pos.nbytes + q.nbytes + fl.nbytes
         e2e_wall = time.perf_counter() - t0
         h2d = c2.bytes_in_use()
         e2e_vs = sum(c2.info(i).num_voxel for i in ids2) * args.steps
         c2.close()
         e2e = dict(value=e2e_vs / e2e_wall, unit="voxel-steps/s", h2d_bytes_per_step=int(h2d / args.steps),
                    d2h_bytes_per_step=int(d2h / args.steps),
-                   note="wall clock of vx3_load_vxa (host VXA parse + topology) for every creature, the upload, "
-                        f"{args.steps} batched steps and the read-back of every voxel's pose")
+                   note="wall clock of vx3_load_vxa_many (host VXA parse + topology for every creature, on "
+                        f"host threads), the upload, {args.steps} batched steps and vx3_get_states (every voxel's "
+                        "pose, one device pass and one copy)")
     if rank != 0:
         if dist:
             dist.destroy_process_group()

@@ -35,7 +35,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
-           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals"]
+           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -94,6 +94,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_load_vxa_many": (I, [P, S, P, P, I, P, P]),
         "vx3_record_history": (I, [P, I64, S]),
         "vx3_inspect_externals": (I, [S, S, P, P, P]),
+        "vx3_get_states": (I, [P, P, I, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -271,6 +272,17 @@ class Context:
         pos = np.zeros((nv, 3)); q = np.zeros((nv, 4)); fl = np.zeros(nv, np.uint8)
         self._check(self.L.vx3_get_state(self.h, sim, _p(pos), _p(q), _p(fl)))
         return pos, q, fl
+
+    def get_states(self, ids):
+        """Poses of many simulations in one device pass: (pos, orient, flags, offsets) with the
+        simulations' voxels one after another; simulation k owns rows offsets[k]:offsets[k+1]."""
+        a = self._ids(ids)
+        counts = [self.info(int(i)).num_voxel for i in a]
+        offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        tot = int(offsets[-1])
+        pos = np.zeros((tot, 3)); q = np.zeros((tot, 4)); fl = np.zeros(tot, np.uint8)
+        self._check(self.L.vx3_get_states(self.h, _p(a), len(a), _p(pos), _p(q), _p(fl)))
+        return pos, q, fl, offsets
 
     def write_report(self, ids, path: str, input_dir: str = ""):
         a = self._ids(ids)

@@ -340,6 +340,13 @@ int vx3_get_state(vx3_ctx* c, vx3_sim_id id, double* pos, double* orient, uint8_
     return VX3_OK;
 }
 
+int vx3_get_states(vx3_ctx* c, const vx3_sim_id* ids, int n, double* pos, double* orient, uint8_t* flags) {
+    if (!c || n < 0 || (n > 0 && !ids)) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->gather_states(ids, n, pos, orient, flags, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
 int vx3_get_voxel_state(vx3_ctx* c, vx3_sim_id id, double* d13, float* f4, int32_t* flags) {
     if (!c) return VX3_E_ARG;
     std::string err;

@@ -30,6 +30,23 @@ double now_s() {
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// Control-block updates for a list of slots (one launch instead of per-slot copies).
+__global__ void k_ctl_run(dev::Ctl* ctl, const int* __restrict__ slots, const int64_t* __restrict__ targets, int n, int no_stop) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dev::Ctl& c = ctl[slots[k]];
+    c.status = SIM_RUNNING;
+    c.target = targets[k];
+    c.no_stop = no_stop;
+}
+__global__ void k_ctl_end_steps(dev::Ctl* ctl, const int* __restrict__ slots, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dev::Ctl& c = ctl[slots[k]];
+    c.no_stop = 0;
+    if (c.status == SIM_DONE) c.status = SIM_IDLE;
+}
+
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // First-fit allocator over one device allocation (the HBM budget).
@@ -89,6 +106,8 @@ struct SimRec {
     SimResult result{};
     int n_vox_items = 0;
     std::vector<double> final_pos;  // x block, y block, z block at finish (SavePositionOfAllVoxels only)
+    dev::Ctl pending_ctl{};         // control block between upload_begin and upload_finish
+    dev::Sim pending_sim{};         // device descriptor between upload_begin and upload_finish
 };
 
 class EngineImpl final : public Engine {
@@ -128,10 +147,29 @@ public:
     cudaGraphExec_t graph_ = nullptr;
     int graph_len_ = 0;
     bool batch_dirty_ = true;
+    // pinned host staging: two upload buffers used in turn (the copy of one simulation's
+    // region overlaps filling the next), and one buffer for batched state read-back
+    struct Pinned {
+        char* p = nullptr;
+        size_t cap = 0;
+        cudaEvent_t done = nullptr;   // the last copy out of this buffer
+    };
+    Pinned up_[2];
+    int up_next_ = 0;
+    Pinned rb_;
+    char* d_gather_ = nullptr;
+    size_t cap_gather_ = 0;
+    static constexpr size_t kPinnedUploadMax = 256u << 20;   // larger regions are copied from pageable memory
 
     ~EngineImpl() override {
         if (graph_) cudaGraphExecDestroy(graph_);
         cudaSetDevice(device_);
+        if (stream_) cudaStreamSynchronize(stream_);
+        for (Pinned* b : {&up_[0], &up_[1], &rb_}) {
+            if (b->p) cudaFreeHost(b->p);
+            if (b->done) cudaEventDestroy(b->done);
+        }
+        cudaFree(d_gather_);
         cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_partials_); cudaFree(d_com4_);
         cudaFree(arena_base_);
         if (ev0_) cudaEventDestroy(ev0_);
@@ -158,7 +196,21 @@ public:
         CK(cudaMalloc(&d_tickets_, 4 * sizeof(int)));
         CK(cudaMemset(d_tickets_, 0, 4 * sizeof(int)));
         CK(cudaMalloc(&d_com4_, 4 * sizeof(double)));
+        for (Pinned* b : {&up_[0], &up_[1], &rb_}) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
         return grow_slots(64, err);
+    }
+
+    // A pinned buffer of at least `bytes`, once its previous copy has finished.
+    int pinned(Pinned* b, size_t bytes, std::string* err) {
+        CK(cudaEventSynchronize(b->done));
+        if (b->cap >= bytes) return 0;
+        if (b->p) CK(cudaFreeHost(b->p));
+        b->p = nullptr;
+        b->cap = 0;
+        const size_t cap = std::max<size_t>(bytes, 16u << 20);
+        CK(cudaHostAlloc((void**)&b->p, cap, cudaHostAllocDefault));
+        b->cap = cap;
+        return 0;
     }
 
     int grow_slots(int n, std::string* err) {
@@ -340,6 +392,16 @@ public:
     // Copies a simulation's topology and initial state to the device.
     int upload(SimRec* r, std::string* err) {
         if (r->resident) return 0;
+        std::vector<SimRec*> one;
+        if (int e = upload_begin(r, err)) return e;
+        one.push_back(r);
+        return upload_finish(one, err);
+    }
+
+    // First half of an upload, without waiting for the device: region image, copies and
+    // the initial temperature / stable-step / hash kernels.  Many simulations are begun
+    // and then finished together (one synchronisation for the whole generation).
+    int upload_begin(SimRec* r, std::string* err) {
         SimWorld& w = r->w;
         Layout L;
         Offs o;
@@ -355,12 +417,32 @@ public:
             if (e) { arena_.release(off, L.total); return e; }
             slot = free_slot();
         }
+        slot_owner_[slot] = r;   // taken now, so that the next begun upload picks another slot
+        r->slot = slot;
         r->off = off;
         r->bytes = L.total;
         char* base = arena_base_ + off;
-        std::vector<char> h(L.total, 0);
+        // host image of the region: built in a pinned staging buffer so that its copy runs
+        // asynchronously while the next simulation's image is filled (pageable for huge regions)
+        std::vector<char> hv;
+        char* hp = nullptr;
+        Pinned* stage = nullptr;
+        if (L.total <= kPinnedUploadMax) {
+            stage = &up_[up_next_];
+            up_next_ ^= 1;
+            if (int e = pinned(stage, L.total, err)) {
+                arena_.release(off, L.total);
+                slot_owner_[slot] = nullptr;
+                return e;
+            }
+            hp = stage->p;
+            memset(hp, 0, L.total);
+        } else {
+            hv.assign(L.total, 0);
+            hp = hv.data();
+        }
         const size_t nv = w.nv, nl = w.nl;
-        auto P = [&](size_t o2) { return h.data() + o2; };
+        auto P = [&](size_t o2) { return hp + o2; };
         // materials
         dev::VMat* vm = (dev::VMat*)P(o.vm);
         for (size_t i = 0; i < w.vmats.size(); i++) {
@@ -495,54 +577,106 @@ public:
         }
         if (w.desc.enable_cilia) S.cilia = (const double*)D(o.cilia);
         if (w.desc.has_force_field) S.ffield = (const MathTree*)D(o.ffield);
-        CK(cudaMemcpyAsync(base, h.data(), L.total, cudaMemcpyHostToDevice, stream_));
-        CK(cudaMemcpyAsync(d_sims_ + slot, &S, sizeof(S), cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(base, hp, L.total, cudaMemcpyHostToDevice, stream_));
+        if (stage) CK(cudaEventRecord(stage->done, stream_));
+        // the descriptor and control block go to the device with the others in upload_finish
+        r->pending_sim = S;
         dev::Ctl c{};
         c.status = SIM_IDLE;
         c.stop = w.desc.stop_formula;
         c.hash_parity = 0;
-        CK(cudaMemcpyAsync(d_ctl_ + slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
-        // first actuation temperature (t = 0), then the stable step from it
-        int g = std::min(4 * sm_count_, (int)((nv + 255) / 256));
-        ks_.init_temp(std::max(1, g), stream_, d_sims_, slot, w.desc.initial_temp);
+        r->pending_ctl = c;
+        return 0;
+    }
+
+    // Second half: reads every begun simulation's largest link frequency in one strided
+    // copy, derives the time steps on the host (the reference's float arithmetic) and
+    // writes the control blocks, with one synchronisation in all.
+    int upload_finish(const std::vector<SimRec*>& rs, std::string* err) {
+        if (rs.empty()) return 0;
+        const size_t n = rs.size();
+        // pinned image: descriptors, first control blocks, slot list, initial temperatures,
+        // every slot's frequency word, the final control blocks
+        auto al = [](size_t x) { return (x + 63) & ~(size_t)63; };
+        const size_t o_sim = 0, o_ctl0 = al(o_sim + sizeof(dev::Sim) * n), o_slot = al(o_ctl0 + sizeof(dev::Ctl) * n);
+        const size_t o_init = al(o_slot + 4 * n), o_bits = al(o_init + 4 * n), o_ctl = al(o_bits + 4 * (size_t)cap_slots_);
+        const size_t total = al(o_ctl + sizeof(dev::Ctl) * n);
+        if (int e = pinned(&rb_, total, err)) return e;
+        if (total > cap_gather_) {
+            CK(cudaStreamSynchronize(stream_));
+            cudaFree(d_gather_);
+            d_gather_ = nullptr;
+            cap_gather_ = 0;
+            CK(cudaMalloc(&d_gather_, total));
+            cap_gather_ = total;
+        }
+        char* h = rb_.p;
+        dev::Sim* sim_img = (dev::Sim*)(h + o_sim);
+        dev::Ctl* ctl0_img = (dev::Ctl*)(h + o_ctl0);
+        int* slot_img = (int*)(h + o_slot);
+        float* init_img = (float*)(h + o_init);
+        int max_nv = 1, max_nl = 1, max_ns = 1;
+        for (size_t k = 0; k < n; k++) {
+            SimRec* r = rs[k];
+            sim_img[k] = r->pending_sim;
+            ctl0_img[k] = r->pending_ctl;
+            slot_img[k] = r->slot;
+            init_img[k] = r->w.desc.initial_temp;
+            max_nv = std::max(max_nv, r->w.nv);
+            max_nl = std::max(max_nl, r->w.nl);
+            max_ns = std::max(max_ns, r->w.surface_count);
+            CK(cudaMemcpyAsync(d_sims_ + r->slot, &sim_img[k], sizeof(dev::Sim), cudaMemcpyHostToDevice, stream_));
+            CK(cudaMemcpyAsync(d_ctl_ + r->slot, &ctl0_img[k], sizeof(dev::Ctl), cudaMemcpyHostToDevice, stream_));
+        }
+        CK(cudaMemcpyAsync(d_gather_ + o_slot, h + o_slot, o_bits - o_slot, cudaMemcpyHostToDevice, stream_));
+        const int* d_slots = (const int*)(d_gather_ + o_slot);
+        const float* d_init = (const float*)(d_gather_ + o_init);
+        // first actuation temperature (t = 0), then the stable step from it, then the collision hash
+        auto blocks = [&](int elems) { return std::max(1, std::min(4 * sm_count_, (elems + 255) / 256) / (int)std::min<size_t>(n, 64)); };
+        ks_.init_temp(blocks(max_nv), stream_, d_sims_, d_slots, d_init, (int)n);
         CK(cudaGetLastError());
-        if (nl > 0) {
-            int gl = std::min(4 * sm_count_, (int)((nl + 255) / 256));
-            ks_.dt(std::max(1, gl), stream_, d_sims_, d_ctl_, slot);
-            CK(cudaGetLastError());
-        }
-        if (w.desc.collisions && w.surface_count > 0) {
-            ks_.hash_build(std::max(1, std::min(4 * sm_count_, (w.surface_count + 255) / 256)), stream_, d_sims_, d_ctl_, slot);
-            CK(cudaGetLastError());
-        }
-        uint32_t bits = 0;
-        CK(cudaMemcpyAsync(&bits, &d_ctl_[slot].maxf2_bits, 4, cudaMemcpyDeviceToHost, stream_));
+        ks_.dt(blocks(max_nl), stream_, d_sims_, d_ctl_, d_slots, (int)n);
+        CK(cudaGetLastError());
+        ks_.hash_build(blocks(max_ns), stream_, d_sims_, d_ctl_, d_slots, (int)n);
+        CK(cudaGetLastError());
+        uint32_t* bits_all = (uint32_t*)(h + o_bits);
+        dev::Ctl* ctl_img = (dev::Ctl*)(h + o_ctl);
+        CK(cudaMemcpy2DAsync(bits_all, sizeof(uint32_t), &d_ctl_[0].maxf2_bits, sizeof(dev::Ctl), sizeof(uint32_t), cap_slots_,
+                             cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
-        float maxf2;
-        memcpy(&maxf2, &bits, 4);
-        if (!(maxf2 > 0.0f)) {   // no links: per-voxel frequencies (Voxelyze.cpp:302-307)
-            maxf2 = 0.0f;
-            for (size_t i = 0; i < nv; i++) {
-                const VoxelMaterial& m = w.vmats[w.desc.voxels[4 * i + 3]];
-                float f2 = (float)(m.E * m.nom / m.mass);
-                if (f2 > maxf2) maxf2 = f2;
+        for (size_t k = 0; k < rs.size(); k++) {
+            SimRec* r = rs[k];
+            const SimWorld& w = r->w;
+            const uint32_t bits = bits_all[r->slot];
+            float maxf2;
+            memcpy(&maxf2, &bits, 4);
+            if (!(maxf2 > 0.0f)) {   // no links: per-voxel frequencies (Voxelyze.cpp:302-307)
+                maxf2 = 0.0f;
+                for (int i = 0; i < w.nv; i++) {
+                    const VoxelMaterial& m = w.vmats[w.desc.voxels[4 * i + 3]];
+                    float f2 = (float)(m.E * m.nom / m.mass);
+                    if (f2 > maxf2) maxf2 = f2;
+                }
             }
+            float opt = maxf2 <= 0.0f ? 0.0f : 1.0f / (6.283185f * sqrtf(maxf2));
+            if (opt < 1e-10f) opt = 1e-10f;
+            r->optdt = opt;
+            r->dt = (float)(w.desc.dt_frac * (double)opt);
+            r->cycle_step = r->dt > 0 ? (int)(w.desc.temp_period / r->dt) : 0;
+            dev::Ctl& c = ctl_img[k];
+            c = r->pending_ctl;
+            c.dt = r->dt;
+            c.optdt = opt;
+            c.cycle_step = r->cycle_step;
+            c.maxf2_bits = bits;
+            CK(cudaMemcpyAsync(d_ctl_ + r->slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
         }
-        float opt = maxf2 <= 0.0f ? 0.0f : 1.0f / (6.283185f * sqrtf(maxf2));
-        if (opt < 1e-10f) opt = 1e-10f;
-        r->optdt = opt;
-        r->dt = (float)(w.desc.dt_frac * (double)opt);
-        r->cycle_step = r->dt > 0 ? (int)(w.desc.temp_period / r->dt) : 0;
-        c.dt = r->dt;
-        c.optdt = opt;
-        c.cycle_step = r->cycle_step;
-        c.maxf2_bits = bits;
-        CK(cudaMemcpyAsync(d_ctl_ + slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+        CK(cudaEventRecord(rb_.done, stream_));
         CK(cudaStreamSynchronize(stream_));
-        r->slot = slot;
-        r->resident = true;
-        r->status = SIM_IDLE;
-        slot_owner_[slot] = r;
+        for (SimRec* r : rs) {
+            r->resident = true;
+            r->status = SIM_IDLE;
+        }
         batch_dirty_ = true;
         return 0;
     }
@@ -622,12 +756,48 @@ public:
         if (prof) cudaEventRecord(evk_[3], st);
     }
 
-    int set_running(const std::vector<int>& slots, const std::vector<int64_t>& targets, std::string* err) {
-        for (size_t i = 0; i < slots.size(); i++) {
-            int32_t st = SIM_RUNNING;
-            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].status, &st, 4, cudaMemcpyHostToDevice, stream_));
-            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].target, &targets[i], 8, cudaMemcpyHostToDevice, stream_));
+    // Marks the slots running towards their target step counts (no_stop: vx3_step's fixed
+    // count, the stop formula is not applied), one copy of the lists and one kernel.
+    int set_running(const std::vector<int>& slots, const std::vector<int64_t>& targets, std::string* err, int no_stop = 0) {
+        if (slots.empty()) return 0;
+        const size_t n = slots.size(), o_tg = ((4 * n + 15) & ~(size_t)15), total = o_tg + 8 * n;
+        if (int e = pinned(&rb_, total, err)) return e;
+        if (total > cap_gather_) {
+            CK(cudaStreamSynchronize(stream_));
+            cudaFree(d_gather_);
+            d_gather_ = nullptr;
+            cap_gather_ = 0;
+            CK(cudaMalloc(&d_gather_, total));
+            cap_gather_ = total;
         }
+        memcpy(rb_.p, slots.data(), 4 * n);
+        memcpy(rb_.p + o_tg, targets.data(), 8 * n);
+        CK(cudaMemcpyAsync(d_gather_, rb_.p, total, cudaMemcpyHostToDevice, stream_));
+        CK(cudaEventRecord(rb_.done, stream_));
+        k_ctl_run<<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(d_ctl_, (const int*)d_gather_, (const int64_t*)(d_gather_ + o_tg),
+                                                                   (int)n, no_stop);
+        CK(cudaGetLastError());
+        return 0;
+    }
+
+    // After a vx3_step call: the stop formula applies again and DONE (target reached) is IDLE.
+    int end_fixed_steps(const std::vector<int>& slots, std::string* err) {
+        if (slots.empty()) return 0;
+        const size_t n = slots.size();
+        if (int e = pinned(&rb_, 4 * n, err)) return e;
+        if (4 * n > cap_gather_) {
+            CK(cudaStreamSynchronize(stream_));
+            cudaFree(d_gather_);
+            d_gather_ = nullptr;
+            cap_gather_ = 0;
+            CK(cudaMalloc(&d_gather_, 4 * n));
+            cap_gather_ = 4 * n;
+        }
+        memcpy(rb_.p, slots.data(), 4 * n);
+        CK(cudaMemcpyAsync(d_gather_, rb_.p, 4 * n, cudaMemcpyHostToDevice, stream_));
+        CK(cudaEventRecord(rb_.done, stream_));
+        k_ctl_end_steps<<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(d_ctl_, (const int*)d_gather_, (int)n);
+        CK(cudaGetLastError());
         return 0;
     }
 
@@ -637,14 +807,26 @@ public:
         return 0;
     }
 
+    // The scalar part of the control blocks of the slots lo..hi (one strided copy, one
+    // synchronisation); out[s - lo] holds slot s.
+    int read_ctls(int lo, int hi, std::vector<dev::Ctl>* out, std::string* err) {
+        out->resize((size_t)(hi - lo + 1));
+        CK(cudaMemcpy2DAsync(out->data(), sizeof(dev::Ctl), d_ctl_ + lo, sizeof(dev::Ctl), offsetof(dev::Ctl, stop),
+                             (size_t)(hi - lo + 1), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        return 0;
+    }
+
     // Runs until every listed simulation has left the RUNNING state.
     int drive(const std::vector<SimRec*>& rs, int mode, std::string* err) {
         int64_t vsteps_before = 0;
         std::vector<int64_t> steps0(rs.size());
-        for (size_t i = 0; i < rs.size(); i++) {
-            dev::Ctl c;
-            if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
-            steps0[i] = c.steps;
+        int slo = INT32_MAX, shi = -1;
+        for (auto* r : rs) { slo = std::min(slo, r->slot); shi = std::max(shi, r->slot); }
+        std::vector<dev::Ctl> cs;
+        if (!rs.empty()) {
+            if (int e = read_ctls(slo, shi, &cs, err)) return e;
+            for (size_t i = 0; i < rs.size(); i++) steps0[i] = cs[(size_t)(rs[i]->slot - slo)].steps;
         }
         timing_.launches = 0;
         double w0 = now_s();
@@ -733,24 +915,30 @@ public:
             cudaEventElapsedTime(&c, evk_[2], evk_[3]);
             timing_.link_kernel_ms = a; timing_.contact_kernel_ms = b; timing_.voxel_kernel_ms = c;
         }
-        for (size_t i = 0; i < rs.size(); i++) {
-            dev::Ctl c;
-            if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
-            rs[i]->status = c.status;
-            vsteps_before += (c.steps - steps0[i]) * rs[i]->w.nv;
+        if (!rs.empty()) {
+            if (int e = read_ctls(slo, shi, &cs, err)) return e;
+            for (size_t i = 0; i < rs.size(); i++) {
+                const dev::Ctl& c = cs[(size_t)(rs[i]->slot - slo)];
+                rs[i]->status = c.status;
+                vsteps_before += (c.steps - steps0[i]) * rs[i]->w.nv;
+            }
         }
         timing_.voxel_steps = vsteps_before;
         return 0;
     }
 
     int prepare(const int64_t* ids, int n, std::vector<SimRec*>* rs, std::string* err) {
+        std::vector<SimRec*> begun;
         for (int i = 0; i < n; i++) {
             SimRec* r = find(ids[i]);
             if (!r) { *err = "unknown simulation id"; return -6; }
-            if (int e = upload(r, err)) return e;
+            if (!r->resident) {
+                if (int e = upload_begin(r, err)) { upload_finish(begun, err); return e; }
+                begun.push_back(r);
+            }
             rs->push_back(r);
         }
-        return 0;
+        return upload_finish(begun, err);
     }
 
     int step(const int64_t* ids, int n, int mode, int64_t steps, std::string* err) override {
@@ -758,41 +946,29 @@ public:
         if (int e = prepare(ids, n, &rs, err)) return e;
         std::vector<int> slots;
         std::vector<int64_t> targets;
+        std::vector<SimRec*> act;
+        if (rs.empty()) return 0;
+        int lo = INT32_MAX, hi = -1;
+        for (auto* r : rs) { lo = std::min(lo, r->slot); hi = std::max(hi, r->slot); }
+        std::vector<dev::Ctl> cs;
+        if (int e = read_ctls(lo, hi, &cs, err)) return e;
         for (auto* r : rs) {
-            dev::Ctl c;
-            if (int e = read_ctl(r->slot, &c, err)) return e;
+            const dev::Ctl& c = cs[(size_t)(r->slot - lo)];
             if (c.status == SIM_DIVERGED || c.status == SIM_ERROR) continue;
             slots.push_back(r->slot);
             targets.push_back(c.steps + steps);
+            act.push_back(r);
         }
         if (slots.empty()) return 0;
-        // the stop formula is not applied by step(): clear it for the call, restore afterwards
-        std::vector<MathTree> saved(slots.size());
-        MathTree none;
-        none.n = 0;
-        for (size_t i = 0; i < slots.size(); i++) {
-            CK(cudaMemcpyAsync(&saved[i], &d_ctl_[slots[i]].stop, sizeof(MathTree), cudaMemcpyDeviceToHost, stream_));
-            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].stop, &none, sizeof(MathTree), cudaMemcpyHostToDevice, stream_));
-        }
-        CK(cudaStreamSynchronize(stream_));
-        if (int e = set_running(slots, targets, err)) return e;
-        std::vector<SimRec*> act;
-        for (auto* r : rs) if (std::find(slots.begin(), slots.end(), r->slot) != slots.end()) act.push_back(r);
+        // the stop formula is not applied by step() (no_stop), and reaching the target leaves the
+        // simulation IDLE for the next call
+        if (int e = set_running(slots, targets, err, 1)) return e;
         exact_steps_ = steps;
         int e = drive(act, mode, err);
         exact_steps_ = -1;
-        for (size_t i = 0; i < slots.size(); i++)
-            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].stop, &saved[i], sizeof(MathTree), cudaMemcpyHostToDevice, stream_));
-        std::vector<int32_t> st(act.size());
-        for (size_t i = 0; i < act.size(); i++)
-            CK(cudaMemcpyAsync(&st[i], &d_ctl_[act[i]->slot].status, 4, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaStreamSynchronize(stream_));
-        const int32_t idle = SIM_IDLE;
-        for (size_t i = 0; i < act.size(); i++) {
-            if (st[i] == SIM_DONE) { st[i] = SIM_IDLE; CK(cudaMemcpyAsync(&d_ctl_[act[i]->slot].status, &idle, 4, cudaMemcpyHostToDevice, stream_)); }
-            act[i]->status = st[i];
-        }
-        CK(cudaStreamSynchronize(stream_));
+        if (int e2 = end_fixed_steps(slots, err)) return e2;
+        if (int e2 = read_ctls(lo, hi, &cs, err)) return e2;
+        for (auto* r : act) r->status = cs[(size_t)(r->slot - lo)].status;
         return e;
     }
 
@@ -802,9 +978,13 @@ public:
         std::vector<int> slots;
         std::vector<int64_t> targets;
         std::vector<SimRec*> act;
+        if (rs.empty()) return 0;
+        int lo = INT32_MAX, hi = -1;
+        for (auto* r : rs) { lo = std::min(lo, r->slot); hi = std::max(hi, r->slot); }
+        std::vector<dev::Ctl> cs;
+        if (int e = read_ctls(lo, hi, &cs, err)) return e;
         for (auto* r : rs) {
-            dev::Ctl c;
-            if (int e = read_ctl(r->slot, &c, err)) return e;
+            const dev::Ctl& c = cs[(size_t)(r->slot - lo)];
             if (c.status != SIM_IDLE) continue;
             // StopConditionMet is checked before each step (VX3_SimulationManager.cu:62-64)
             if (r->w.desc.stop_formula.n > 0) {
@@ -890,23 +1070,35 @@ public:
     int pending() const override { return (int)(queue_.size() + active_.size()); }
 
     int poll(SimResult* out, int max, int chunk, std::string* err) override {
-        // admit while the HBM budget allows (first come, first served)
+        // admit while the HBM budget allows (first come, first served); the uploads of
+        // everything admitted now are finished together
+        std::vector<SimRec*> begun, admitted;
         while (!queue_.empty()) {
             SimRec* r = find(queue_.front());
             if (!r) { queue_.pop_front(); continue; }
             std::string e2;
-            int e = upload(r, &e2);
+            const bool fresh = !r->resident;
+            int e = fresh ? upload_begin(r, &e2) : 0;
             if (e == -2) {
-                if (active_.empty()) { *err = "simulation larger than the HBM budget"; return -2; }
+                if (active_.empty() && admitted.empty()) { *err = "simulation larger than the HBM budget"; return -2; }
                 break;
             }
-            if (e) { *err = e2; return e; }
+            if (e) { upload_finish(begun, err); *err = e2; return e; }
+            if (fresh) begun.push_back(r);
+            admitted.push_back(r);
             queue_.pop_front();
             r->start_s = now_s() - t0_;
-            std::vector<int> one{r->slot};
-            std::vector<int64_t> tg{r->horizon > 0 ? r->horizon : 1000000};
-            if (int e3 = set_running(one, tg, err)) return e3;
             active_.push_back(r->id);
+        }
+        if (int e = upload_finish(begun, err)) return e;
+        if (!admitted.empty()) {
+            std::vector<int> slots;
+            std::vector<int64_t> tg;
+            for (SimRec* r : admitted) {
+                slots.push_back(r->slot);
+                tg.push_back(r->horizon > 0 ? r->horizon : 1000000);
+            }
+            if (int e3 = set_running(slots, tg, err)) return e3;
             batch_dirty_ = true;
         }
         if (active_.empty()) return 0;
@@ -932,9 +1124,13 @@ public:
         CK(cudaGraphLaunch(graph_, stream_));
         timing_.launches += (int64_t)k * (any_collide_ ? 3 : 2);
         std::vector<int32_t> st(active_.size());
-        for (size_t i = 0; i < active_.size(); i++)
-            CK(cudaMemcpyAsync(&st[i], &d_ctl_[find(active_[i])->slot].status, 4, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaStreamSynchronize(stream_));
+        {
+            int lo = INT32_MAX, hi = -1;
+            for (int s : slots) { lo = std::min(lo, s); hi = std::max(hi, s); }
+            std::vector<dev::Ctl> cs;
+            if (int e = read_ctls(lo, hi, &cs, err)) return e;
+            for (size_t i = 0; i < active_.size(); i++) st[i] = cs[(size_t)(slots[i] - lo)].status;
+        }
         int nout = 0;
         std::vector<int64_t> still;
         for (size_t i = 0; i < active_.size(); i++) {
@@ -1015,6 +1211,54 @@ public:
             if (f3) for (int k = 0; k < 3; k++) f3[3 * (size_t)i + k] = sf[(size_t)k * nl + i];
             if (flags) flags[i] = fl[i];
         }
+        return 0;
+    }
+
+    int gather_states(const int64_t* ids, int n, double* pos3, double* q4, uint8_t* flags, std::string* err) override {
+        std::vector<int> slots((size_t)n);
+        std::vector<int64_t> offs((size_t)n);
+        int64_t total = 0;
+        for (int k = 0; k < n; k++) {
+            SimRec* r = find(ids[k]);
+            if (!r) { *err = "unknown simulation id"; return -6; }
+            if (!r->resident) if (int e = upload(r, err)) return e;
+            slots[k] = r->slot;
+            offs[k] = total;
+            total += r->w.nv;
+        }
+        if (total == 0) return 0;
+        const size_t b_pos = 24 * (size_t)total, b_q = 32 * (size_t)total, b_fl = (size_t)total;
+        const size_t b_idx = 4 * (size_t)n + 8 * (size_t)n;
+        const size_t need = b_pos + b_q + b_fl + 16 + b_idx + 16;
+        if (need > cap_gather_) {
+            CK(cudaStreamSynchronize(stream_));
+            cudaFree(d_gather_);
+            d_gather_ = nullptr;
+            cap_gather_ = 0;
+            CK(cudaMalloc(&d_gather_, need));
+            cap_gather_ = need;
+        }
+        if (int e = pinned(&rb_, need, err)) return e;
+        // the index tables go through the pinned buffer too
+        const size_t o_idx = (b_pos + b_q + b_fl + 15) & ~(size_t)15;
+        char* h = rb_.p;
+        memcpy(h + o_idx, offs.data(), 8 * (size_t)n);
+        memcpy(h + o_idx + 8 * (size_t)n, slots.data(), 4 * (size_t)n);
+        CK(cudaMemcpyAsync(d_gather_ + o_idx, h + o_idx, b_idx, cudaMemcpyHostToDevice, stream_));
+        double* dpos = (double*)d_gather_;
+        double* dq = (double*)(d_gather_ + b_pos);
+        uint8_t* dfl = (uint8_t*)(d_gather_ + b_pos + b_q);
+        const int64_t* doff = (const int64_t*)(d_gather_ + o_idx);
+        const int* dslot = (const int*)(d_gather_ + o_idx + 8 * (size_t)n);
+        for (int k0 = 0; k0 < n; k0 += 65535)
+            ks_.gather(stream_, d_sims_, dslot + k0, doff + k0, std::min(65535, n - k0), dpos, dq, dfl);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h, d_gather_, b_pos + b_q + b_fl, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaEventRecord(rb_.done, stream_));
+        CK(cudaEventSynchronize(rb_.done));
+        if (pos3) memcpy(pos3, h, b_pos);
+        if (q4) memcpy(q4, h + b_pos, b_q);
+        if (flags) memcpy(flags, h + b_pos + b_q, b_fl);
         return 0;
     }
 

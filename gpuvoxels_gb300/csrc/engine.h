@@ -72,6 +72,9 @@ public:
     virtual int result(int64_t id, SimResult* out, std::string* err) = 0;
     virtual int info(int64_t id, int* nv, int* nl, double* dt, double* t, int64_t* steps, int* status) = 0;
     virtual int voxel_state(int64_t id, double* d13, float* f4, int32_t* flags, std::string* err) = 0;
+    // Poses of many simulations in one device pass and one copy: pos3/q4/flags hold the
+    // simulations' voxels one after another in the order of ids (any pointer may be null).
+    virtual int gather_states(const int64_t* ids, int n, double* pos3, double* q4, uint8_t* flags, std::string* err) = 0;
     virtual int link_state(int64_t id, double* d9, float* f3, int32_t* flags, std::string* err) = 0;
     // Report extras of VXA Simulator/SavePositionOfAllVoxels: initial and current voxel positions
     // (x,y,z per voxel) and palette material ids (1-based); *save = the VXA flag (vectors untouched if 0).

@@ -57,7 +57,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         lvv = false;
     }
     d3 a1v;
-    bool wide1 = false, wide2 = false;      // branches taken, kept as the next step's ordering key
+    bool wide1 = false, acos1 = false, wide2 = false;   // branches taken, kept as the next step's ordering key
     if (small) {
         pos2.x -= restLen;
         a1v = D3(0, 0, 0);                  // ToRotationVector of the identity
@@ -65,7 +65,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         angle1 = q_from_angle_to_posx(angle1, pos2, &wide1);
         angle2 = qmul(angle1, angle2);
         pos2 = D3(sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z) - restLen, 0, 0);
-        a1v = q_to_rotvec(angle1, &wide1);
+        a1v = q_to_rotvec(angle1, &acos1);
     }
     const d3 a2v = q_to_rotvec(angle2, &wide2);
     st[l] = pos2.x; st[nl + l] = pos2.y; st[2 * nl + l] = pos2.z;
@@ -145,7 +145,8 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         fN = to_axis_orig(axis, fN); fP = to_axis_orig(axis, fP);
         mN = to_axis_orig(axis, mN); mP = to_axis_orig(axis, mP);
     }
-    S.lfl[l] = (uint8_t)((small ? LF_SMALL : 0) | (lvv ? LF_LVV : 0) | (wide1 ? LF_WIDE1 : 0) | (wide2 ? LF_WIDE2 : 0));
+    S.lfl[l] = (uint8_t)((small ? LF_SMALL : 0) | (lvv ? LF_LVV : 0) | (wide1 ? LF_WIDE1 : 0) | (wide2 ? LF_WIDE2 : 0) |
+                         (acos1 ? LF_ACOS1 : 0));
 
     // direction slots: the negative-end voxel sees this link in direction 2*axis,
     // the positive-end voxel in direction 2*axis+1 (CVX_Voxel::force, VX_Voxel.cpp:236-238)
@@ -171,7 +172,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
 // deterministic.  The order never changes results: every link writes only its own
 // state and its two direction slots, and voxel work is per voxel.
 constexpr int kOrderMax = 1024;   // elements per item that are reordered (larger items run in index order)
-constexpr int kOrderKeys = 8;
+constexpr int kOrderKeys = 10;
 
 // perm[0..n) = element indices grouped by key(j) in increasing key order; wc holds
 // kOrderKeys x 8 warp counts.  Every thread of the block must call it.
@@ -221,13 +222,16 @@ __device__ __forceinline__ void order_by_key(int n, KeyFn key, int* perm, int* w
     }
 }
 
-// Link key: small-angle mode, then within each mode which rotation branches were taken.
+// Link key: small-angle mode, then within each mode which rotation branches were taken
+// (small links: angle2's rotation-vector branch; large links: that, angle1's, and
+// FromAngleToPosX's).  10 groups.
 struct LinkKey {
     const uint8_t* lfl;
     int begin;
     __device__ int operator()(int j) const {
         const uint8_t f = lfl[begin + j];
-        return ((f & LF_SMALL) ? 4 : 0) | ((f & LF_WIDE1) ? 2 : 0) | ((f & LF_WIDE2) ? 1 : 0);
+        if (f & LF_SMALL) return 8 | ((f & LF_WIDE2) ? 1 : 0);
+        return ((f & LF_WIDE1) ? 4 : 0) | ((f & LF_ACOS1) ? 2 : 0) | ((f & LF_WIDE2) ? 1 : 0);
     }
 };
 
@@ -635,7 +639,7 @@ __device__ __noinline__ void sim_control(Ctl& c, bool div, double t_next, int64_
         }
     }
     bool stop = c.target > 0 && stepno >= c.target;
-    if (c.stop.n > 0) {
+    if (c.stop.n > 0 && !c.no_stop) {
         MathVars mv;
         mv.x = c.com[0]; mv.y = c.com[1]; mv.z = c.com[2]; mv.hit = 0; mv.t = c.t; mv.angle = c.recent_angle;
         mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = nv;
@@ -712,7 +716,11 @@ __global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim
 
 // Stable time step (CVoxelyze::recommendedTimeStep, Voxelyze3/src/old/Voxelyze.cpp:286-311,
 // with CVX_Link::axialStiffness, VX_Link.cpp:251-259): a warp-shuffle max over links.
-__global__ void k_dt(const Sim* __restrict__ sims, Ctl* ctl, int sim) {
+// The three set-up kernels run for a whole list of newly uploaded simulations at once:
+// blockIdx.y picks the simulation (slots[y]), the blocks along x stride over its elements.
+__global__ void k_dt(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
+    if ((int)blockIdx.y >= n) return;
+    const int sim = slots[blockIdx.y];
     const Sim& S = sims[sim];
     float best = 0.0f;
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < S.nl; l += gridDim.x * blockDim.x) {
@@ -735,8 +743,10 @@ __global__ void k_dt(const Sim* __restrict__ sims, Ctl* ctl, int sim) {
     if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(&ctl[sim].maxf2_bits, __float_as_uint(best));
 }
 
-__global__ void k_init_temp(const Sim* __restrict__ sims, int sim, float initial) {
-    const Sim& S = sims[sim];
+__global__ void k_init_temp(const Sim* __restrict__ sims, const int* __restrict__ slots, const float* __restrict__ initials, int n) {
+    if ((int)blockIdx.y >= n) return;
+    const Sim& S = sims[slots[blockIdx.y]];
+    const float initial = initials[blockIdx.y];
     const float two_pi = 2 * 3.1415926f;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < S.nv; v += gridDim.x * blockDim.x) {
         if ((S.flags & SF_VARY) && !fp64i::gt(S.vm[S.vmat[v]].thermalOn, 0.0)) {
@@ -749,12 +759,32 @@ __global__ void k_init_temp(const Sim* __restrict__ sims, int sim, float initial
     }
 }
 
-__global__ void k_hash_build(const Sim* __restrict__ sims, Ctl* ctl, int sim) {
+__global__ void k_hash_build(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
+    if ((int)blockIdx.y >= n) return;
+    const int sim = slots[blockIdx.y];
     const Sim& S = sims[sim];
+    if (!(S.flags & SF_COLLIDE) || S.nsurf == 0) return;
     int* head = S.hash_head + (size_t)ctl[sim].hash_parity * S.hash_size;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nsurf; i += gridDim.x * blockDim.x) {
         const int v = S.surf[i];
         hash_insert(S, v, D3(S.px[v], S.py[v], S.pz[v]), S.temp[v], head);
+    }
+}
+
+// Poses of many simulations packed for one device-to-host copy: blockIdx.y picks the
+// simulation, the blocks along x stride over its voxels.  Flags are the voxel flag word
+// shifted to the reference's CVX_Voxel bit order (static friction first).
+__global__ void k_gather(const Sim* __restrict__ sims, const int* __restrict__ slot, const int64_t* __restrict__ off, int n, double* pos3,
+                         double* q4, uint8_t* flags) {
+    const int k = blockIdx.y;
+    if (k >= n) return;
+    const Sim& S = sims[slot[k]];
+    const int64_t o = off[k];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < S.nv; v += gridDim.x * blockDim.x) {
+        const int64_t i = o + v;
+        pos3[3 * i] = S.px[v]; pos3[3 * i + 1] = S.py[v]; pos3[3 * i + 2] = S.pz[v];
+        q4[4 * i] = S.qw[v]; q4[4 * i + 1] = S.qx[v]; q4[4 * i + 2] = S.qy[v]; q4[4 * i + 3] = S.qz[v];
+        flags[i] = (uint8_t)(S.vfl[v] >> 6);
     }
 }
 
@@ -786,12 +816,23 @@ inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, 
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk, double* p) {
     k_voxels<<<g, b, 0, s>>>(sims, ctl, it, n, tk, p);
 }
-inline void l_dt(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, int sim) { k_dt<<<g, 256, 0, s>>>(sims, ctl, sim); }
-inline void l_init_temp(int g, cudaStream_t s, const Sim* sims, int sim, float t0) { k_init_temp<<<g, 256, 0, s>>>(sims, sim, t0); }
-inline void l_hash_build(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, int sim) { k_hash_build<<<g, 256, 0, s>>>(sims, ctl, sim); }
+inline void l_dt(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
+    for (int k0 = 0; k0 < n; k0 += 65535) k_dt<<<dim3(g, (unsigned)std::min(65535, n - k0)), 256, 0, s>>>(sims, ctl, slots + k0, n - k0);
+}
+inline void l_init_temp(int g, cudaStream_t s, const Sim* sims, const int* slots, const float* t0, int n) {
+    for (int k0 = 0; k0 < n; k0 += 65535)
+        k_init_temp<<<dim3(g, (unsigned)std::min(65535, n - k0)), 256, 0, s>>>(sims, slots + k0, t0 + k0, n - k0);
+}
+inline void l_hash_build(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
+    for (int k0 = 0; k0 < n; k0 += 65535)
+        k_hash_build<<<dim3(g, (unsigned)std::min(65535, n - k0)), 256, 0, s>>>(sims, ctl, slots + k0, n - k0);
+}
 inline void l_com(cudaStream_t s, const Sim* sims, int sim, double* out4) { k_com<<<1, 256, 0, s>>>(sims, sim, out4); }
+inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int64_t* off, int n, double* pos3, double* q4, uint8_t* fl) {
+    if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
+}
 inline KernelSet make_kernelset(const char* name) {
-    return KernelSet{name, l_links, l_contacts, l_voxels, l_dt, l_init_temp, l_hash_build, l_com};
+    return KernelSet{name, l_links, l_contacts, l_voxels, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

@@ -13,10 +13,15 @@ struct KernelSet {
     void (*contacts)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
     void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets,
                    double* partials);
-    void (*dt)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, int sim);
-    void (*init_temp)(int grid, cudaStream_t s, const dev::Sim* sims, int sim, float initial);
-    void (*hash_build)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, int sim);
+    // set-up of n newly uploaded simulations (device slot list), grid = blocks per simulation
+    void (*dt)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
+    void (*init_temp)(int grid, cudaStream_t s, const dev::Sim* sims, const int* slots, const float* initial, int n);
+    void (*hash_build)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
     void (*com)(cudaStream_t s, const dev::Sim* sims, int sim, double* out4);
+    // Packs position, orientation and the reference-order flag byte of the voxels of
+    // n simulations (slot[k], output offset off[k]) into pos3 / q4 / flags (one launch).
+    void (*gather)(cudaStream_t s, const dev::Sim* sims, const int* slot, const int64_t* off, int n, double* pos3, double* q4,
+                   uint8_t* flags);
 };
 
 KernelSet kernelset_exact();   // every multiply and add rounded separately (the reference's CPU rounding)

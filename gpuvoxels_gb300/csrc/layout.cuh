@@ -22,8 +22,9 @@ constexpr uint32_t VF_MEASURED = 1u << 9;
 // link flag bits
 constexpr uint8_t LF_SMALL = 1;           // small-angle mode
 constexpr uint8_t LF_LVV = 2;             // LOCAL_VELOCITY_VALID
-constexpr uint8_t LF_WIDE1 = 4;           // last step: angle1 took the general (acos/sincos) branches
+constexpr uint8_t LF_WIDE1 = 4;           // last step: angle1 came from FromAngleToPosX's general (acos/sincos) branch
 constexpr uint8_t LF_WIDE2 = 8;           // last step: angle2's rotation vector took the acos branch
+constexpr uint8_t LF_ACOS1 = 16;          // last step: angle1's rotation vector took the acos branch
 constexpr uint32_t VF_FLOORC = 1u << 10;  // last step: the voxel touched the floor
 
 // sim flag bits
@@ -116,6 +117,8 @@ struct Ctl {
     int32_t done_items, n_vox_items, item_begin, angle_samples;
     uint32_t maxf2_bits;
     int32_t hash_parity;
+    int32_t no_stop;            // set while vx3_step advances a fixed count: the stop formula is not applied
+    int32_t pad_ctl;
     double com[3], com_hist[2][3];
     double recent_angle;
     MathTree stop;

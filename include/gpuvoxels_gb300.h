@@ -121,6 +121,11 @@ int vx3_sim_info_get(vx3_ctx* ctx, vx3_sim_id id, vx3_sim_info* out);
 /* Voxel state in the reference's CVX_Voxel member layout (Voxelyze3/src/old/VX_Voxel.h:166-182):
  * pos[3*nv], orient[4*nv] (w,x,y,z) and flags[nv]; any pointer may be NULL. */
 int vx3_get_state(vx3_ctx* ctx, vx3_sim_id id, double* pos, double* orient, uint8_t* flags);
+/* The same for a whole generation in one device pass and one copy (the read-back loop of
+ * VX3_SimulationManager::collectResults, VX3_SimulationManager.cu:416-455): the voxels of
+ * ids[0], ids[1], ... follow one another in pos / orient / flags, each simulation's block
+ * sized by its num_voxel.  Any output pointer may be NULL. */
+int vx3_get_states(vx3_ctx* ctx, const vx3_sim_id* ids, int n, double* pos, double* orient, uint8_t* flags);
 /* Full voxel state: d13 = pos3 linMom3 orient4 angMom3, f4 = temperature, poisson strain3, flags. */
 int vx3_get_voxel_state(vx3_ctx* ctx, vx3_sim_id id, double* d13, float* f4, int32_t* flags);
 /* Link state (CVX_Link, VX_Link.h:68-99): d9 = pos2 angle1v angle2v, f3 = strain maxStrain strainOffset, flags. */

@@ -39,6 +39,25 @@ def test_load_many_matches_one_by_one(ctx):
             ctx.free(s)
 
 
+def test_get_states_equals_per_simulation_readback(ctx):
+    """vx3_get_states (one gather kernel, one copy) returns exactly what vx3_get_state
+    returns for each simulation, in id order, including for a simulation never stepped."""
+    cs = synth.config1_batch(4, seed=31)
+    ids = [ctx.load_vxa(c.vxa, name=f"g{i}") for i, c in enumerate(cs)]
+    try:
+        ctx.step(ids[:3], 60, g.BATCHED)
+        order = [ids[2], ids[0], ids[3], ids[1]]
+        pos, q, fl, off = ctx.get_states(order)
+        for k, i in enumerate(order):
+            p1, q1, f1 = ctx.get_state(i)
+            assert np.array_equal(_bits(pos[off[k]:off[k + 1]]), _bits(p1))
+            assert np.array_equal(_bits(q[off[k]:off[k + 1]]), _bits(q1))
+            assert np.array_equal(fl[off[k]:off[k + 1]], f1)
+    finally:
+        for s in ids:
+            ctx.free(s)
+
+
 def test_plain_and_batched_are_bit_identical(ctx):
     cs = synth.config1_batch(4, seed=9)
     a = [ctx.load_vxa(c.vxa, name=f"p{i}") for i, c in enumerate(cs)]

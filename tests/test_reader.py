@@ -110,6 +110,17 @@ def test_formula_evaluation():
     "<Z_Voxels>1</Z_Voxels><Data><Layer><![CDATA[1]]></Layer></Data></Structure></VXC></VXA>",   # short layer
     "<VXA><VXC><Palette/><Structure Compression=\"ASCII_READABLE\"><X_Voxels>1</X_Voxels><Y_Voxels>1</Y_Voxels>"
     "<Z_Voxels>1</Z_Voxels><Data><Layer><![CDATA[3]]></Layer></Data></Structure></VXC></VXA>",   # missing material
+    "<VXA><VXC><Palette><Material><Mechanical><Elastic_Mod>1e6</Elastic_Mod></Mechanical></Material></Palette>"
+    "<Structure Compression=\"ASCII_READABLE\"><X_Voxels>2</X_Voxels><Y_Voxels>1</Y_Voxels><Z_Voxels>1</Z_Voxels>"
+    "<Data><Layer><![CDATA[00]]></Layer></Data></Structure></VXC></VXA>",   # no voxels (the reference aborts such a simulation)
+    "<VXA><Environment><Boundary_Conditions><NumBCs>1</NumBCs><FRegion><PrimType>3</PrimType></FRegion></Boundary_Conditions>"
+    "</Environment><VXC><Palette><Material><Mechanical><Elastic_Mod>1e6</Elastic_Mod></Mechanical></Material></Palette>"
+    "<Structure Compression=\"ASCII_READABLE\"><X_Voxels>1</X_Voxels><Y_Voxels>1</Y_Voxels><Z_Voxels>1</Z_Voxels>"
+    "<Data><Layer><![CDATA[1]]></Layer></Data></Structure></VXC></VXA>",   # mesh boundary-condition region
+    "<VXA><Environment><Boundary_Conditions><NumBCs>2</NumBCs><FRegion><PrimType>0</PrimType></FRegion></Boundary_Conditions>"
+    "</Environment><VXC><Palette><Material><Mechanical><Elastic_Mod>1e6</Elastic_Mod></Mechanical></Material></Palette>"
+    "<Structure Compression=\"ASCII_READABLE\"><X_Voxels>1</X_Voxels><Y_Voxels>1</Y_Voxels><Z_Voxels>1</Z_Voxels>"
+    "<Data><Layer><![CDATA[1]]></Layer></Data></Structure></VXC></VXA>",   # fewer regions than NumBCs
 ])
 def test_reader_rejects_malformed_worlds(bad):
     with pytest.raises(g.VX3Error, match="VX3_E_PARSE"):
