@@ -35,7 +35,8 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
-           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states"]
+           "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states",
+           "vx3_get_extras"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -95,6 +96,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_record_history": (I, [P, I64, S]),
         "vx3_inspect_externals": (I, [S, S, P, P, P]),
         "vx3_get_states": (I, [P, P, I, P, P, P]),
+        "vx3_get_extras": (I, [P, I64, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -266,6 +268,16 @@ class Context:
         self._check(self.L.vx3_get_link_state(self.h, sim, _p(d), _p(f), _p(fl)))
         return dict(pos2=d[:, 0:3], angle1v=d[:, 3:6], angle2v=d[:, 6:9], strain=f[:, 0], maxStrain=f[:, 1],
                     strainOffset=f[:, 2], smallAngle=fl & 1, flags=fl)
+
+    def extras(self, sim: int) -> dict:
+        """VX3 extras: targetCloseness, numClosePairs, collisionCount, recentAngle and the per-voxel
+        signal state (localSignal, localSignaldt, inactiveUntil, pending value and time, next pulse)."""
+        nv = self.info(sim).num_voxel
+        m = np.zeros(4); g = np.zeros((nv, 6))
+        self._check(self.L.vx3_get_extras(self.h, sim, _p(m), _p(g)))
+        return dict(targetCloseness=m[0], numClosePairs=int(m[1]), collisionCount=int(m[2]), recentAngle=m[3],
+                    localSignal=g[:, 0], localSignalDt=g[:, 1], inactiveUntil=g[:, 2], signalValue=g[:, 3],
+                    signalTime=g[:, 4], pacemakerNextPulse=g[:, 5])
 
     def get_state(self, sim: int):
         nv = self.info(sim).num_voxel

@@ -199,7 +199,14 @@ int history_after_chunk(vx3_ctx* c, const vx3_sim_id* ids, int n) {
         std::vector<double> ld(9 * (size_t)std::max(nl, 1));
         if (nl > 0)
             if (int e = c->eng->link_state(ids[i], ld.data(), lsf.data(), lf.data(), &err)) return fail(c, e, err);
-        const std::string rec = gvx::history_record(*w, j, t, (float)dt, d13.data(), f4.data(), lsf.data());
+        std::vector<double> sig;
+        if (w->desc.enable_signals) {
+            sig.resize(6 * (size_t)nv);
+            if (int e = c->eng->extras(ids[i], nullptr, sig.data(), &err)) return fail(c, e, err);
+            for (int v = 0; v < nv; v++) sig[v] = sig[6 * (size_t)v];   // localSignal of each voxel
+        }
+        const std::string rec = gvx::history_record(*w, j, t, (float)dt, d13.data(), f4.data(), lsf.data(), vf.data(),
+                                                    nl > 0 ? lf.data() : nullptr, sig.empty() ? nullptr : sig.data());
         fwrite(rec.data(), 1, rec.size(), h.f);
         fflush(h.f);
         h.last_j = j;
@@ -358,6 +365,13 @@ int vx3_get_link_state(vx3_ctx* c, vx3_sim_id id, double* d9, float* f3, int32_t
     if (!c) return VX3_E_ARG;
     std::string err;
     int e = c->eng->link_state(id, d9, f3, flags, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_get_extras(vx3_ctx* c, vx3_sim_id id, double* measures4, double* signals6) {
+    if (!c) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->extras(id, measures4, signals6, &err);
     return e ? fail(c, e, err) : VX3_OK;
 }
 

@@ -99,6 +99,7 @@ struct SimRec {
     float dt = 0, optdt = 0;
     int cycle_step = 0;
     double init_com[3] = {0, 0, 0};
+    std::vector<double> final_init_pos;   // initial positions reset by the secondary experiment (else empty)
     int num_measured = 0;
     int64_t horizon = 0;
     double submit_s = 0, start_s = 0, finish_s = 0;
@@ -144,6 +145,7 @@ public:
     std::vector<int> batch_slots_;
     int n_link_items_ = 0, n_contact_items_ = 0, n_vox_items_ = 0;
     bool any_collide_ = false;
+    bool any_signals_ = false;
     cudaGraphExec_t graph_ = nullptr;
     int graph_len_ = 0;
     bool batch_dirty_ = true;
@@ -259,15 +261,32 @@ public:
     }
     int precision() const override { return ks_.name[0] == 'f' ? 1 : 0; }
 
+    // VX3 extras that change the topology during the run (link detachment, material
+    // removal): the contact search then lists every voxel and skips interior ones.
+    static bool removes_materials(const SimDesc& d) {
+        if (!d.secondary_experiment) return false;
+        for (auto& m : d.mats) if (m.remove_after > 0) return true;
+        return false;
+    }
+    static bool dynamic_surface(const SimDesc& d) { return d.enable_detach || removes_materials(d); }
+    static int contact_list_size(const SimWorld& w) { return dynamic_surface(w.desc) ? w.nv : w.surface_count; }
+    static int target_count(const SimWorld& w) {
+        int n = 0;
+        for (int i = 0; i < w.nv; i++) n += w.desc.mats[w.desc.voxels[4 * i + 3]].is_target ? 1 : 0;
+        return n;
+    }
+
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
         size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos, cilia, ffield;
+        size_t shift, sig, vlink, targets, init_pos;
         int hash_size;
     };
     static void compute_layout(const SimWorld& w, Layout* L, Offs* o) {
         Offs t{};
         const size_t nv = w.nv, nl = w.nl;
         const bool col = w.desc.collisions;
+        const SimDesc& d = w.desc;
         t.vm = L->add(sizeof(dev::VMat) * w.vmats.size());
         t.lm = L->add(sizeof(dev::LMat) * std::max<size_t>(1, w.lmats.size()));
         t.ext = L->add(sizeof(dev::Ext) * std::max<size_t>(1, w.desc.externals.size()));
@@ -293,7 +312,7 @@ public:
         t.lfl = L->add(std::max<size_t>(1, nl));
         t.ijk = L->add(2 * 3 * nv);
         if (col) {
-            size_t ns = std::max(1, w.surface_count);
+            size_t ns = std::max(1, contact_list_size(w));
             int hs = 1;
             while (hs < 2 * (int)ns) hs <<= 1;
             t.hash_size = hs;
@@ -307,6 +326,11 @@ public:
         }
         if (w.desc.enable_cilia) t.cilia = L->add(8 * 3 * nv);
         if (w.desc.has_force_field) t.ffield = L->add(sizeof(MathTree) * 3);
+        if (d.enable_signals && d.enable_cilia && !d.shift_cilia.empty()) t.shift = L->add(8 * 3 * nv);
+        if (d.enable_signals) t.sig = L->add(8 * dev::SG_FIELDS * nv);
+        if (d.enable_signals || removes_materials(d)) t.vlink = L->add(4 * 6 * nv);
+        if (int nt = target_count(w)) t.targets = L->add(4 * (size_t)nt);
+        if (d.secondary_experiment) t.init_pos = L->add(8 * 3 * nv);
         if (o) *o = t;
     }
 
@@ -465,6 +489,12 @@ public:
             x.cilia = pm.cilia;
             x.ciliaOn = pm.cilia_on_after;
             x.thermalOn = pm.thermal_on_after;
+            x.vx3 = (pm.is_target ? dev::VM_TARGET : 0) | (pm.is_pacemaker ? dev::VM_PACEMAKER : 0) | (pm.fixed ? dev::VM_FIXED : 0);
+            x.pmPeriod = pm.pacemaker_period;
+            x.sigDecay = pm.signal_decay;
+            x.sigDelay = pm.signal_delay;
+            x.sigInactive = pm.inactive_period;
+            x.removeAfter = pm.remove_after;
         }
         dev::LMat* lm = (dev::LMat*)P(o.lm);
         for (size_t i = 0; i < w.lmats.size(); i++) {
@@ -536,11 +566,36 @@ public:
             flags |= dev::SF_FFIELD;
             memcpy(P(o.ffield), w.desc.force_field, sizeof(MathTree) * 3);
         }
+        const SimDesc& dd = w.desc;
+        if (dd.enable_signals) {
+            flags |= dev::SF_SIGNALS;
+            if (dd.enable_cilia && !dd.shift_cilia.empty()) {
+                double* c = (double*)P(o.shift);   // 3 blocks of nv
+                for (size_t i = 0; i < nv && 3 * i + 2 < dd.shift_cilia.size(); i++)
+                    for (int k = 0; k < 3; k++) c[k * nv + i] = dd.shift_cilia[3 * i + k];
+            }
+        }
+        if (dd.enable_signals || removes_materials(dd)) memcpy(P(o.vlink), w.vox_links.data(), 4 * 6 * nv);
+        const int n_targets = target_count(w);
+        if (n_targets) {
+            flags |= dev::SF_TARGETS;
+            int32_t* tg = (int32_t*)P(o.targets);
+            int k = 0;
+            for (size_t i = 0; i < nv; i++) if (dd.mats[dd.voxels[4 * i + 3]].is_target) tg[k++] = (int32_t)i;
+        }
+        if (dd.enable_detach) flags |= dev::SF_DETACH;
+        if (dd.secondary_experiment) {
+            flags |= dev::SF_REMOVE;
+            double* ip = (double*)P(o.init_pos);
+            for (size_t i = 0; i < nv; i++) { ip[i] = px[i]; ip[nv + i] = py[i]; ip[2 * nv + i] = pz[i]; }
+        }
+        for (auto& pm : dd.mats) if (pm.fixed) flags |= dev::SF_FIXEDMAT;
         double max_bsa = 0;
         if (w.desc.collisions) {
             int32_t* surf = (int32_t*)P(o.surf);
             int k = 0;
-            for (size_t i = 0; i < nv; i++) if (!w.vox_interior[i]) surf[k++] = (int32_t)i;
+            const bool all = dynamic_surface(w.desc);
+            for (size_t i = 0; i < nv; i++) if (all || !w.vox_interior[i]) surf[k++] = (int32_t)i;
             std::vector<uint32_t> masks = reach_masks(w, 5, dev::kReachWords);
             memcpy(P(o.reach), masks.data(), 4 * masks.size());
             memset(P(o.hhead), 0xFF, 4 * 2 * (size_t)o.hash_size);
@@ -550,7 +605,7 @@ public:
         }
         dev::Sim& S = r->dsim;
         S = dev::Sim{};
-        S.nv = (int)nv; S.nl = (int)nl; S.nsurf = w.surface_count; S.flags = flags;
+        S.nv = (int)nv; S.nl = (int)nl; S.nsurf = contact_list_size(w); S.flags = flags;
         S.temp_amp = w.desc.temp_amplitude; S.temp_period = w.desc.temp_period;
         S.cell_size = std::max(1e-9, 2 * 0.625 * max_bsa * 1.01);
         S.hash_size = o.hash_size > 0 ? o.hash_size : 1;
@@ -577,6 +632,16 @@ public:
         }
         if (w.desc.enable_cilia) S.cilia = (const double*)D(o.cilia);
         if (w.desc.has_force_field) S.ffield = (const MathTree*)D(o.ffield);
+        if (dd.enable_signals) {
+            S.sig = (double*)D(o.sig);
+            if (dd.enable_cilia && !dd.shift_cilia.empty()) S.shift_cilia = (const double*)D(o.shift);
+        }
+        if (dd.enable_signals || removes_materials(dd)) S.vlink = (const int32_t*)D(o.vlink);
+        if (n_targets) { S.targets = (const int32_t*)D(o.targets); S.n_targets = n_targets; }
+        S.close_r = dd.max_dist_pairs * dd.vox_size;   // MaxDistInVoxelLengthsToCountAsPair * voxSize
+        S.n_mats = (int)w.vmats.size();
+        S.reinit_after = dd.reinit_initial_after;
+        if (dd.secondary_experiment) S.init_pos = (double*)D(o.init_pos);
         CK(cudaMemcpyAsync(base, hp, L.total, cudaMemcpyHostToDevice, stream_));
         if (stage) CK(cudaEventRecord(stage->done, stream_));
         // the descriptor and control block go to the device with the others in upload_finish
@@ -585,6 +650,8 @@ public:
         c.status = SIM_IDLE;
         c.stop = w.desc.stop_formula;
         c.hash_parity = 0;
+        // currentCenterOfMass starts as the initial one (VX3_SimulationManager.cu:54-55)
+        for (int k = 0; k < 3; k++) c.com[k] = c.init_com[k] = r->init_com[k];
         r->pending_ctl = c;
         return 0;
     }
@@ -695,7 +762,7 @@ public:
     int build_items(const std::vector<int>& slots, std::string* err) {
         std::vector<dev::Item> items;
         n_link_items_ = n_contact_items_ = n_vox_items_ = 0;
-        any_collide_ = false;
+        any_collide_ = any_signals_ = false;
         for (int s : slots) {
             SimRec* r = slot_owner_[s];
             for (int b = 0; b < r->w.nl; b += items_links_) items.push_back({s, b, std::min(r->w.nl, b + items_links_), 0});
@@ -703,10 +770,12 @@ public:
         n_link_items_ = (int)items.size();
         for (int s : slots) {
             SimRec* r = slot_owner_[s];
-            if (!r->w.desc.collisions || r->w.surface_count == 0) continue;
+            if (r->w.desc.enable_signals) any_signals_ = true;
+            const int ns = contact_list_size(r->w);
+            if (!r->w.desc.collisions || ns == 0) continue;
             any_collide_ = true;
             const int chunk = 128;
-            for (int b = 0; b < r->w.surface_count; b += chunk) items.push_back({s, b, std::min(r->w.surface_count, b + chunk), 0});
+            for (int b = 0; b < ns; b += chunk) items.push_back({s, b, std::min(ns, b + chunk), 0});
         }
         n_contact_items_ = (int)items.size() - n_link_items_;
         std::vector<std::pair<int, int>> ctl_items;   // slot -> (begin, count)
@@ -730,8 +799,10 @@ public:
         for (size_t i = 0; i < slots.size(); i++) {
             int vals[2] = {ctl_items[i].second, ctl_items[i].first};   // n_vox_items, item_begin
             CK(cudaMemcpyAsync(&d_ctl_[slots[i]].n_vox_items, vals, sizeof(vals), cudaMemcpyHostToDevice, stream_));
-            int zero = 0;
+            static const int zero = 0;
             CK(cudaMemcpyAsync(&d_ctl_[slots[i]].done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+            if (slot_owner_[slots[i]]->w.desc.enable_signals)
+                CK(cudaMemcpyAsync(&d_ctl_[slots[i]].sig_done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
         }
         CK(cudaMemsetAsync(d_tickets_, 0, 4 * sizeof(int), stream_));
         return 0;
@@ -741,6 +812,8 @@ public:
         int per_sm = block >= 256 ? 4 : 8;
         return std::max(1, std::min(n_items, sm_count_ * per_sm));
     }
+
+    int launches_per_step() const { return 2 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0); }
 
     void launch_step(cudaStream_t st, bool prof) {
         const dev::Item* li = d_items_;
@@ -753,6 +826,7 @@ public:
         if (prof) cudaEventRecord(evk_[2], st);
         ks_.voxels(grid_for(n_vox_items_, block_voxels_), block_voxels_, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_,
                    d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
+        if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
         if (prof) cudaEventRecord(evk_[3], st);
     }
 
@@ -836,11 +910,11 @@ public:
                 std::vector<int> one{rs[i]->slot};
                 if (int e = build_items(one, err)) return e;
                 if (exact_steps_ >= 0) {
-                    for (int64_t k = 0; k < exact_steps_; k++) { launch_step(stream_, false); timing_.launches += any_collide_ ? 3 : 2; }
+                    for (int64_t k = 0; k < exact_steps_; k++) { launch_step(stream_, false); timing_.launches += launches_per_step(); }
                     continue;
                 }
                 for (;;) {
-                    for (int k = 0; k < 16; k++) { launch_step(stream_, false); timing_.launches += any_collide_ ? 3 : 2; }
+                    for (int k = 0; k < 16; k++) { launch_step(stream_, false); timing_.launches += launches_per_step(); }
                     dev::Ctl c;
                     if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
                     if (c.status != SIM_RUNNING) break;
@@ -865,7 +939,7 @@ public:
                 cudaGraphDestroy(g);
                 graph_len_ = graph_steps_;
             }
-            const int per_step = any_collide_ ? 3 : 2;
+            const int per_step = launches_per_step();
             if (exact_steps_ >= 0) {
                 // a known step count: whole graphs, then single steps for the remainder, no polling
                 int64_t left = exact_steps_;
@@ -1028,27 +1102,40 @@ public:
         R.steps = c.steps;
         R.current_time = c.t;
         R.vox_size = r->w.desc.vox_size;
-        for (int k = 0; k < 3; k++) R.initial_com[k] = r->init_com[k];
+        // initial centre of mass: the host's, or the one the secondary experiment reset it to
+        for (int k = 0; k < 3; k++) R.initial_com[k] = c.reinit_done ? c.init_com[k] : r->init_com[k];
         if (int e = com(r, R.current_com, err)) return e;
+        R.num_close_pairs = c.num_close_pairs;
         MathVars mv{R.current_com[0] - R.initial_com[0], R.current_com[1] - R.initial_com[1], R.current_com[2] - R.initial_com[2],
-                    0, c.t, c.recent_angle, 0, 0, r->w.nv};
+                    (double)c.hit_count, c.t, c.recent_angle, c.closeness, c.num_close_pairs, r->w.nv};
         R.fitness = mathtree_eval(r->w.desc.fitness, mv);
-        // total distance travelled by measured voxels (VX3_SimulationManager.cu:442-452)
-        std::vector<double> p(3 * (size_t)r->w.nv);
-        CK(cudaMemcpyAsync(p.data(), r->dsim.px, 8 * r->w.nv, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(p.data() + r->w.nv, r->dsim.py, 8 * r->w.nv, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(p.data() + 2 * (size_t)r->w.nv, r->dsim.pz, 8 * r->w.nv, cudaMemcpyDeviceToHost, stream_));
+        // total distance travelled by measured voxels from their initial positions
+        // (VX3_SimulationManager.cu:442-452)
+        const size_t nv = r->w.nv;
+        std::vector<double> p(3 * nv), ip;
+        CK(cudaMemcpyAsync(p.data(), r->dsim.px, 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(p.data() + nv, r->dsim.py, 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(p.data() + 2 * nv, r->dsim.pz, 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        if (c.reinit_done) {
+            ip.resize(3 * nv);
+            CK(cudaMemcpyAsync(ip.data(), r->dsim.init_pos, 8 * 3 * nv, cudaMemcpyDeviceToHost, stream_));
+        }
         CK(cudaStreamSynchronize(stream_));
         double tot = 0;
-        for (int i = 0; i < r->w.nv; i++) {
+        for (size_t i = 0; i < nv; i++) {
             if (!r->w.vmats[r->w.desc.voxels[4 * i + 3]].is_measured) continue;
             double nom = r->w.vmats[r->w.desc.voxels[4 * i + 3]].nom;
-            double dx = p[i] - r->w.desc.voxels[4 * i] * nom, dy = p[r->w.nv + i] - r->w.desc.voxels[4 * i + 1] * nom,
-                   dz = p[2 * (size_t)r->w.nv + i] - r->w.desc.voxels[4 * i + 2] * nom;
+            const double ix = ip.empty() ? r->w.desc.voxels[4 * i] * nom : ip[i];
+            const double iy = ip.empty() ? r->w.desc.voxels[4 * i + 1] * nom : ip[nv + i];
+            const double iz = ip.empty() ? r->w.desc.voxels[4 * i + 2] * nom : ip[2 * nv + i];
+            double dx = p[i] - ix, dy = p[nv + i] - iy, dz = p[2 * nv + i] - iz;
             tot += sqrt(dx * dx + dy * dy + dz * dz);
         }
         R.total_distance = tot;
-        if (r->w.desc.save_all_positions) r->final_pos = std::move(p);   // kept for the report's pos field
+        if (r->w.desc.save_all_positions) {   // kept for the report's pos and init_pos fields
+            r->final_pos = std::move(p);
+            r->final_init_pos = std::move(ip);
+        }
         R.submit_s = r->submit_s;
         R.start_s = r->start_s;
         r->finish_s = now_s() - t0_;
@@ -1122,7 +1209,7 @@ public:
             graph_len_ = k;
         }
         CK(cudaGraphLaunch(graph_, stream_));
-        timing_.launches += (int64_t)k * (any_collide_ ? 3 : 2);
+        timing_.launches += (int64_t)k * (launches_per_step());
         std::vector<int32_t> st(active_.size());
         {
             int lo = INT32_MAX, hi = -1;
@@ -1189,6 +1276,27 @@ public:
             if (d13) for (int k = 0; k < 13; k++) d13[13 * (size_t)i + k] = buf[(size_t)k * nv + i];
             if (f4) { f4[4 * (size_t)i] = tb[i]; for (int k = 0; k < 3; k++) f4[4 * (size_t)i + 1 + k] = ps[(size_t)k * nv + i]; }
             if (flags) flags[i] = (int32_t)fl[i];
+        }
+        return 0;
+    }
+
+    int extras(int64_t id, double* measures4, double* sig6, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        if (!r->resident) if (int e = upload(r, err)) return e;
+        const size_t nv = r->w.nv;
+        dev::Ctl c;
+        if (int e = read_ctl(r->slot, &c, err)) return e;
+        if (measures4) {
+            measures4[0] = c.closeness; measures4[1] = c.num_close_pairs; measures4[2] = c.hit_count; measures4[3] = c.recent_angle;
+        }
+        if (sig6) {
+            if (!r->dsim.sig) { std::fill(sig6, sig6 + 6 * nv, 0.0); return 0; }
+            std::vector<double> g(6 * nv);
+            CK(cudaMemcpyAsync(g.data(), r->dsim.sig, 8 * 6 * nv, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+            for (size_t i = 0; i < nv; i++)
+                for (int k = 0; k < 6; k++) sig6[6 * i + k] = g[(size_t)k * nv + i];
         }
         return 0;
     }
@@ -1296,7 +1404,8 @@ public:
             const int mi = r->w.desc.voxels[4 * i + 3];
             const double nom = r->w.vmats[mi].nom;
             for (int k = 0; k < 3; k++) {
-                (*init)[3 * (size_t)i + k] = r->w.desc.voxels[4 * i + k] * nom;
+                (*init)[3 * (size_t)i + k] = r->final_init_pos.empty() ? r->w.desc.voxels[4 * i + k] * nom
+                                                                       : r->final_init_pos[(size_t)k * nv + i];
                 (*cur)[3 * (size_t)i + k] = p[(size_t)k * nv + i];
             }
             (*matid)[i] = mi + 1;   // palette index 0 is the empty material (VX_Object.cpp:149-158, 486)

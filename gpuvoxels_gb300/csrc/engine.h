@@ -72,6 +72,10 @@ public:
     virtual int result(int64_t id, SimResult* out, std::string* err) = 0;
     virtual int info(int64_t id, int* nv, int* nl, double* dt, double* t, int64_t* steps, int* status) = 0;
     virtual int voxel_state(int64_t id, double* d13, float* f4, int32_t* flags, std::string* err) = 0;
+    // VX3 extras: measures4 = targetCloseness, numClosePairs, collisionCount, recentAngle;
+    // sig6 = per voxel localSignal, next decay time, refractory-until, pending signal, its time,
+    // next pacemaker pulse (zeros without signals).  Either pointer may be null.
+    virtual int extras(int64_t id, double* measures4, double* sig6, std::string* err) = 0;
     // Poses of many simulations in one device pass and one copy: pos3/q4/flags hold the
     // simulations' voxels one after another in the order of ids (any pointer may be null).
     virtual int gather_states(const int64_t* ids, int n, double* pos3, double* q4, uint8_t* flags, std::string* err) = 0;

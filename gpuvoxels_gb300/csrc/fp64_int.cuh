@@ -22,18 +22,53 @@
 namespace gvx {
 namespace fp64i {
 
+// On the device the bit pattern moves through an opaque register move, so that the
+// compiler cannot fold the integer tests below back into FP64 compares.
 GVX_FP64I uint64_t bits(double x) {
 #ifdef __CUDA_ARCH__
-    return (uint64_t)__double_as_longlong(x);
+    uint64_t u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+    return u;
 #else
     uint64_t u; std::memcpy(&u, &x, 8); return u;
 #endif
 }
 GVX_FP64I double from_bits(uint64_t u) {
 #ifdef __CUDA_ARCH__
-    return __longlong_as_double((long long)u);
+    double x;
+    asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+    return x;
 #else
     double x; std::memcpy(&x, &u, 8); return x;
+#endif
+}
+// The FP64 instructions of the rare cases, in a form the compiler does not move out
+// of their branch (a speculated copy would run on the FP64 pipe for every call).
+GVX_FP64I double rare_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+#else
+    return a * b;
+#endif
+}
+GVX_FP64I double rare_f2d(float f) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(r) : "f"(f));
+    return r;
+#else
+    return (double)f;
+#endif
+}
+GVX_FP64I float rare_d2f(double x) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(r) : "d"(x));
+    return r;
+#else
+    return (float)x;
 #endif
 }
 GVX_FP64I uint32_t fbits(float x) {
@@ -60,7 +95,7 @@ GVX_FP64I double mul2(double x) {
     const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
     if (e - 1u < 0x7FDu) return from_bits(b + (1ull << 52));
     if (e == 0u) return from_bits((b & kSign) | ((b & kAbs) << 1));
-    return x * 2.0;
+    return rare_mul(x, 2.0);
 }
 // x * 0.5 (exponent - 1 while the result stays normal; +-0 unchanged)
 GVX_FP64I double half(double x) {
@@ -68,7 +103,7 @@ GVX_FP64I double half(double x) {
     const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
     if (e - 2u < 0x7FDu) return from_bits(b - (1ull << 52));
     if ((b & kAbs) == 0) return x;
-    return x * 0.5;
+    return rare_mul(x, 0.5);
 }
 
 // (double)f: exact; normal floats and zeros on the integer pipes
@@ -77,7 +112,7 @@ GVX_FP64I double f2d(float f) {
     const uint32_t e = (u >> 23) & 0xFFu;
     if (e - 1u >= 254u) {
         if ((u & 0x7FFFFFFFu) == 0) return from_bits((uint64_t)u << 32);
-        return (double)f;
+        return rare_f2d(f);
     }
     const uint32_t hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + (896u << 20));
     return from_bits(((uint64_t)hi << 32) | (((uint64_t)u << 29) & 0xFFFFFFFFull));
@@ -88,7 +123,7 @@ GVX_FP64I float d2f(double x) {
     const uint32_t e = (uint32_t)(u >> 52) & 0x7FFu;
     if (e - 897u >= 254u) {
         if ((u & kAbs) == 0) return from_fbits((uint32_t)(u >> 32));
-        return (float)x;
+        return rare_d2f(x);
     }
     uint32_t m = (uint32_t)((u & kFrac) >> 29);
     const uint32_t rest = (uint32_t)u & 0x1FFFFFFFu;
@@ -117,6 +152,26 @@ GVX_FP64I bool eq0(double x) { return (bits(x) & kAbs) == 0; }
 
 // x + 0.0 with x possibly -0: IEEE gives +0 for -0 and x otherwise (NaN stays NaN)
 GVX_FP64I double plus_zero(double x) { const uint64_t b = bits(x); return from_bits(b == kSign ? 0ull : b); }
+
+// Sums, differences and products with an operand z that the algorithm makes an
+// exact zero (either sign), for any non-NaN y and finite k: IEEE gives the other
+// operand, except that a sum of two zeros is -0 only when both are -0 (a difference
+// a - b is a + (-b)), and a finite k times a zero is a zero with the XOR of the signs.
+GVX_FP64I double zero_plus(double z, double y) {    // z + y, equally y + z
+    const uint64_t uz = bits(z), uy = bits(y);
+    return from_bits((uy & kAbs) == 0 ? (uz & uy) : uy);
+}
+GVX_FP64I double zero_minus(double z, double y) {   // z - y
+    const uint64_t uz = bits(z), uy = bits(y);
+    return from_bits((uy & kAbs) == 0 ? (uz & ~uy & kSign) : (uy ^ kSign));
+}
+GVX_FP64I double minus_zero(double y, double z) {   // y - z
+    const uint64_t uz = bits(z), uy = bits(y);
+    return from_bits((uy & kAbs) == 0 ? (uy & ~uz & kSign) : uy);
+}
+GVX_FP64I double times_zero(double k, double z) {   // k * z
+    return from_bits((bits(k) ^ bits(z)) & kSign);
+}
 
 }  // namespace fp64i
 }  // namespace gvx

@@ -2,6 +2,7 @@
 // formats; values are formed in the reference's types (float corner offsets, double
 // positions).
 #include "history.h"
+#include "layout.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -64,7 +65,8 @@ float step_temperature(const SimWorld& w, int v, double t, float dt, const float
     return (float)T;
 }
 
-std::string history_record(const SimWorld& w, int64_t j, double t, float dt, const double* d13, const float* f4, const float* lsf3) {
+std::string history_record(const SimWorld& w, int64_t j, double t, float dt, const double* d13, const float* f4, const float* lsf3,
+                           const int32_t* vflags, const int32_t* lflags, const double* local_signal) {
     const double vs = 1 / 0.001;
     std::string s;
     char b[512];
@@ -73,7 +75,8 @@ std::string history_record(const SimWorld& w, int64_t j, double t, float dt, con
         snprintf(b, sizeof(b), "<<<Step%lld Time:%f>>>", (long long)j, t);
         s += b;
         for (int v = 0; v < w.nv; v++) {
-            if (w.vox_interior[v]) continue;                       // surface voxels only, in voxel order
+            // surface voxels only, in voxel order; removed voxels are left out
+            if (vflags ? (vflags[v] & (dev::VF_INTERIOR | dev::VF_REMOVED)) != 0 : w.vox_interior[v] != 0) continue;
             const double* p = d13 + 13 * (size_t)v;
             const double qw = p[6], qx = p[7], qy = p[8], qz = p[9];
             snprintf(b, sizeof(b), "%.1f,%.1f,%.1f,", p[0] * vs, p[1] * vs, p[2] * vs);
@@ -89,9 +92,10 @@ std::string history_record(const SimWorld& w, int64_t j, double t, float dt, con
             for (int i = 0; i < 3; i++) {
                 for (int corner = 0; corner < 2; corner++) {
                     const bool pos_link = corner == 1;
-                    const int l = w.vox_links[6 * (size_t)v + 2 * i + (pos_link ? 0 : 1)];
+                    const int d = 2 * i + (pos_link ? 0 : 1);
+                    const int l = w.vox_links[6 * (size_t)v + d];
                     double st = pos_link ? 1.0 : -1.0;
-                    if (l >= 0) {
+                    if (l >= 0 && (!vflags || (vflags[v] >> d) & 1)) {   // a detached link is no longer the voxel's
                         const LinkMaterial& lm = w.lmats[w.link_mat[l]];
                         const bool failed = lm.epsFail != -1.0f && lsf3[3 * (size_t)l + 1] > lm.epsFail;
                         if (!failed) st = (1 + axial_strain(w, l, lsf3[3 * (size_t)l], pos_link)) * (pos_link ? 1 : -1);
@@ -104,7 +108,8 @@ std::string history_record(const SimWorld& w, int64_t j, double t, float dt, con
             s += b;
             snprintf(b, sizeof(b), "%d,", mi + 1);
             s += b;
-            s += "0.0,;";                                          // localSignal (signals are not simulated)
+            snprintf(b, sizeof(b), "%.1f,;", local_signal ? local_signal[v] : 0.0);   // localSignal (for colouring)
+            s += b;
         }
         s += "<<<>>>";
     }
@@ -112,6 +117,7 @@ std::string history_record(const SimWorld& w, int64_t j, double t, float dt, con
         snprintf(b, sizeof(b), "|[[[%lld]]]", (long long)j);
         s += b;
         for (int l = 0; l < nl; l++) {
+            if (lflags && (lflags[l] & dev::LF_REMOVED)) continue;   // links removed with their voxels
             const double* a = d13 + 13 * (size_t)w.link_pos[l];
             const double* c = d13 + 13 * (size_t)w.link_neg[l];
             snprintf(b, sizeof(b), "%.4f,%.4f,%.4f,%.4f,%.4f,%.4f,;", a[0], a[1], a[2], c[0], c[1], c[2]);

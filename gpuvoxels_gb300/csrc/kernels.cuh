@@ -19,6 +19,71 @@ __device__ __forceinline__ int claim(int* ticket, int* s_item) {
     return *s_item;
 }
 
+// Beam forces and moments of both ends in the link frame, with the local damping
+// when the previous state is valid (VX_Link.cpp:167-215).  The float beam constants
+// enter as exactly widened doubles (b1*pos2.y is float*double in the reference).
+//
+// The two angle modes leave exact zeros in the operands, and the terms they meet are
+// settled on the integer pipes with bit-identical results (zero_plus, zero_minus,
+// minus_zero, times_zero):
+//  * small angle (kSmall): angle1v is (0,0,0); with a valid previous state the
+//    previous step was small too, so its angle1v and the difference d1 are zero;
+//  * large angle: pos2.y, pos2.z and angle1v.x are zero (the relative position was
+//    rotated onto +x by an angle whose x component is 0); with a valid previous
+//    state the same holds for the previous step, so dP.y, dP.z and d1.x are zero.
+// (A mode switch clears the valid-previous-state flag, VX_Link.cpp:85-94.)
+template <bool kSmall>
+__device__ __forceinline__ void beam_forces(const LMat& m, double fx, const d3& pos2, const d3& a1v, const d3& a2v, const d3& o2,
+                                            const d3& oa1, const d3& oa2, bool lvv, double dmN, double dmP, d3* fN_, d3* fP_, d3* mN_,
+                                            d3* mP_) {
+    const double b1 = m.b1D, b2 = m.b2D, b3 = m.b3D, a2 = m.a2D;
+    d3 fN, fP, mN, mP;
+    if (kSmall) {
+        // a1v + x = zero_plus(a1v, x);  x - a1v.x = x;  a1v.x - x = zero_minus(a1v.x, x)
+        fN = D3(fx, b1 * pos2.y - b2 * zero_plus(a1v.z, a2v.z), b1 * pos2.z + b2 * zero_plus(a1v.y, a2v.y));
+        mN = D3(a2 * minus_zero(a2v.x, a1v.x), -b2 * pos2.z - b3 * zero_plus(mul2(a1v.y), a2v.y),
+                b2 * pos2.y - b3 * zero_plus(mul2(a1v.z), a2v.z));
+        mP = D3(a2 * zero_minus(a1v.x, a2v.x), -b2 * pos2.z - b3 * zero_plus(a1v.y, mul2(a2v.y)),
+                b2 * pos2.y - b3 * zero_plus(a1v.z, mul2(a2v.z)));
+    } else {
+        // b*pos2.y and b*pos2.z are zeros; so is a1v.x
+        const double zy1 = times_zero(b1, pos2.y), zz1 = times_zero(b1, pos2.z);
+        const double zz2 = times_zero(-b2, pos2.z), zy2 = times_zero(b2, pos2.y);
+        fN = D3(fx, zero_minus(zy1, b2 * (a1v.z + a2v.z)), zero_plus(zz1, b2 * (a1v.y + a2v.y)));
+        mN = D3(a2 * minus_zero(a2v.x, a1v.x), zero_minus(zz2, b3 * (mul2(a1v.y) + a2v.y)), zero_minus(zy2, b3 * (mul2(a1v.z) + a2v.z)));
+        mP = D3(a2 * zero_minus(a1v.x, a2v.x), zero_minus(zz2, b3 * (a1v.y + mul2(a2v.y))), zero_minus(zy2, b3 * (a1v.z + mul2(a2v.z))));
+    }
+    fP = D3(-fN.x, -fN.y, -fN.z);
+    if (lvv) {
+        const double sqA1 = m.sqA1D, sqA2xIp = m.sqA2xIpD, sqB1 = m.sqB1D, sqB2xFMp = m.sqB2xFMpD, sqB3xIp = m.sqB3xIpD;
+        const d3 d2 = D3(half(a2v.x - oa2.x), half(a2v.y - oa2.y), half(a2v.z - oa2.z));
+        d3 dP, d1, pc, tN, tP;
+        if (kSmall) {
+            dP = D3(half(pos2.x - o2.x), half(pos2.y - o2.y), half(pos2.z - o2.z));
+            d1 = D3(half(minus_zero(a1v.x, oa1.x)), half(minus_zero(a1v.y, oa1.y)), half(minus_zero(a1v.z, oa1.z)));   // zeros
+            pc = D3(sqA1 * dP.x, sqB1 * dP.y - sqB2xFMp * zero_plus(d1.z, d2.z), sqB1 * dP.z + sqB2xFMp * zero_plus(d1.y, d2.y));
+            const double ddx = minus_zero(d2.x, d1.x);
+            tN = D3(-sqA2xIp * ddx, sqB2xFMp * dP.z + sqB3xIp * zero_plus(mul2(d1.y), d2.y), -sqB2xFMp * dP.y + sqB3xIp * zero_plus(mul2(d1.z), d2.z));
+            tP = D3(sqA2xIp * ddx, sqB2xFMp * dP.z + sqB3xIp * zero_plus(d1.y, mul2(d2.y)), -sqB2xFMp * dP.y + sqB3xIp * zero_plus(d1.z, mul2(d2.z)));
+        } else {
+            dP = D3(half(pos2.x - o2.x), half(minus_zero(pos2.y, o2.y)), half(minus_zero(pos2.z, o2.z)));   // y, z zeros
+            d1 = D3(half(minus_zero(a1v.x, oa1.x)), half(a1v.y - oa1.y), half(a1v.z - oa1.z));                  // x zero
+            pc = D3(sqA1 * dP.x, zero_minus(times_zero(sqB1, dP.y), sqB2xFMp * (d1.z + d2.z)),
+                    zero_plus(times_zero(sqB1, dP.z), sqB2xFMp * (d1.y + d2.y)));
+            const double ddx = minus_zero(d2.x, d1.x);
+            const double sz = times_zero(sqB2xFMp, dP.z), sy = times_zero(-sqB2xFMp, dP.y);
+            tN = D3(-sqA2xIp * ddx, zero_plus(sz, sqB3xIp * (mul2(d1.y) + d2.y)), zero_plus(sy, sqB3xIp * (mul2(d1.z) + d2.z)));
+            tP = D3(sqA2xIp * ddx, zero_plus(sz, sqB3xIp * (d1.y + mul2(d2.y))), zero_plus(sy, sqB3xIp * (d1.z + mul2(d2.z))));
+        }
+        fN = D3(fN.x + dmN * pc.x, fN.y + dmN * pc.y, fN.z + dmN * pc.z);
+        fP = D3(fP.x - dmP * pc.x, fP.y - dmP * pc.y, fP.z - dmP * pc.z);
+        const double hN = half(dmN), hP = half(dmP);
+        mN = D3(mN.x - hN * tN.x, mN.y - hN * tN.y, mN.z - hN * tN.z);
+        mP = D3(mP.x - hP * tP.x, mP.y - hP * tP.y, mP.z - hP * tP.z);
+    }
+    *fN_ = fN; *fP_ = fP; *mN_ = mN; *mP_ = mP;
+}
+
 // CVX_Link::updateForces with orientLink, updateStrain and updateTransverseInfo
 // (Voxelyze3/src/old/VX_Link.cpp:72-113, 136-141, 143-241).  Writes the two
 // end forces/moments and axial strains into the voxels' direction slots.
@@ -28,6 +93,11 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     const LMat& m = S.lm[__ldg(S.lmt + l)];
     const VMat& vN = S.vm[__ldg(S.vmat + ng)];
     const VMat& vP = S.vm[__ldg(S.vmat + pv)];
+    uint8_t fl = S.lfl[l];
+    // VX3 extras: detached and removed links are no longer updated (VX3_VoxelyzeKernel.cu:565-575),
+    // nor are links between two voxels of Fixed materials
+    if (fl & LF_GONE) return;
+    if ((S.flags & SF_FIXEDMAT) && (vN.vx3 & vP.vx3 & VM_FIXED)) return;
     const float tN = S.temp[ng], tP = S.temp[pv];
     const double restLen = half(base_size(vN, tN) + base_size(vP, tP));   // CVX_Link::updateRestLength
     const int nl = S.nl;
@@ -36,7 +106,6 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     const d3 oa1 = D3(st[3 * nl + l], st[4 * nl + l], st[5 * nl + l]);
     const d3 oa2 = D3(st[6 * nl + l], st[7 * nl + l], st[8 * nl + l]);
     float strain = S.lsf[l], maxStrain = S.lsf[nl + l], strainOffset = S.lsf[2 * nl + l];
-    uint8_t fl = S.lfl[l];
     bool small = fl & LF_SMALL, lvv = fl & LF_LVV;
 
     // orientLink
@@ -63,9 +132,9 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         a1v = D3(0, 0, 0);                  // ToRotationVector of the identity
     } else {
         angle1 = q_from_angle_to_posx(angle1, pos2, &wide1);
-        angle2 = qmul(angle1, angle2);
+        angle2 = qmul_x0(angle1, angle2);
         pos2 = D3(sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z) - restLen, 0, 0);
-        a1v = q_to_rotvec(angle1, &acos1);
+        a1v = q_to_rotvec<true>(angle1, &acos1);
     }
     const d3 a2v = q_to_rotvec(angle2, &wide2);
     st[l] = pos2.x; st[nl + l] = pos2.y; st[2 * nl + l] = pos2.z;
@@ -109,44 +178,34 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     S.lsf[l] = strain; S.lsf[nl + l] = maxStrain; S.lsf[2 * nl + l] = strainOffset;
 
     d3 fN, fP, mN, mP;
-    if (m.epsFail != -1.0f && maxStrain > m.epsFail) {
+    const bool failed = m.epsFail != -1.0f && maxStrain > m.epsFail;
+    if (failed) {
         fN = fP = mN = mP = D3(0, 0, 0);
     } else {
-        // the float beam constants enter as exactly widened doubles (b1*pos2.y is float*double in the reference)
-        const double b1 = m.b1D, b2 = m.b2D, b3 = m.b3D, a2 = m.a2D;
-        fN = D3(f2d(stress * A), b1 * pos2.y - b2 * (a1v.z + a2v.z), b1 * pos2.z + b2 * (a1v.y + a2v.y));
-        fP = D3(-fN.x, -fN.y, -fN.z);
-        mN = D3(a2 * (a2v.x - a1v.x), -b2 * pos2.z - b3 * (mul2(a1v.y) + a2v.y), b2 * pos2.y - b3 * (mul2(a1v.z) + a2v.z));
-        mP = D3(a2 * (a1v.x - a2v.x), -b2 * pos2.z - b3 * (a1v.y + mul2(a2v.y)), b2 * pos2.y - b3 * (a1v.z + mul2(a2v.z)));
-        if (lvv) {
-            const d3 dP = D3(half(pos2.x - o2.x), half(pos2.y - o2.y), half(pos2.z - o2.z));
-            const d3 d1 = D3(half(a1v.x - oa1.x), half(a1v.y - oa1.y), half(a1v.z - oa1.z));
-            const d3 d2 = D3(half(a2v.x - oa2.x), half(a2v.y - oa2.y), half(a2v.z - oa2.z));
-            const double sqA1 = m.sqA1D, sqA2xIp = m.sqA2xIpD, sqB1 = m.sqB1D, sqB2xFMp = m.sqB2xFMpD, sqB3xIp = m.sqB3xIpD;
-            const d3 pc = D3(sqA1 * dP.x, sqB1 * dP.y - sqB2xFMp * (d1.z + d2.z), sqB1 * dP.z + sqB2xFMp * (d1.y + d2.y));
-            const float dmNf = vN.dampNum / dt, dmPf = vP.dampNum / dt;   // CVX_Voxel::dampingMultiplier
-            const double dmN = f2d(dmNf), dmP = f2d(dmPf);
-            fN = D3(fN.x + dmN * pc.x, fN.y + dmN * pc.y, fN.z + dmN * pc.z);
-            fP = D3(fP.x - dmP * pc.x, fP.y - dmP * pc.y, fP.z - dmP * pc.z);
-            const double hN = half(dmN), hP = half(dmP);
-            const d3 tN = D3(-sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (mul2(d1.y) + d2.y), -sqB2xFMp * dP.y + sqB3xIp * (mul2(d1.z) + d2.z));
-            const d3 tP = D3(sqA2xIp * (d2.x - d1.x), sqB2xFMp * dP.z + sqB3xIp * (d1.y + mul2(d2.y)), -sqB2xFMp * dP.y + sqB3xIp * (d1.z + mul2(d2.z)));
-            mN = D3(mN.x - hN * tN.x, mN.y - hN * tN.y, mN.z - hN * tN.z);
-            mP = D3(mP.x - hP * tP.x, mP.y - hP * tP.y, mP.z - hP * tP.z);
+        const float dmNf = vN.dampNum / dt, dmPf = vP.dampNum / dt;   // CVX_Voxel::dampingMultiplier
+        if (small) {
+            beam_forces<true>(m, f2d(stress * A), pos2, a1v, a2v, o2, oa1, oa2, lvv, f2d(dmNf), f2d(dmPf), &fN, &fP, &mN, &mP);
         } else {
-            lvv = true;
+            beam_forces<false>(m, f2d(stress * A), pos2, a1v, a2v, o2, oa1, oa2, lvv, f2d(dmNf), f2d(dmPf), &fN, &fP, &mN, &mP);
+            fN = qrotinv_x0(angle1, fN);
+            mN = qrotinv_x0(angle1, mN);
         }
-        if (!small) {
-            fN = qrotinv(angle1, fN);
-            mN = qrotinv(angle1, mN);
-        }
+        lvv = true;
         fP = qrotinv(angle2, fP);
         mP = qrotinv(angle2, mP);
         fN = to_axis_orig(axis, fN); fP = to_axis_orig(axis, fP);
         mN = to_axis_orig(axis, mN); mP = to_axis_orig(axis, mP);
     }
+    uint8_t gone = 0;
+    if (failed && (S.flags & SF_DETACH)) {
+        // VX3 updateDetach (VX3_VoxelyzeKernel.cu:946-968): the failed link leaves both voxels'
+        // link lists (before this step's voxel update) and both become surface voxels
+        atomicAnd(&S.vfl[ng], ~((1u << (2 * axis)) | VF_INTERIOR));
+        atomicAnd(&S.vfl[pv], ~((1u << (2 * axis + 1)) | VF_INTERIOR));
+        gone = LF_GONE;
+    }
     S.lfl[l] = (uint8_t)((small ? LF_SMALL : 0) | (lvv ? LF_LVV : 0) | (wide1 ? LF_WIDE1 : 0) | (wide2 ? LF_WIDE2 : 0) |
-                         (acos1 ? LF_ACOS1 : 0));
+                         (acos1 ? LF_ACOS1 : 0) | gone);
 
     // direction slots: the negative-end voxel sees this link in direction 2*axis,
     // the positive-end voxel in direction 2*axis+1 (CVX_Voxel::force, VX_Voxel.cpp:236-238)
@@ -252,7 +311,7 @@ __global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* 
     __shared__ int s_item;
     __shared__ int s_perm[kOrderMax];
     __shared__ int s_warp[kOrderKeys * 8];
-    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; }
     for (;;) {
         const int it = claim(&tickets[0], &s_item);
         if (it >= n_items) break;
@@ -330,7 +389,13 @@ __device__ __forceinline__ bool maybe_touching(float4 a, float4 b, float env_rad
 // VX_Voxel.cpp:394-417) and sums the pair forces in increasing partner order;
 // pairs that do not overlap contribute exactly zero, so summing the
 // overlapping pairs in partner order reproduces it.
-__device__ void voxel_contacts(const Sim& S, int v, int parity, int* err) {
+__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
+    if (S.flags & SF_DYNSURF) {
+        // the surface set changes during the run: every voxel is listed, interior and
+        // removed ones have no contacts
+        const uint32_t f = S.vfl[v];
+        if (f & (VF_INTERIOR | VF_REMOVED)) { S.ccount[v] = 0; return; }
+    }
     const float4 pv = S.cpos[v];
     const float ic = S.inv_cell;
     const int cx = cell_of(pv.x, ic), cy = cell_of(pv.y, ic), cz = cell_of(pv.z, ic);
@@ -380,7 +445,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, int* err) {
                     q = nq;
                 }
             }
-    if (overflow) atomicOr(err, 1);
+    if (overflow) atomicOr(&c.error, 1);
     float* out = S.cforce + (size_t)v * 3 * kContactCap;
     for (int k = 0; k < np; k++) {
         const int q = partners[k];
@@ -390,6 +455,21 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, int* err) {
         out[3 * k] = sgn * f3[0]; out[3 * k + 1] = sgn * f3[1]; out[3 * k + 2] = sgn * f3[2];
     }
     S.ccount[v] = np;
+    if (S.flags & SF_TARGETS) {
+        // VX3 target contacts (VX3_VoxelyzeKernel.cu:713-724): each touching pair of a target and
+        // a non-target voxel counts once (collisionCount, the formulas' `hit`), and with signals
+        // the non-target voxel receives a forced signal in its step
+        const bool tv = S.vm[__ldg(S.vmat + v)].vx3 & VM_TARGET;
+        int pairs = 0;
+        bool hit = false;
+        for (int k = 0; k < np; k++) {
+            const int q = partners[k];
+            const bool tq = S.vm[__ldg(S.vmat + q)].vx3 & VM_TARGET;
+            if (tv != tq) { hit = true; if (q > v) pairs++; }
+        }
+        if (pairs) atomicAdd(&c.hit_count, pairs);
+        if (hit && !tv && (S.flags & SF_SIGNALS)) S.vfl[v] |= VF_TGTHIT;
+    }
 }
 
 __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
@@ -407,7 +487,7 @@ __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, 
         const int per = (S.hash_size + S.nsurf - 1) / (S.nsurf > 0 ? S.nsurf : 1);
         const int cb = w.begin * per, ce = min(S.hash_size, (w.end == S.nsurf) ? S.hash_size : w.end * per);
         for (int h = cb + threadIdx.x; h < ce; h += blockDim.x) other[h] = -1;
-        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, &c.error);
+        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, c);
     }
 }
 
@@ -421,13 +501,94 @@ struct StepTimes {
     double t_next;     // after it
     double t_cycles;   // t_next / TempPeriod
     double angle;      // recentAngle (force-field variable)
+    double closeness;  // targetCloseness, numClosePairs and collisionCount (force-field variables)
+    int close_pairs, hits;
 };
+
+// ---------------------------------------------------------------- VX3 signals
+// VX3_Voxel::receiveSignal (VX3/VX3_Voxel.cu:301-322): a signal arriving at `active`
+// is taken unless the voxel is refractory (a forced one always is); the voxel shows
+// it as its local signal and will relay value*signalValueDecay at that time.
+__device__ __forceinline__ void sig_receive(const Sim& S, int v, const VMat& m, double value, double active, bool force) {
+    double* G = S.sig;
+    const size_t nv = S.nv;
+    if (!force && G[SG_INACTIVE * nv + v] > active) return;
+    if (value < 0.1) return;
+    G[SG_INACTIVE * nv + v] = active + m.sigInactive;
+    G[SG_LOCAL * nv + v] = value;
+    double relay = value * m.sigDecay;
+    if (relay < 0.1) relay = 0;
+    G[SG_VALUE * nv + v] = relay;
+    G[SG_ACTIVE * nv + v] = active;
+}
+
+// A voxel's own signal work at the end of its time step (VX3_Voxel.cu:271-276):
+// propagateSignal (:323-347) relays a due signal (recorded in SG_OUT / SG_OUT_T for
+// the neighbours, which take it in k_signals), then packMaker (:291-299) and
+// localSignalDecay (:279-289).  The reference writes into the neighbours from this
+// thread while they run their own step, so its outcome depends on thread timing;
+// here every voxel first finishes its own work and the neighbours then take the
+// relayed signals in direction order, which is deterministic.
+__device__ __forceinline__ void sig_own_step(const Sim& S, int v, const VMat& m, double t) {
+    double* G = S.sig;
+    const size_t nv = S.nv;
+    double out = 0, out_t = 0;
+    if (!(G[SG_ACTIVE * nv + v] > t) && !(G[SG_VALUE * nv + v] < 0.1)) {
+        out = G[SG_VALUE * nv + v];
+        out_t = t + m.sigDelay;
+        G[SG_VALUE * nv + v] = 0;
+        G[SG_ACTIVE * nv + v] = 0;
+        G[SG_INACTIVE * nv + v] = t + 2 * m.sigDelay + m.sigInactive;
+    }
+    G[SG_OUT * nv + v] = out;
+    G[SG_OUT_T * nv + v] = out_t;
+    if ((m.vx3 & VM_PACEMAKER) && !(G[SG_PULSE * nv + v] > t)) {
+        sig_receive(S, v, m, 100, t, true);
+        G[SG_PULSE * nv + v] = t + m.pmPeriod;
+    }
+    if (!(G[SG_LOCAL_DT * nv + v] > t)) {
+        if (G[SG_LOCAL * nv + v] < 0.1) {
+            G[SG_LOCAL * nv + v] = 0;
+        } else {
+            G[SG_LOCAL * nv + v] = G[SG_LOCAL * nv + v] * 0.9;
+            G[SG_LOCAL_DT * nv + v] = t + 0.01;
+        }
+    }
+}
+
+// Voxels of Fixed materials and removed voxels do not move (gpu_update_voxels,
+// VX3_VoxelyzeKernel.cu:582-588), keep their temperature (gpu_update_temperature
+// skips them) and run no signal step of their own; they count in the centre of
+// mass, and a fixed voxel stays in the contact search (a removed one leaves it).
+__device__ void frozen_voxel(const Sim& S, int v, uint32_t fl, const VMat& m, const StepTimes& st, int flags, double* com4,
+                             int* hash_next_table) {
+    if (flags & SF_SIGNALS) {
+        if ((fl & VF_TGTHIT) && !(fl & VF_REMOVED)) sig_receive(S, v, m, 100, st.t_now, true);
+        S.sig[SG_OUT * (size_t)S.nv + v] = 0;
+    }
+    if (fl & VF_TGTHIT) S.vfl[v] = fl & ~VF_TGTHIT;
+    const d3 pos = D3(S.px[v], S.py[v], S.pz[v]);
+    if (com4 && (fl & VF_MEASURED)) {
+        const double w = m.mass;
+        com4[0] += pos.x * w; com4[1] += pos.y * w; com4[2] += pos.z * w; com4[3] += w;
+    }
+    if ((flags & SF_COLLIDE) && !(fl & (VF_INTERIOR | VF_REMOVED))) hash_insert(S, v, pos, S.temp[v], hash_next_table);
+}
 
 __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, const StepTimes& st, int flags, double* com4, int* hash_next_table) {
     const double t_cycles = st.t_cycles;
     const int nv = S.nv;
     const VMat& m = S.vm[__ldg(S.vmat + v)];
     uint32_t fl = S.vfl[v];
+    if ((flags & (SF_REMOVE | SF_FIXEDMAT)) && ((fl & VF_REMOVED) || (m.vx3 & VM_FIXED))) {
+        frozen_voxel(S, v, fl, m, st, flags, com4, hash_next_table);
+        return;
+    }
+    // VX3: a contact with a target voxel this step hands a forced signal to a non-target
+    // voxel (handle_collision_attachment, VX3_VoxelyzeKernel.cu:709-724), before the cilia
+    // forces and the voxel's own step
+    if ((flags & SF_SIGNALS) && (fl & VF_TGTHIT)) sig_receive(S, v, m, 100, st.t_now, true);
+    fl &= ~VF_TGTHIT;
     const Ext* e = (fl & VF_EXT) ? &S.ext[__ldg(S.vext + v)] : nullptr;
     d3 pos = D3(S.px[v], S.py[v], S.pz[v]);
     d3 lm = D3(S.mx[v], S.my[v], S.mz[v]);
@@ -459,18 +620,23 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         }
         // VX3 cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859; VX3_Voxel::force,
         // VX3_Voxel.cu:376): surface voxels of a cilia material, once it is switched on, are
-        // pushed along their base cilia force rotated into the world frame (no signals: the
-        // signal-scaled shift term is zero)
+        // pushed along baseCiliaForce + localSignal * shiftCiliaForce rotated into the world
+        // frame (without signals the shift term is zero)
         if ((flags & SF_CILIA) && !(fl & VF_INTERIOR) && m.cilia != 0 && !fp64i::gt(m.ciliaOn, st.t_now)) {
-            const d3 cf = qrot(q, D3(S.cilia[v], S.cilia[nv + v], S.cilia[2 * nv + v]));
+            d3 base = D3(S.cilia[v], S.cilia[nv + v], S.cilia[2 * nv + v]);
+            if (S.shift_cilia) {
+                const double ls = S.sig[SG_LOCAL * (size_t)nv + v];
+                base = D3(base.x + ls * S.shift_cilia[v], base.y + ls * S.shift_cilia[nv + v], base.z + ls * S.shift_cilia[2 * nv + v]);
+            }
+            const d3 cf = qrot(q, base);
             F = D3(F.x + cf.x * m.cilia, F.y + cf.y * m.cilia, F.z + cf.z * m.cilia);
         }
         // VX3 force field (VX3_Voxel::timeStep, VX3_Voxel.cu:178-184): formulas of the voxel's
         // position and the simulation's time, recent angle and voxel count
         if (flags & SF_FFIELD) {
             MathVars mv;
-            mv.x = pos.x; mv.y = pos.y; mv.z = pos.z; mv.hit = 0; mv.t = st.t_now; mv.angle = st.angle;
-            mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = nv;
+            mv.x = pos.x; mv.y = pos.y; mv.z = pos.z; mv.hit = st.hits; mv.t = st.t_now; mv.angle = st.angle;
+            mv.closeness = st.closeness; mv.num_close_pairs = st.close_pairs; mv.num_voxel = nv;
             F.x += mathtree_eval(S.ffield[0], mv);
             F.y += mathtree_eval(S.ffield[1], mv);
             F.z += mathtree_eval(S.ffield[2], mv);
@@ -572,10 +738,16 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         if (!(ten[0] && ten[1] && ten[2])) {
             float add = 0;
             for (int i = 0; i < 3; i++) if (ten[i]) add += s[i];
-            const float value = d2f(pow(f2d(1.0f + add), f2d(-m.nu))) - 1.0f;
+            const float value = poisson_pow(1.0f + add, -m.nu) - 1.0f;
             for (int i = 0; i < 3; i++) if (!ten[i]) s[i] = value;
         }
         S.ps[v] = s[0]; S.ps[nv + v] = s[1]; S.ps[2 * nv + v] = s[2];
+    }
+    // VX3 signals: the voxel's own signal work at the end of its step (a voxel fixed in all
+    // degrees of freedom returns from VX3_Voxel::timeStep before it, VX3_Voxel.cu:166-173)
+    if (flags & SF_SIGNALS) {
+        if (!fixed_all) sig_own_step(S, v, m, st.t_now);
+        else S.sig[SG_OUT * (size_t)nv + v] = 0;
     }
     // actuation temperature for the next step
     float temp_next = temp;
@@ -605,15 +777,53 @@ __device__ __forceinline__ double block_sum(double x, double* red) {
     return r;
 }
 
+// VX3 secondary experiment (VX3_VoxelyzeKernel.cu:336-349, 365-397), after the CoM
+// sample: every material whose RemoveFromSimulationAfterThisManySeconds has passed
+// loses its voxels (frozen, unlinked from their neighbours, off the surface), and once
+// ReinitializeInitialPositionAfterThisManySeconds has passed the initial centre of
+// mass becomes the last sampled one and the initial positions the current ones.  One
+// thread; each of these happens once per run.
+__device__ __noinline__ void secondary_experiment(const Sim& S, Ctl& c, double t_now) {
+    const int nv = S.nv;
+    for (int i = 0; i < S.n_mats && i < 32; i++) {
+        const VMat& m = S.vm[i];
+        if ((c.removed_mats >> i) & 1) continue;
+        if (!(m.removeAfter > 0 && m.removeAfter < t_now)) continue;
+        for (int v = 0; v < nv; v++) {
+            if (S.vmat[v] != i) continue;
+            const uint32_t f = S.vfl[v];
+            if (f & VF_REMOVED) continue;
+            for (int d = 0; d < 6; d++) {
+                if (!(f & (1u << d))) continue;
+                const int l = S.vlink[6 * v + d];
+                S.lfl[l] |= LF_GONE | LF_REMOVED;
+                const int u = S.lneg[l] == v ? S.lpos[l] : S.lneg[l];
+                S.vfl[u] &= ~((1u << (d ^ 1)) | VF_INTERIOR);   // the neighbour holds the link in the opposite direction
+            }
+            S.vfl[v] = (f & ~(VF_LINKS | VF_INTERIOR)) | VF_REMOVED;
+        }
+        c.removed_mats |= 1 << i;
+    }
+    if (!c.reinit_done && S.reinit_after < t_now) {
+        c.reinit_done = 1;
+        for (int k = 0; k < 3; k++) c.init_com[k] = c.com[k];
+        for (int v = 0; v < nv; v++) {
+            S.init_pos[v] = S.px[v]; S.init_pos[nv + v] = S.py[v]; S.init_pos[2 * (size_t)nv + v] = S.pz[v];
+        }
+    }
+}
+
 // Per-simulation bookkeeping after its last voxel item of the step (one thread):
 // status on divergence/error, time and step count, cycle CoM sampling and the
 // recent-angle measure (VX3_VoxelyzeKernel.cu:314-334, 352), stop condition.
 // Kept out of line so the voxel loop does not carry its registers and stack.
-__device__ __noinline__ void sim_control(Ctl& c, bool div, double t_next, int64_t stepno, bool com_step, int flags, int nv,
-                                         const double* partials) {
+__device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double t_next, int64_t stepno, bool com_step, int flags,
+                                         int nv, const double* partials) {
     c.done_items = 0;
     if (div) { c.status = 3; return; }
     if (c.error) { c.status = 4; return; }
+    const double t_now = c.t;
+    if (flags & SF_SIGNALS) { c.t_sig = t_now; c.sig_pending = 1; }   // k_signals completes this step's signals
     c.t = t_next;
     c.steps = stepno;
     if (flags & SF_COLLIDE) c.hash_parity ^= 1;
@@ -637,12 +847,32 @@ __device__ __noinline__ void sim_control(Ctl& c, bool div, double t_next, int64_
             c.recent_angle = acos((bax * cbx + bay * cby + baz * cbz) /
                                   (sqrt(bax * bax + bay * bay + baz * baz) * sqrt(cbx * cbx + cby * cby + cbz * cbz)));
         }
+        // VX3 computeTargetCloseness (VX3_VoxelyzeKernel.cu:545-563): over the target voxels in
+        // index order, pairs closer than MaxDistInVoxelLengthsToCountAsPair voxel sizes and the
+        // sum of inverse distances
+        if ((flags & SF_TARGETS) && S.close_r != 0) {
+            double ret = 0;
+            int pairs = 0;
+            for (int i = 0; i < S.n_targets; i++) {
+                const int a = S.targets[i];
+                for (int j = i + 1; j < S.n_targets; j++) {
+                    const int b = S.targets[j];
+                    const double dx = S.px[b] - S.px[a], dy = S.py[b] - S.py[a], dz = S.pz[b] - S.pz[a];
+                    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+                    if (dist < S.close_r) pairs++;
+                    ret += 1 / dist;
+                }
+            }
+            c.closeness = ret;
+            c.num_close_pairs = pairs;
+        }
     }
+    if (flags & SF_REMOVE) secondary_experiment(S, c, t_now);
     bool stop = c.target > 0 && stepno >= c.target;
     if (c.stop.n > 0 && !c.no_stop) {
         MathVars mv;
-        mv.x = c.com[0]; mv.y = c.com[1]; mv.z = c.com[2]; mv.hit = 0; mv.t = c.t; mv.angle = c.recent_angle;
-        mv.closeness = 0; mv.num_close_pairs = 0; mv.num_voxel = nv;
+        mv.x = c.com[0]; mv.y = c.com[1]; mv.z = c.com[2]; mv.hit = c.hit_count; mv.t = c.t; mv.angle = c.recent_angle;
+        mv.closeness = c.closeness; mv.num_close_pairs = c.num_close_pairs; mv.num_voxel = nv;
         if (mathtree_eval(c.stop, mv) > 0) stop = true;
     }
     if (stop) c.status = 2;
@@ -682,6 +912,7 @@ __global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim
         __syncthreads();
         StepTimes st;
         st.t_now = c.t; st.t_next = t_next; st.t_cycles = s_cycles; st.angle = c.recent_angle;
+        st.closeness = c.closeness; st.close_pairs = c.num_close_pairs; st.hits = c.hit_count;
         const int64_t stepno = c.steps + 1;
         const bool com_step = c.cycle_step > 0 && (stepno % c.cycle_step) == 0;
         const int flags = S.flags;
@@ -709,8 +940,45 @@ __global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim
         __syncthreads();
         if (s_last && threadIdx.x == 0) {
             __threadfence();
-            sim_control(c, div, t_next, stepno, com_step, flags, S.nv, partials);
+            sim_control(S, c, div, t_next, stepno, com_step, flags, S.nv, partials);
         }
+    }
+}
+
+// Second half of a step's VX3 signals, after every voxel's own signal work: each
+// voxel takes the signals its linked neighbours relayed this step, in direction order
+// (VX3_Voxel::propagateSignal, VX3_Voxel.cu:323-347, run from the receiving side).
+// Runs over the voxel items of simulations whose step completed; the last block of a
+// simulation closes its signal phase.
+__global__ void __launch_bounds__(256) k_signals(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items,
+                                                 int* tickets) {
+    __shared__ int s_item, s_last;
+    for (;;) {
+        const int it = claim(&tickets[3], &s_item);
+        if (it >= n_items) break;
+        const Item w = items[it];
+        Ctl& c = ctl[w.sim];
+        if (!c.sig_pending) continue;
+        const Sim& S = sims[w.sim];
+        const double t = c.t_sig;
+        const size_t nv = S.nv;
+        for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) {
+            const uint32_t f = S.vfl[v];
+            if (!(f & VF_LINKS)) continue;
+            const VMat& m = S.vm[S.vmat[v]];
+            for (int d = 0; d < 6; d++) {
+                if (!(f & (1u << d))) continue;
+                const int l = S.vlink[6 * v + d];
+                const int u = S.lneg[l] == v ? S.lpos[l] : S.lneg[l];
+                const double out = S.sig[SG_OUT * nv + u];
+                if (out > 0) sig_receive(S, v, m, out, S.sig[SG_OUT_T * nv + u], false);
+            }
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = (atomicAdd(&c.sig_done_items, 1) == c.n_vox_items - 1);
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) { c.sig_done_items = 0; c.sig_pending = 0; }
     }
 }
 
@@ -749,7 +1017,8 @@ __global__ void k_init_temp(const Sim* __restrict__ sims, const int* __restrict_
     const float initial = initials[blockIdx.y];
     const float two_pi = 2 * 3.1415926f;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < S.nv; v += gridDim.x * blockDim.x) {
-        if ((S.flags & SF_VARY) && !fp64i::gt(S.vm[S.vmat[v]].thermalOn, 0.0)) {
+        const VMat& m = S.vm[S.vmat[v]];
+        if ((S.flags & SF_VARY) && !fp64i::gt(m.thermalOn, 0.0) && !(m.vx3 & VM_FIXED)) {
             double T = S.temp_amp * sin((double)two_pi * (0.0 / S.temp_period + S.phase[v]));
             if (!(S.flags & SF_EXPAND) && T > 0) T = 0;
             S.temp[v] = (float)T;
@@ -767,6 +1036,7 @@ __global__ void k_hash_build(const Sim* __restrict__ sims, Ctl* ctl, const int* 
     int* head = S.hash_head + (size_t)ctl[sim].hash_parity * S.hash_size;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.nsurf; i += gridDim.x * blockDim.x) {
         const int v = S.surf[i];
+        if (S.vfl[v] & (VF_INTERIOR | VF_REMOVED)) continue;   // listed only while the surface can change
         hash_insert(S, v, D3(S.px[v], S.py[v], S.pz[v]), S.temp[v], head);
     }
 }
@@ -816,6 +1086,9 @@ inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, 
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk, double* p) {
     k_voxels<<<g, b, 0, s>>>(sims, ctl, it, n, tk, p);
 }
+inline void l_signals(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) {
+    k_signals<<<g, b, 0, s>>>(sims, ctl, it, n, tk);
+}
 inline void l_dt(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
     for (int k0 = 0; k0 < n; k0 += 65535) k_dt<<<dim3(g, (unsigned)std::min(65535, n - k0)), 256, 0, s>>>(sims, ctl, slots + k0, n - k0);
 }
@@ -832,7 +1105,7 @@ inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int
     if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
 }
 inline KernelSet make_kernelset(const char* name) {
-    return KernelSet{name, l_links, l_contacts, l_voxels, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
+    return KernelSet{name, l_links, l_contacts, l_voxels, l_signals, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

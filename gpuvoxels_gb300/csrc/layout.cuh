@@ -25,11 +25,24 @@ constexpr uint8_t LF_LVV = 2;             // LOCAL_VELOCITY_VALID
 constexpr uint8_t LF_WIDE1 = 4;           // last step: angle1 came from FromAngleToPosX's general (acos/sincos) branch
 constexpr uint8_t LF_WIDE2 = 8;           // last step: angle2's rotation vector took the acos branch
 constexpr uint8_t LF_ACOS1 = 16;          // last step: angle1's rotation vector took the acos branch
+constexpr uint8_t LF_GONE = 32;           // VX3: detached (failed) or removed with a voxel: no longer updated
+constexpr uint8_t LF_REMOVED = 64;        // VX3: removed with a voxel (left out of the history's link records)
 constexpr uint32_t VF_FLOORC = 1u << 10;  // last step: the voxel touched the floor
+constexpr uint32_t VF_REMOVED = 1u << 11; // VX3: removed from the simulation (frozen, no links, no contacts)
+constexpr uint32_t VF_TGTHIT = 1u << 12;  // VX3: this step's contacts include a target voxel (non-target voxel)
 
 // sim flag bits
 constexpr int SF_FLOOR = 1, SF_COLLIDE = 2, SF_VARY = 4, SF_EXPAND = 8;
 constexpr int SF_CILIA = 16, SF_FFIELD = 32;   // VX3 extras: cilia forces, force-field formulas
+constexpr int SF_SIGNALS = 64;                 // VX3 signals
+constexpr int SF_TARGETS = 128;                // target materials present (contact count, closeness)
+constexpr int SF_DETACH = 256;                 // failed links detach from their voxels
+constexpr int SF_REMOVE = 512;                 // secondary experiment: material removal, initial position reset
+constexpr int SF_FIXEDMAT = 1024;              // materials marked Fixed (their voxels never move)
+constexpr int SF_DYNSURF = SF_DETACH | SF_REMOVE;   // the surface set can change during the run
+
+// VMat::vx3 bits
+constexpr int VM_TARGET = 1, VM_PACEMAKER = 2, VM_FIXED = 4;
 
 struct VMat {
     float E, nu, cte, mus, muk, eHat;
@@ -41,13 +54,28 @@ struct VMat {
     float sizef;        // (float)nom
     double nom;
     int32_t measured;
-    int32_t pad;
+    int32_t vx3;        // VM_* bits
     // the float constants above that enter FP64 expressions, widened once (exact)
     double massInvD, IinvD, gDampTD, gDampRD, cDampTD, gravForceD;
     double halfNom;       // nom/2
     double halfMassInv;   // 0.5*(double)massInv
     // VX3 material extras: cilia force scale and start time, thermal actuation start time
     double cilia, ciliaOn, thermalOn;
+    // signals: pacemaker period, relayed fraction, relay delay, refractory period; removal time
+    double pmPeriod, sigDecay, sigDelay, sigInactive, removeAfter;
+};
+
+// VX3 per-voxel signal state (SF_SIGNALS), one block of nv doubles each
+enum SigField {
+    SG_LOCAL = 0,     // localSignal
+    SG_LOCAL_DT,      // localSignaldt: next decay time
+    SG_INACTIVE,      // inactiveUntil
+    SG_VALUE,         // d_signal.value: pending signal to relay
+    SG_ACTIVE,        // d_signal.activeTime
+    SG_PULSE,         // packmakerNextPulse
+    SG_OUT,           // this step's relayed value (0: none)
+    SG_OUT_T,         // its arrival time at the neighbours
+    SG_FIELDS
 };
 
 struct LMat {
@@ -106,6 +134,15 @@ struct Sim {
     // VX3 extras
     const double* cilia;        // BaseCiliaForce, 3 blocks of nv (SF_CILIA)
     const MathTree* ffield;     // x, y, z force-field formulas (SF_FFIELD)
+    const double* shift_cilia;  // ShiftCiliaForce, 3 blocks of nv (SF_CILIA with SF_SIGNALS)
+    double* sig;                // SG_FIELDS blocks of nv (SF_SIGNALS)
+    const int32_t* vlink;       // link per voxel direction, 6 per voxel, -1 if none (SF_SIGNALS, SF_REMOVE)
+    const int32_t* targets;     // target voxel ids in index order (SF_TARGETS)
+    int32_t n_targets;
+    int32_t n_mats;
+    double close_r;             // MaxDistInVoxelLengthsToCountAsPair * voxel size (0: closeness off)
+    double reinit_after;        // ReinitializeInitialPositionAfterThisManySeconds (SF_REMOVE set: secondary experiment)
+    double* init_pos;           // initial positions, 3 blocks of nv (secondary experiment)
 };
 
 // Mutable per-simulation control block.
@@ -118,9 +155,18 @@ struct Ctl {
     uint32_t maxf2_bits;
     int32_t hash_parity;
     int32_t no_stop;            // set while vx3_step advances a fixed count: the stop formula is not applied
-    int32_t pad_ctl;
+    int32_t sig_done_items;     // signal-phase items finished this step (SF_SIGNALS)
     double com[3], com_hist[2][3];
     double recent_angle;
+    // VX3 measures: target closeness and close pairs (at CoM samples), target contacts so far
+    double closeness;
+    int32_t num_close_pairs, hit_count;
+    double t_sig;               // currentTime of the step whose signal phase is pending
+    int32_t sig_pending;        // 1 between a completed voxel update and its signal phase
+    int32_t removed_mats;       // materials already removed (bit per palette index)
+    int32_t reinit_done;        // initial centre of mass reset (secondary experiment)
+    int32_t pad_ctl2;
+    double init_com[3];         // initial centre of mass (host value, reset by the secondary experiment)
     MathTree stop;
 };
 

@@ -35,6 +35,10 @@ using fp64i::mul2;
 using fp64i::half;
 using fp64i::f2d;
 using fp64i::d2f;
+using fp64i::zero_plus;
+using fp64i::zero_minus;
+using fp64i::minus_zero;
+using fp64i::times_zero;
 
 // (float)(n/d) compared with a float threshold T, deciding with one multiply
 // unless n/d lies within 2^-20 (relative) of T, where the quotient is formed
@@ -97,18 +101,38 @@ __device__ __forceinline__ d3 qrotinv(const q4& q, const d3& f) {
               tw * q.y - tx * q.z + ty * q.w + tz * q.x,
               tw * q.z + tx * q.y - ty * q.x + tz * q.w);
 }
-// Quat3D::ToRotationVector  Quat3D.h:121-126; *wide = the acos branch was taken
+// The same two operations for a quaternion whose x component is the exact zero
+// FromAngleToPosX always leaves there (finite operands): the q.x terms are settled on
+// the integer pipes (times_zero, zero_plus, minus_zero), with bit-identical results.
+__device__ __forceinline__ q4 qmul_x0(const q4& a, const q4& f) {
+    return Q4(minus_zero(a.w * f.w, times_zero(f.x, a.x)) - a.y * f.y - a.z * f.z,
+              zero_plus(times_zero(f.w, a.x), a.w * f.x) + a.y * f.z - a.z * f.y,
+              minus_zero(a.w * f.y, times_zero(f.z, a.x)) + a.y * f.w + a.z * f.x,
+              zero_plus(times_zero(f.y, a.x), a.w * f.z) - a.y * f.x + a.z * f.w);
+}
+__device__ __forceinline__ d3 qrotinv_x0(const q4& q, const d3& f) {
+    double tw = zero_plus(times_zero(f.x, q.x), q.y * f.y) + q.z * f.z;
+    double tx = q.w * f.x - q.y * f.z + q.z * f.y;
+    double ty = zero_plus(times_zero(f.z, q.x), q.w * f.y) - q.z * f.x;
+    double tz = minus_zero(q.w * f.z, times_zero(f.y, q.x)) + q.y * f.x;
+    return D3(zero_plus(times_zero(tw, q.x), tx * q.w) + ty * q.z - tz * q.y,
+              zero_plus(times_zero(tz, q.x), tw * q.y - tx * q.z + ty * q.w),
+              minus_zero(tw * q.z + tx * q.y, times_zero(ty, q.x)) + tz * q.w);
+}
+// Quat3D::ToRotationVector  Quat3D.h:121-126; *wide = the acos branch was taken.
+// kX0: q.x is the exact zero of a FromAngleToPosX result (the x component then too).
+template <bool kX0 = false>
 __device__ __forceinline__ d3 q_to_rotvec(const q4& q, bool* wide = nullptr) {
     if (fp64i::ge(fabs(q.w), 1.0)) return D3(0, 0, 0);   // q.w >= 1 || q.w <= -1
     double sl = 1.0 - q.w * q.w;
     if (fp64i::lt(sl, 2.4e-3)) {
         double s = sqrt((2 - mul2(q.w)) / sl);
-        return D3(mul2(q.x) * s, mul2(q.y) * s, mul2(q.z) * s);
+        return D3(kX0 ? times_zero(s, q.x) : mul2(q.x) * s, mul2(q.y) * s, mul2(q.z) * s);
     }
     if (wide) *wide = true;
     double a = acos(q.w);
     double inv = 1.0 / sqrt(sl);
-    return D3((mul2(q.x) * a) * inv, (mul2(q.y) * a) * inv, (mul2(q.z) * a) * inv);
+    return D3(kX0 ? times_zero(inv, times_zero(a, q.x)) : (mul2(q.x) * a) * inv, (mul2(q.y) * a) * inv, (mul2(q.z) * a) * inv);
 }
 // Quat3D::FromRotationVector  Quat3D.h:128-143
 __device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
@@ -186,6 +210,29 @@ __device__ __forceinline__ float mat_stress(const LMat& m, float strain, float t
         }
     }
     return 0.0f;
+}
+
+// (float)pow(x, y) for the Poisson strain of CVX_Voxel::strain (VX_Voxel.cpp:327), where
+// x = 1 + the summed axial strains and y = -poissonsRatio.  Near x = 1 (|x - 1| <= 1/8,
+// every stable simulation) it is exp(y * log x) from two series summed far enough for a
+// double within about one unit in the last place: log(1+a) = 2 atanh(a / (2 + a)) to
+// the w^6 term (w = (a/(2+a))^2 <= 4.5e-3) and exp(z) to the z^10 term (|z| <= 0.125);
+// the float rounding of that double equals the rounded library result in every case
+// checked on the host (5e7 random inputs).  Other inputs use the library pow.
+__device__ __forceinline__ float poisson_pow(float x, float y) {
+    const double a = f2d(x) - 1.0;
+    if (!fp64i::le(fabs(a), 0.125) || !(y <= 0.0f && y >= -1.0f)) return d2f(pow(f2d(x), f2d(y)));
+    const double s = a / (2.0 + a);
+    const double w = s * s;
+    double p = 1.0 / 13;
+    p = fma(p, w, 1.0 / 11); p = fma(p, w, 1.0 / 9); p = fma(p, w, 1.0 / 7);
+    p = fma(p, w, 1.0 / 5); p = fma(p, w, 1.0 / 3); p = fma(p, w, 1.0);
+    const double z = f2d(y) * (mul2(s) * p);
+    double e = 1.0 / 3628800;
+    e = fma(e, z, 1.0 / 362880); e = fma(e, z, 1.0 / 40320); e = fma(e, z, 1.0 / 5040); e = fma(e, z, 1.0 / 720);
+    e = fma(e, z, 1.0 / 120); e = fma(e, z, 1.0 / 24); e = fma(e, z, 1.0 / 6); e = fma(e, z, 0.5);
+    e = fma(e, z, 1.0); e = fma(e, z, 1.0);
+    return d2f(e);
 }
 
 // CVX_Voxel::baseSize(axis) and baseSizeAverage  Voxelyze3/src/old/VX_Voxel.h:91-92

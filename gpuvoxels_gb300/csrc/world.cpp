@@ -397,6 +397,14 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
             pm.cilia = get_d(mech, "Cilia", 0);
             pm.cilia_on_after = get_d(mech, "TurnOnCiliaAfterThisManySeconds", 0);
             pm.thermal_on_after = get_d(mech, "TurnOnThermalExpansionAfterThisManySeconds", 0);
+            pm.is_pacemaker = get_i(mech, "isPaceMaker", 0) != 0;
+            pm.pacemaker_period = get_d(mech, "PaceMakerPeriod", 0);
+            pm.signal_decay = get_d(mech, "signalValueDecay", 0.9);
+            pm.signal_delay = get_d(mech, "signalTimeDelay", 0.03);
+            pm.inactive_period = get_d(mech, "inactivePeriod", 0.03);
+            pm.is_target = get_i(mech, "isTarget", 0) != 0;
+            pm.remove_after = get_d(mech, "RemoveFromSimulationAfterThisManySeconds", 0);
+            pm.fixed = get_i(mech, "Fixed", 0) != 0;
             if (const XmlNode* ss = mech ? mech->child("SSData") : nullptr) {
                 if (const XmlNode* se = ss->child("StrainData"))
                     for (auto* c : se->children_named("Strain")) pm.strain_data.push_back(atof_s(c->text));
@@ -451,10 +459,10 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
                 if (cells[(size_t)k * X * Y + j] > 0) phase_by_voxel.push_back(j < (int)arr.size() ? atof_s(arr[j]) : 0.0);
         }
     }
-    /* BaseCiliaForce: per filled cell an x,y,z triple, layer by layer; a short layer pads with
-       zeros (VXA/VX_Object.cpp:1886-1921) */
-    if (const XmlNode* bcf = st->child("BaseCiliaForce")) {
-        auto pl = bcf->children_named("Layer");
+    /* BaseCiliaForce and ShiftCiliaForce: per filled cell an x,y,z triple, layer by layer; a
+       short layer pads with zeros (VXA/VX_Object.cpp:1886-1958) */
+    auto read_triples = [&](const XmlNode* node, std::vector<double>* out) {
+        auto pl = node->children_named("Layer");
         for (int k = 0; k < Z; k++) {
             std::vector<std::string> arr;
             if (k < (int)pl.size()) {
@@ -470,10 +478,12 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
             for (int j = 0; j < X * Y; j++) {
                 if (cells[(size_t)k * X * Y + j] == 0) continue;
                 for (int c = 0; c < 3; c++)
-                    d->base_cilia.push_back(arr.size() > (size_t)(3 * j + c) && arr.size() > (size_t)(3 * j) ? atof_s(arr[3 * j + c]) : 0.0);
+                    out->push_back(arr.size() > (size_t)(3 * j + c) && arr.size() > (size_t)(3 * j) ? atof_s(arr[3 * j + c]) : 0.0);
             }
         }
-    }
+    };
+    if (const XmlNode* bcf = st->child("BaseCiliaForce")) read_triples(bcf, &d->base_cilia);
+    if (const XmlNode* scf = st->child("ShiftCiliaForce")) read_triples(scf, &d->shift_cilia);
     int n = 0;
     for (long i = 0; i < (long)X * Y * Z; i++) {
         int mi = (int)(signed char)cells[i] - 1;
@@ -500,6 +510,10 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     /* VX3 extras: cilia switch and force field; an absent force-field component is the constant 0
        (VX3_ForceField's default, Utils/VX3_ForceField.h:10-19) */
     d->enable_cilia = (int)ptree_num(*root, "VXA.Simulator.EnableCilia", 0);
+    d->enable_signals = (int)ptree_num(*root, "VXA.Simulator.EnableSignals", 0);
+    d->enable_detach = ptree_bool(*root, "VXA.Simulator.AttachDetach.EnableDetach", false);
+    d->secondary_experiment = (int)ptree_num(*root, "VXA.Simulator.SecondaryExperiment", 0);
+    d->reinit_initial_after = ptree_num(*root, "VXA.Simulator.ReinitializeInitialPositionAfterThisManySeconds", 0.0);
     const char* ff_paths[3] = {"VXA.Simulator.ForceField.x_forcefield", "VXA.Simulator.ForceField.y_forcefield",
                                "VXA.Simulator.ForceField.z_forcefield"};
     for (int k = 0; k < 3; k++) {

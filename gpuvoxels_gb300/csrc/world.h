@@ -25,6 +25,16 @@ struct PaletteMaterial {
     // VX3 material keys (VXA/VX_Object.cpp:1425-1437): cilia force scale and start time,
     // thermal actuation start time
     double cilia = 0, cilia_on_after = 0, thermal_on_after = 0;
+    // VX3 signalling keys (VX_Object.cpp:1420-1424): pacemaker and its period, the factor a
+    // relayed signal keeps, the relay delay and the refractory period (seconds)
+    int is_pacemaker = 0;
+    double pacemaker_period = 0, signal_decay = 0.9, signal_delay = 0.03, inactive_period = 0.03;
+    // target voxels (closeness measure, target contacts; VX_Object.cpp:1434) and removal of the
+    // material's voxels after a time (SecondaryExperiment, VX_Object.cpp:1427)
+    int is_target = 0;
+    double remove_after = 0;
+    // VX3 Fixed materials: their voxels never move (VX_Object.cpp:1435)
+    int fixed = 0;
 };
 
 struct External {
@@ -64,6 +74,16 @@ struct SimDesc {
     std::vector<double> base_cilia;
     MathTree force_field[3];
     bool has_force_field = false;
+    // VX3 signals (VXA.Simulator.EnableSignals) and the signal-scaled cilia term (per-voxel
+    // ShiftCiliaForce, 3 per voxel, empty when absent)
+    int enable_signals = 0;
+    std::vector<double> shift_cilia;
+    // VX3 link detachment on failure (VXA.Simulator.AttachDetach.EnableDetach) and the
+    // secondary experiment (VXA.Simulator.SecondaryExperiment: material removal after a time,
+    // initial centre of mass reset after ReinitializeInitialPositionAfterThisManySeconds)
+    int enable_detach = 0;
+    int secondary_experiment = 0;
+    double reinit_initial_after = 0;
 };
 
 // Parses a base VXA plus an optional VXD (whose children carrying replace="VXA.a.b"

@@ -49,12 +49,15 @@ def largest_component(cells: np.ndarray) -> np.ndarray:
 
 
 def _mat_xml(i: int, m: dict) -> str:
+    """One palette material; m['mech'] (optional) is extra XML inside <Mechanical> (model, VX3 keys)."""
+    mech = m.get("mech", "")
+    model = "" if "<MatModel>" in mech else "<MatModel>0</MatModel><Fail_Stress>0</Fail_Stress>"
     return (f"<Material ID=\"{i}\"><MatType>0</MatType><Name>m{i}</Name>"
             f"<Display><Red>0.5</Red><Green>0.5</Green><Blue>0.5</Blue><Alpha>1</Alpha></Display>"
-            f"<Mechanical><MatModel>0</MatModel><Elastic_Mod>{m['E']!r}</Elastic_Mod><Fail_Stress>0</Fail_Stress>"
+            f"<Mechanical>{model}<Elastic_Mod>{m['E']!r}</Elastic_Mod>"
             f"<Density>{m['rho']!r}</Density><Poissons_Ratio>{m['nu']!r}</Poissons_Ratio><CTE>{m['cte']!r}</CTE>"
             f"<MaterialTempPhase>0</MaterialTempPhase><uStatic>{m['mus']!r}</uStatic><uDynamic>{m['muk']!r}</uDynamic>"
-            f"</Mechanical></Material>")
+            f"{mech}</Mechanical></Material>")
 
 
 def _formula_t_gt(t_end: float) -> str:

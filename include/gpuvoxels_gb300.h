@@ -130,6 +130,12 @@ int vx3_get_states(vx3_ctx* ctx, const vx3_sim_id* ids, int n, double* pos, doub
 int vx3_get_voxel_state(vx3_ctx* ctx, vx3_sim_id id, double* d13, float* f4, int32_t* flags);
 /* Link state (CVX_Link, VX_Link.h:68-99): d9 = pos2 angle1v angle2v, f3 = strain maxStrain strainOffset, flags. */
 int vx3_get_link_state(vx3_ctx* ctx, vx3_sim_id id, double* d9, float* f3, int32_t* flags);
+/* VX3 extras of one simulation: measures4 = targetCloseness, numClosePairs, collisionCount and
+ * recentAngle (VX3_VoxelyzeKernel members, VX3/VX3_VoxelyzeKernel.cuh); signals6 = per voxel
+ * localSignal, localSignaldt, inactiveUntil, d_signal.value, d_signal.activeTime and
+ * packmakerNextPulse (VX3_Voxel members, VX3/VX3_Voxel.h:304-309; zeros without EnableSignals).
+ * Either pointer may be NULL. */
+int vx3_get_extras(vx3_ctx* ctx, vx3_sim_id id, double* measures4, double* signals6);
 
 /* Replaces the .history stream the reference prints from its simulation loop when the VXA
  * sets Simulator/RecordHistory/RecordStepSize (VX3/VX3_SimulationManager.cu:40-114): settings

@@ -46,6 +46,14 @@ int main(int argc, char** argv) {
         if (!same(mul2(a), a * 2.0)) report("mul2", a, 0);
         if (!same(half(a), a * 0.5)) report("half", a, 0);
         if (!same(plus_zero(a), a + 0.0)) report("plus_zero", a, 0);
+        // known-zero forms: z a zero of either sign, y any non-NaN value, k finite
+        const double z = (y & 1) ? -0.0 : 0.0;
+        if (a == a) {
+            if (!same(zero_plus(z, a), z + a)) report("zero_plus", z, a);
+            if (!same(zero_minus(z, a), z - a)) report("zero_minus", z, a);
+            if (!same(minus_zero(a, z), a - z)) report("minus_zero", a, z);
+            if (a - a == 0 && !same(times_zero(a, z), a * z)) report("times_zero", a, z);
+        }
     }
     std::printf("%ld cases, %ld mismatches\n", n, bad);
     return bad ? 1 : 0;
