@@ -36,7 +36,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
            "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states",
-           "vx3_get_extras"]
+           "vx3_get_extras", "vx3_get_links"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -97,6 +97,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_inspect_externals": (I, [S, S, P, P, P]),
         "vx3_get_states": (I, [P, P, I, P, P, P]),
         "vx3_get_extras": (I, [P, I64, P, P]),
+        "vx3_get_links": (I, [P, I64, P, P, I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -278,6 +279,15 @@ class Context:
         return dict(targetCloseness=m[0], numClosePairs=int(m[1]), collisionCount=int(m[2]), recentAngle=m[3],
                     localSignal=g[:, 0], localSignalDt=g[:, 1], inactiveUntil=g[:, 2], signalValue=g[:, 3],
                     signalTime=g[:, 4], pacemakerNextPulse=g[:, 5])
+
+    def links(self, sim: int) -> np.ndarray:
+        """Every link in use (loaded, then made by VX3 attachment): rows of negative end,
+        positive end, axis, flags."""
+        n = np.zeros(1, np.int32)
+        self._check(self.L.vx3_get_links(self.h, sim, _p(n), None, 0))
+        out = np.zeros((max(int(n[0]), 1), 4), np.int32)
+        self._check(self.L.vx3_get_links(self.h, sim, _p(n), _p(out), int(n[0])))
+        return out[:int(n[0])]
 
     def get_state(self, sim: int):
         nv = self.info(sim).num_voxel

@@ -205,8 +205,16 @@ int history_after_chunk(vx3_ctx* c, const vx3_sim_id* ids, int n) {
             if (int e = c->eng->extras(ids[i], nullptr, sig.data(), &err)) return fail(c, e, err);
             for (int v = 0; v < nv; v++) sig[v] = sig[6 * (size_t)v];   // localSignal of each voxel
         }
+        std::vector<int32_t> l4;
+        int32_t n_links = 0;
+        if (w->desc.enable_attach) {   // links made during the run are recorded too
+            if (int e = c->eng->links(ids[i], &n_links, nullptr, 0, &err)) return fail(c, e, err);
+            l4.resize(4 * (size_t)std::max(n_links, 1));
+            if (int e = c->eng->links(ids[i], &n_links, l4.data(), n_links, &err)) return fail(c, e, err);
+        }
         const std::string rec = gvx::history_record(*w, j, t, (float)dt, d13.data(), f4.data(), lsf.data(), vf.data(),
-                                                    nl > 0 ? lf.data() : nullptr, sig.empty() ? nullptr : sig.data());
+                                                    nl > 0 ? lf.data() : nullptr, sig.empty() ? nullptr : sig.data(),
+                                                    l4.empty() ? nullptr : l4.data(), n_links);
         fwrite(rec.data(), 1, rec.size(), h.f);
         fflush(h.f);
         h.last_j = j;
@@ -365,6 +373,13 @@ int vx3_get_link_state(vx3_ctx* c, vx3_sim_id id, double* d9, float* f3, int32_t
     if (!c) return VX3_E_ARG;
     std::string err;
     int e = c->eng->link_state(id, d9, f3, flags, &err);
+    return e ? fail(c, e, err) : VX3_OK;
+}
+
+int vx3_get_links(vx3_ctx* c, vx3_sim_id id, int32_t* n_links, int32_t* ends4, int max) {
+    if (!c || !n_links || max < 0) return VX3_E_ARG;
+    std::string err;
+    int e = c->eng->links(id, n_links, ends4, max, &err);
     return e ? fail(c, e, err) : VX3_OK;
 }
 
@@ -549,7 +564,7 @@ int vx3_inspect_vxa(const char* base, const char* vxd, int32_t* counts, double* 
         return e;
     }
     if (counts) {
-        counts[0] = w.nv; counts[1] = w.nl; counts[2] = (int32_t)w.vmats.size(); counts[3] = (int32_t)w.lmats.size();
+        counts[0] = w.nv; counts[1] = w.nl; counts[2] = (int32_t)w.vmats.size(); counts[3] = (int32_t)w.loaded_lmats;
         counts[4] = w.surface_count; counts[5] = (int32_t)w.desc.externals.size();
     }
     if (env) {
@@ -578,7 +593,7 @@ int vx3_inspect_topology(const char* base, const char* vxd, int32_t* vox4, int32
         if (vmat18) memcpy(vmat18 + 18 * k, v, sizeof(v));
         if (vnom) vnom[k] = m.nom;
     }
-    for (size_t k = 0; k < w.lmats.size(); k++) {
+    for (size_t k = 0; k < (size_t)w.loaded_lmats; k++) {
         const gvx::LinkMaterial& m = w.lmats[k];
         if (lidx2) { lidx2[2 * k] = m.vox1; lidx2[2 * k + 1] = m.vox2; }
         float v[20] = {m.E, m.nu, m.eHat, m.a1, m.a2, m.b1, m.b2, m.b3, m.sqA1, m.sqA2xIp, m.sqB1, m.sqB2xFMp, m.sqB3xIp,

@@ -146,6 +146,9 @@ public:
     int n_link_items_ = 0, n_contact_items_ = 0, n_vox_items_ = 0;
     bool any_collide_ = false;
     bool any_signals_ = false;
+    int n_attach_ = 0, cap_attach_ = 0;     // simulations with VX3 attachment in the batch
+    int* d_attach_slots_ = nullptr;
+    std::vector<int> attach_slots_host_;
     cudaGraphExec_t graph_ = nullptr;
     int graph_len_ = 0;
     bool batch_dirty_ = true;
@@ -173,6 +176,7 @@ public:
         }
         cudaFree(d_gather_);
         cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_partials_); cudaFree(d_com4_);
+        cudaFree(d_attach_slots_);
         cudaFree(arena_base_);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
@@ -268,8 +272,12 @@ public:
         for (auto& m : d.mats) if (m.remove_after > 0) return true;
         return false;
     }
-    static bool dynamic_surface(const SimDesc& d) { return d.enable_detach || removes_materials(d); }
+    static bool dynamic_surface(const SimDesc& d) { return d.enable_detach || removes_materials(d) || attaches(d); }
     static int contact_list_size(const SimWorld& w) { return dynamic_surface(w.desc) ? w.nv : w.surface_count; }
+    // VX3 attachment needs the contact pass to find touching pairs; links made at run time
+    // take slots nl .. 3*nv-1 (every voxel has six link directions)
+    static bool attaches(const SimDesc& d) { return d.enable_attach && d.collisions; }
+    static int link_capacity(const SimWorld& w) { return attaches(w.desc) ? std::max(w.nl, 3 * w.nv) : w.nl; }
     static int target_count(const SimWorld& w) {
         int n = 0;
         for (int i = 0; i < w.nv; i++) n += w.desc.mats[w.desc.voxels[4 * i + 3]].is_target ? 1 : 0;
@@ -279,12 +287,12 @@ public:
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
         size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos, cilia, ffield;
-        size_t shift, sig, vlink, targets, init_pos;
+        size_t shift, sig, vlink, targets, init_pos, lnew, cand, cpart, acond;
         int hash_size;
     };
     static void compute_layout(const SimWorld& w, Layout* L, Offs* o) {
         Offs t{};
-        const size_t nv = w.nv, nl = w.nl;
+        const size_t nv = w.nv, nl = link_capacity(w);
         const bool col = w.desc.collisions;
         const SimDesc& d = w.desc;
         t.vm = L->add(sizeof(dev::VMat) * w.vmats.size());
@@ -328,7 +336,13 @@ public:
         if (w.desc.has_force_field) t.ffield = L->add(sizeof(MathTree) * 3);
         if (d.enable_signals && d.enable_cilia && !d.shift_cilia.empty()) t.shift = L->add(8 * 3 * nv);
         if (d.enable_signals) t.sig = L->add(8 * dev::SG_FIELDS * nv);
-        if (d.enable_signals || removes_materials(d)) t.vlink = L->add(4 * 6 * nv);
+        if (d.enable_signals || removes_materials(d) || attaches(d)) t.vlink = L->add(4 * 6 * nv);
+        if (attaches(d)) {
+            t.lnew = L->add(4 * nl);
+            t.cand = L->add(8 * (size_t)dev::kContactCap / 2 * nv + 8);
+            t.cpart = L->add(4 * (size_t)dev::kContactCap * nv);
+            t.acond = L->add(sizeof(MathTree) * 5);
+        }
         if (int nt = target_count(w)) t.targets = L->add(4 * (size_t)nt);
         if (d.secondary_experiment) t.init_pos = L->add(8 * 3 * nv);
         if (o) *o = t;
@@ -495,6 +509,8 @@ public:
             x.sigDelay = pm.signal_delay;
             x.sigInactive = pm.inactive_period;
             x.removeAfter = pm.remove_after;
+            x.attachLmat = w.attach_lmat.empty() ? -1 : w.attach_lmat[i];
+            if (pm.sticky) x.vx3 |= dev::VM_STICKY;
         }
         dev::LMat* lm = (dev::LMat*)P(o.lm);
         for (size_t i = 0; i < w.lmats.size(); i++) {
@@ -540,6 +556,7 @@ public:
             if (w.vox_interior[i]) f |= dev::VF_INTERIOR;
             if (w.vox_ext[i] >= 0) f |= dev::VF_EXT;
             if (w.vmats[mi].is_measured) f |= dev::VF_MEASURED;
+            if (attaches(w.desc)) f |= dev::VF_ATTACH;   // enableAttach starts true (VX3_Voxel.h:302)
             vfl[i] = f;
             vmat[i] = (uint8_t)mi;
             vext[i] = w.vox_ext[i];
@@ -551,6 +568,8 @@ public:
         memcpy(P(o.lax), w.link_axis.data(), nl);
         memcpy(P(o.lmt), w.link_mat.data(), nl);
         memset(P(o.lfl), dev::LF_SMALL, std::max<size_t>(1, nl));
+        const size_t nl_cap = link_capacity(w);
+        if (nl_cap > nl) memset(P(o.lfl) + nl, dev::LF_GONE, nl_cap - nl);   // slots for links made at run time
         int flags = 0;
         if (w.desc.floor) flags |= dev::SF_FLOOR;
         if (w.desc.collisions) flags |= dev::SF_COLLIDE;
@@ -575,7 +594,11 @@ public:
                     for (int k = 0; k < 3; k++) c[k * nv + i] = dd.shift_cilia[3 * i + k];
             }
         }
-        if (dd.enable_signals || removes_materials(dd)) memcpy(P(o.vlink), w.vox_links.data(), 4 * 6 * nv);
+        if (dd.enable_signals || removes_materials(dd) || attaches(dd)) memcpy(P(o.vlink), w.vox_links.data(), 4 * 6 * nv);
+        if (attaches(dd)) {
+            flags |= dev::SF_ATTACH;
+            memcpy(P(o.acond), dd.attach_cond, sizeof(MathTree) * 5);
+        }
         const int n_targets = target_count(w);
         if (n_targets) {
             flags |= dev::SF_TARGETS;
@@ -605,7 +628,7 @@ public:
         }
         dev::Sim& S = r->dsim;
         S = dev::Sim{};
-        S.nv = (int)nv; S.nl = (int)nl; S.nsurf = contact_list_size(w); S.flags = flags;
+        S.nv = (int)nv; S.nl = (int)nl_cap; S.nsurf = contact_list_size(w); S.flags = flags;
         S.temp_amp = w.desc.temp_amplitude; S.temp_period = w.desc.temp_period;
         S.cell_size = std::max(1e-9, 2 * 0.625 * max_bsa * 1.01);
         S.hash_size = o.hash_size > 0 ? o.hash_size : 1;
@@ -619,8 +642,8 @@ public:
         S.temp = (float*)D(o.temp); S.ps = (float*)D(o.ps); S.vfl = (uint32_t*)D(o.vfl);
         S.vmat = (const uint8_t*)D(o.vmat); S.vext = (const int32_t*)D(o.vext); S.phase = (const double*)D(o.phase);
         S.sf = (double*)D(o.sf); S.sm = (double*)D(o.sm); S.ss = (float*)D(o.ss);
-        S.lneg = (const int32_t*)D(o.lneg); S.lpos = (const int32_t*)D(o.lpos);
-        S.lax = (const uint8_t*)D(o.lax); S.lmt = (const uint8_t*)D(o.lmt);
+        S.lneg = (int32_t*)D(o.lneg); S.lpos = (int32_t*)D(o.lpos);
+        S.lax = (uint8_t*)D(o.lax); S.lmt = (uint8_t*)D(o.lmt);
         S.lst = (double*)D(o.lst); S.lsf = (float*)D(o.lsf); S.lfl = (uint8_t*)D(o.lfl);
         S.ijk = (const int16_t*)D(o.ijk);
         if (w.desc.collisions) {
@@ -636,7 +659,17 @@ public:
             S.sig = (double*)D(o.sig);
             if (dd.enable_cilia && !dd.shift_cilia.empty()) S.shift_cilia = (const double*)D(o.shift);
         }
-        if (dd.enable_signals || removes_materials(dd)) S.vlink = (const int32_t*)D(o.vlink);
+        if (dd.enable_signals || removes_materials(dd) || attaches(dd)) S.vlink = (int32_t*)D(o.vlink);
+        if (attaches(dd)) {
+            S.nl_cap = (int)nl_cap;
+            S.cand_cap = dev::kContactCap / 2 * (int)nv + 1;
+            S.safety_guard = dd.safety_guard;
+            S.attach_mask = dd.attach_cond_mask;
+            S.lnew = (int32_t*)D(o.lnew);
+            S.cand = (int32_t*)D(o.cand);
+            S.cpart = (int32_t*)D(o.cpart);
+            S.attach_cond = (const MathTree*)D(o.acond);
+        }
         if (n_targets) { S.targets = (const int32_t*)D(o.targets); S.n_targets = n_targets; }
         S.close_r = dd.max_dist_pairs * dd.vox_size;   // MaxDistInVoxelLengthsToCountAsPair * voxSize
         S.n_mats = (int)w.vmats.size();
@@ -652,6 +685,7 @@ public:
         c.hash_parity = 0;
         // currentCenterOfMass starts as the initial one (VX3_SimulationManager.cu:54-55)
         for (int k = 0; k < 3; k++) c.com[k] = c.init_com[k] = r->init_com[k];
+        c.n_links = w.nl;
         r->pending_ctl = c;
         return 0;
     }
@@ -761,16 +795,19 @@ public:
     // Builds work items for a set of slots: links, contacts and voxels.
     int build_items(const std::vector<int>& slots, std::string* err) {
         std::vector<dev::Item> items;
+        std::vector<int> attach_slots;
         n_link_items_ = n_contact_items_ = n_vox_items_ = 0;
         any_collide_ = any_signals_ = false;
         for (int s : slots) {
             SimRec* r = slot_owner_[s];
-            for (int b = 0; b < r->w.nl; b += items_links_) items.push_back({s, b, std::min(r->w.nl, b + items_links_), 0});
+            const int nl = link_capacity(r->w);
+            for (int b = 0; b < nl; b += items_links_) items.push_back({s, b, std::min(nl, b + items_links_), 0});
         }
         n_link_items_ = (int)items.size();
         for (int s : slots) {
             SimRec* r = slot_owner_[s];
             if (r->w.desc.enable_signals) any_signals_ = true;
+            if (attaches(r->w.desc)) attach_slots.push_back(s);
             const int ns = contact_list_size(r->w);
             if (!r->w.desc.collisions || ns == 0) continue;
             any_collide_ = true;
@@ -796,6 +833,16 @@ public:
             CK(cudaMalloc(&d_partials_, sizeof(double) * 4 * cap_items_));
         }
         if (!items.empty()) CK(cudaMemcpyAsync(d_items_, items.data(), sizeof(dev::Item) * items.size(), cudaMemcpyHostToDevice, stream_));
+        n_attach_ = (int)attach_slots.size();
+        if (n_attach_ > cap_attach_) {
+            cudaFree(d_attach_slots_);
+            cap_attach_ = std::max(n_attach_, 2 * cap_attach_);
+            CK(cudaMalloc(&d_attach_slots_, sizeof(int) * cap_attach_));
+        }
+        if (n_attach_) {
+            attach_slots_host_ = attach_slots;   // kept alive for the asynchronous copy
+            CK(cudaMemcpyAsync(d_attach_slots_, attach_slots_host_.data(), sizeof(int) * n_attach_, cudaMemcpyHostToDevice, stream_));
+        }
         for (size_t i = 0; i < slots.size(); i++) {
             int vals[2] = {ctl_items[i].second, ctl_items[i].first};   // n_vox_items, item_begin
             CK(cudaMemcpyAsync(&d_ctl_[slots[i]].n_vox_items, vals, sizeof(vals), cudaMemcpyHostToDevice, stream_));
@@ -813,7 +860,7 @@ public:
         return std::max(1, std::min(n_items, sm_count_ * per_sm));
     }
 
-    int launches_per_step() const { return 2 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0); }
+    int launches_per_step() const { return 2 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0); }
 
     void launch_step(cudaStream_t st, bool prof) {
         const dev::Item* li = d_items_;
@@ -823,6 +870,7 @@ public:
         ks_.links(grid_for(n_link_items_, block_links_), block_links_, st, d_sims_, d_ctl_, li, n_link_items_, d_tickets_);
         if (prof) cudaEventRecord(evk_[1], st);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
+        if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
         ks_.voxels(grid_for(n_vox_items_, block_voxels_), block_voxels_, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_,
                    d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
@@ -1280,6 +1328,28 @@ public:
         return 0;
     }
 
+    int links(int64_t id, int32_t* n_links, int32_t* ends4, int max, std::string* err) override {
+        SimRec* r = find(id);
+        if (!r) { *err = "unknown simulation id"; return -6; }
+        if (!r->resident) if (int e = upload(r, err)) return e;
+        dev::Ctl c;
+        if (int e = read_ctl(r->slot, &c, err)) return e;
+        *n_links = c.n_links;
+        const int n = std::min(c.n_links, max);
+        if (n <= 0 || !ends4) return 0;
+        std::vector<int32_t> ln((size_t)n), lp((size_t)n);
+        std::vector<uint8_t> la((size_t)n), lf((size_t)n);
+        CK(cudaMemcpyAsync(ln.data(), r->dsim.lneg, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(lp.data(), r->dsim.lpos, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(la.data(), r->dsim.lax, (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(lf.data(), r->dsim.lfl, (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (int i = 0; i < n; i++) {
+            ends4[4 * i] = ln[i]; ends4[4 * i + 1] = lp[i]; ends4[4 * i + 2] = la[i]; ends4[4 * i + 3] = lf[i];
+        }
+        return 0;
+    }
+
     int extras(int64_t id, double* measures4, double* sig6, std::string* err) override {
         SimRec* r = find(id);
         if (!r) { *err = "unknown simulation id"; return -6; }
@@ -1305,18 +1375,19 @@ public:
         SimRec* r = find(id);
         if (!r) { *err = "unknown simulation id"; return -6; }
         if (!r->resident) if (int e = upload(r, err)) return e;
-        const int nl = r->w.nl;
+        const int nl = r->w.nl;                 // the loaded links (links made at run time follow them)
+        const size_t stride = r->dsim.nl;       // link capacity: the blocks' stride
         if (nl == 0) return 0;
-        std::vector<double> st(9 * (size_t)nl);
-        std::vector<float> sf(3 * (size_t)nl);
+        std::vector<double> st(9 * stride);
+        std::vector<float> sf(3 * stride);
         std::vector<uint8_t> fl((size_t)nl);
-        CK(cudaMemcpyAsync(st.data(), r->dsim.lst, 72 * (size_t)nl, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(sf.data(), r->dsim.lsf, 12 * (size_t)nl, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(st.data(), r->dsim.lst, 72 * stride, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(sf.data(), r->dsim.lsf, 12 * stride, cudaMemcpyDeviceToHost, stream_));
         CK(cudaMemcpyAsync(fl.data(), r->dsim.lfl, nl, cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         for (int i = 0; i < nl; i++) {
-            if (d9) for (int k = 0; k < 9; k++) d9[9 * (size_t)i + k] = st[(size_t)k * nl + i];
-            if (f3) for (int k = 0; k < 3; k++) f3[3 * (size_t)i + k] = sf[(size_t)k * nl + i];
+            if (d9) for (int k = 0; k < 9; k++) d9[9 * (size_t)i + k] = st[(size_t)k * stride + i];
+            if (f3) for (int k = 0; k < 3; k++) f3[3 * (size_t)i + k] = sf[(size_t)k * stride + i];
             if (flags) flags[i] = fl[i];
         }
         return 0;

@@ -76,6 +76,9 @@ public:
     // sig6 = per voxel localSignal, next decay time, refractory-until, pending signal, its time,
     // next pacemaker pulse (zeros without signals).  Either pointer may be null.
     virtual int extras(int64_t id, double* measures4, double* sig6, std::string* err) = 0;
+    // Every link in use (the loaded ones, then those VX3 attachment made): *n_links, and for
+    // the first `max` of them negative end, positive end, axis and flag byte.
+    virtual int links(int64_t id, int32_t* n_links, int32_t* ends4, int max, std::string* err) = 0;
     // Poses of many simulations in one device pass and one copy: pos3/q4/flags hold the
     // simulations' voxels one after another in the order of ids (any pointer may be null).
     virtual int gather_states(const int64_t* ids, int n, double* pos3, double* q4, uint8_t* flags, std::string* err) = 0;

@@ -66,7 +66,8 @@ float step_temperature(const SimWorld& w, int v, double t, float dt, const float
 }
 
 std::string history_record(const SimWorld& w, int64_t j, double t, float dt, const double* d13, const float* f4, const float* lsf3,
-                           const int32_t* vflags, const int32_t* lflags, const double* local_signal) {
+                           const int32_t* vflags, const int32_t* lflags, const double* local_signal, const int32_t* links4,
+                           int n_links) {
     const double vs = 1 / 0.001;
     std::string s;
     char b[512];
@@ -116,10 +117,13 @@ std::string history_record(const SimWorld& w, int64_t j, double t, float dt, con
     if (w.desc.record_link) {
         snprintf(b, sizeof(b), "|[[[%lld]]]", (long long)j);
         s += b;
-        for (int l = 0; l < nl; l++) {
-            if (lflags && (lflags[l] & dev::LF_REMOVED)) continue;   // links removed with their voxels
-            const double* a = d13 + 13 * (size_t)w.link_pos[l];
-            const double* c = d13 + 13 * (size_t)w.link_neg[l];
+        const int n = links4 ? n_links : nl;
+        for (int l = 0; l < n; l++) {
+            const int fl = links4 ? links4[4 * l + 3] : (lflags ? lflags[l] : 0);
+            if (fl & dev::LF_REMOVED) continue;   // links removed with their voxels
+            const int lp = links4 ? links4[4 * l + 1] : w.link_pos[l], ln = links4 ? links4[4 * l] : w.link_neg[l];
+            const double* a = d13 + 13 * (size_t)lp;
+            const double* c = d13 + 13 * (size_t)ln;
             snprintf(b, sizeof(b), "%.4f,%.4f,%.4f,%.4f,%.4f,%.4f,;", a[0], a[1], a[2], c[0], c[1], c[2]);
             s += b;
         }

@@ -23,7 +23,10 @@ std::string history_header(const SimWorld& w, double optimal_dt);
 // lflags are the engine's current voxel and link flag words (which voxels are on the surface or
 // removed and which links are present, as VX3 detachment and removal change them) and
 // local_signal the voxels' VX3 local signals; each may be null (the loaded topology, no signals).
+// links4/n_links: the links in use (negative end, positive end, axis, flags) where VX3
+// attachment made links during the run (null: the loaded links).
 std::string history_record(const SimWorld& w, int64_t j, double t, float dt, const double* d13, const float* f4, const float* lsf3,
-                           const int32_t* vflags = nullptr, const int32_t* lflags = nullptr, const double* local_signal = nullptr);
+                           const int32_t* vflags = nullptr, const int32_t* lflags = nullptr, const double* local_signal = nullptr,
+                           const int32_t* links4 = nullptr, int n_links = 0);
 
 }  // namespace gvx

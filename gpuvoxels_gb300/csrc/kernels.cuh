@@ -195,6 +195,12 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         mP = qrotinv(angle2, mP);
         fN = to_axis_orig(axis, fN); fP = to_axis_orig(axis, fP);
         mN = to_axis_orig(axis, mN); mP = to_axis_orig(axis, mP);
+        if (S.lnew && S.lnew[l] > 0) {
+            // VX3 attachment: a new link acts at 1% for its first SafetyGuard updates (VX3_Link.cu:206-213)
+            fN = D3(fN.x * 0.01, fN.y * 0.01, fN.z * 0.01); fP = D3(fP.x * 0.01, fP.y * 0.01, fP.z * 0.01);
+            mN = D3(mN.x * 0.01, mN.y * 0.01, mN.z * 0.01); mP = D3(mP.x * 0.01, mP.y * 0.01, mP.z * 0.01);
+            S.lnew[l] -= 1;
+        }
     }
     uint8_t gone = 0;
     if (failed && (S.flags & SF_DETACH)) {
@@ -429,6 +435,17 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
                             k += ox + (r - abs(oy));
                             near = (S.reach[(size_t)v * kReachWords + (k >> 5)] >> (k & 31)) & 1u;
                         }
+                        if (!near && (S.flags & SF_ATTACH)) {
+                            // links made at run time join voxels the loaded topology kept apart:
+                            // voxels linked to each other do not collide (is_neighbor depth 1,
+                            // VX3_VoxelyzeKernel.cu:697-700)
+                            const uint32_t fv = S.vfl[v];
+                            for (int d = 0; d < 6; d++)
+                                if ((fv >> d) & 1) {
+                                    const int l = S.vlink[6 * v + d];
+                                    if (S.lneg[l] == q || S.lpos[l] == q) near = true;
+                                }
+                        }
                         if (!near) {
                             const int a = v < q ? v : q, b = v < q ? q : v;
                             float f3[3];
@@ -447,6 +464,8 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
             }
     if (overflow) atomicOr(&c.error, 1);
     float* out = S.cforce + (size_t)v * 3 * kContactCap;
+    if (S.cpart)   // partner ids, kept where attachment may drop a pair's force
+        for (int k = 0; k < np; k++) S.cpart[(size_t)v * kContactCap + k] = partners[k];
     for (int k = 0; k < np; k++) {
         const int q = partners[k];
         float f3[3];
@@ -455,6 +474,22 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
         out[3 * k] = sgn * f3[0]; out[3 * k + 1] = sgn * f3[1]; out[3 * k + 2] = sgn * f3[2];
     }
     S.ccount[v] = np;
+    if (S.flags & SF_ATTACH) {
+        // VX3 attachment candidates (handle_collision_attachment, VX3_VoxelyzeKernel.cu:729-742):
+        // touching voxels that both allow attachment, of one sticky material that is not Fixed;
+        // the rest of the test and the link creation run in k_attach, in pair order
+        const uint32_t fv = S.vfl[v];
+        const int mv = __ldg(S.vmat + v);
+        const VMat& mm = S.vm[mv];
+        if ((fv & VF_ATTACH) && (mm.vx3 & VM_STICKY) && !(mm.vx3 & VM_FIXED)) {
+            for (int k = 0; k < np; k++) {
+                const int q = partners[k];
+                if (q < v || __ldg(S.vmat + q) != mv || !(S.vfl[q] & VF_ATTACH)) continue;
+                const int slot = atomicAdd(&c.n_cand, 1);
+                if (slot < S.cand_cap) { S.cand[2 * slot] = v; S.cand[2 * slot + 1] = q; }
+            }
+        }
+    }
     if (S.flags & SF_TARGETS) {
         // VX3 target contacts (VX3_VoxelyzeKernel.cu:713-724): each touching pair of a target and
         // a non-target voxel counts once (collisionCount, the formulas' `hit`), and with signals
@@ -717,6 +752,17 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
     S.mx[v] = lm.x; S.my[v] = lm.y; S.mz[v] = lm.z;
     S.qw[v] = q.w; S.qx[v] = q.x; S.qy[v] = q.y; S.qz[v] = q.z;
     S.ax[v] = am.x; S.ay[v] = am.y; S.az[v] = am.z;
+    if (flags & SF_ATTACH) {
+        // enableAttach (gpu_update_voxels, VX3_VoxelyzeKernel.cu:608-620): every given attach
+        // condition is positive at the voxel's new position
+        MathVars mv;
+        mv.x = pos.x; mv.y = pos.y; mv.z = pos.z; mv.hit = st.hits; mv.t = st.t_now; mv.angle = st.angle;
+        mv.closeness = st.closeness; mv.num_close_pairs = st.close_pairs; mv.num_voxel = nv;
+        bool ok = true;
+        for (int k = 0; k < 5 && ok; k++)
+            if ((S.attach_mask >> k) & 1) ok = mathtree_eval(S.attach_cond[k], mv) > 0;
+        fl = ok ? (fl | VF_ATTACH) : (fl & ~VF_ATTACH);
+    }
     S.vfl[v] = fl;
     if (com4 && (fl & VF_MEASURED)) {
         const double w = m.mass;
@@ -823,7 +869,7 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
     if (div) { c.status = 3; return; }
     if (c.error) { c.status = 4; return; }
     const double t_now = c.t;
-    if (flags & SF_SIGNALS) { c.t_sig = t_now; c.sig_pending = 1; }   // k_signals completes this step's signals
+    if (flags & SF_SIGNALS) c.sig_pending = 1;   // k_signals completes this step's signals
     c.t = t_next;
     c.steps = stepno;
     if (flags & SF_COLLIDE) c.hash_parity ^= 1;
@@ -945,6 +991,119 @@ __global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim
     }
 }
 
+// VX3 attachment (handle_collision_attachment, VX3_VoxelyzeKernel.cu:729-827) for one
+// simulation, after its contact pass and before its voxel update: the candidate pairs
+// (touching voxels of one sticky material that both allow attachment) in increasing
+// pair order; a pair not within 5 links of each other gets a new link along the axis
+// on which the other voxel lies in the first voxel's frame, if both voxels have that
+// link slot free.  The reference creates links from many threads at once with no
+// synchronisation; here one thread creates them in pair order, which is deterministic.
+// The new link starts from the reset state (VX3_Link::reset, VX3_Link.cu:58-70), acts
+// at 1% for SafetyGuard updates, and the pair's contact forces of this step are dropped.
+__device__ bool linked_within(const Sim& S, int from, int target, int depth) {
+    // VX3's is_neighbor (VX3_VoxelyzeKernel.cu:651-680): a path of at most `depth` links that
+    // never steps straight back over the link it arrived by (depth-first, explicit stack)
+    constexpr int kStack = 1 + 5 * 5;
+    int sv[kStack], sl[kStack], sd[kStack];
+    int sp = 0;
+    sv[0] = from; sl[0] = -1; sd[0] = 0;
+    sp = 1;
+    while (sp > 0) {
+        --sp;
+        const int v = sv[sp], in = sl[sp], dd = sd[sp];
+        if (v == target) return true;
+        if (dd >= depth) continue;
+        const uint32_t f = S.vfl[v];
+        for (int d = 5; d >= 0; d--) {
+            if (!((f >> d) & 1)) continue;
+            const int l = S.vlink[6 * v + d];
+            if (l == in || sp >= kStack) continue;
+            sv[sp] = S.lneg[l] == v ? S.lpos[l] : S.lneg[l];
+            sl[sp] = l;
+            sd[sp] = dd + 1;
+            sp++;
+        }
+    }
+    return false;
+}
+
+// Drops voxel v's contact force from partner q for this step (a zero force adds nothing).
+__device__ void drop_pair_contact(const Sim& S, int v, int q) {
+    const int n = S.ccount[v];
+    const int32_t* part = S.cpart + (size_t)v * kContactCap;
+    float* f = S.cforce + (size_t)v * 3 * kContactCap;
+    for (int k = 0; k < n; k++)
+        if (part[k] == q) { f[3 * k] = 0.0f; f[3 * k + 1] = 0.0f; f[3 * k + 2] = 0.0f; }
+}
+
+__global__ void k_attach(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
+    if ((int)blockIdx.x >= n || threadIdx.x != 0) return;
+    const int sim = slots[blockIdx.x];
+    Ctl& c = ctl[sim];
+    const Sim& S = sims[sim];
+    if (c.status != 1 || c.diverged || !(S.flags & SF_ATTACH)) { c.n_cand = 0; return; }
+    const int nc = min(c.n_cand, S.cand_cap);
+    c.n_cand = 0;
+    int* cand = S.cand;
+    // insertion sort of the pairs (few per step)
+    for (int i = 1; i < nc; i++) {
+        const int a = cand[2 * i], b = cand[2 * i + 1];
+        int j = i;
+        while (j > 0 && (cand[2 * j - 2] > a || (cand[2 * j - 2] == a && cand[2 * j - 1] > b))) {
+            cand[2 * j] = cand[2 * j - 2]; cand[2 * j + 1] = cand[2 * j - 1];
+            j--;
+        }
+        cand[2 * j] = a; cand[2 * j + 1] = b;
+    }
+    const int nv = S.nv;
+    for (int i = 0; i < nc; i++) {
+        // voxel1 is the later voxel of the pair in the surface list (gpu_update_attach takes
+        // first > second, VX3_VoxelyzeKernel.cu:833-843)
+        const int v2 = cand[2 * i], v1 = cand[2 * i + 1];
+        if ((S.vfl[v1] | S.vfl[v2]) & VF_REMOVED) continue;
+        if (linked_within(S, v1, v2, 5)) continue;
+        // relative position of voxel2 in voxel1's frame: orientation1.RotateVec3DInv(-(pos1 - pos2))
+        const q4 a = Q4(S.qw[v1], S.qx[v1], S.qy[v1], S.qz[v1]);
+        const d3 e = D3(S.px[v1] - S.px[v2], S.py[v1] - S.py[v2], S.pz[v1] - S.pz[v2]);
+        const d3 ea = qrotinv(a, D3(-e.x, -e.y, -e.z));
+        const double fx = fabs(ea.x), fy = fabs(ea.y), fz = fabs(ea.z);
+        int axis;
+        bool reverse;
+        if (fx >= fy && fx >= fz) { axis = 0; reverse = ea.x < 0; }
+        else if (fy >= fx && fy >= fz) { axis = 1; reverse = ea.y < 0; }
+        else { axis = 2; reverse = ea.z < 0; }
+        // the negative-end voxel holds the link in direction 2*axis, the positive end in 2*axis+1
+        const int vneg = reverse ? v2 : v1, vpos = reverse ? v1 : v2;
+        const int dn = 2 * axis, dp = 2 * axis + 1;
+        if (((S.vfl[vneg] >> dn) & 1) || ((S.vfl[vpos] >> dp) & 1)) continue;
+        if (c.n_links >= S.nl_cap) continue;
+        const int l = c.n_links++;
+        const int nl = S.nl_cap;
+        S.lneg[l] = vneg; S.lpos[l] = vpos; S.lax[l] = (uint8_t)axis;
+        S.lmt[l] = (uint8_t)S.vm[S.vmat[v1]].attachLmat;
+        for (int k = 0; k < 9; k++) S.lst[(size_t)k * nl + l] = 0.0;
+        S.lsf[l] = 0.0f; S.lsf[nl + l] = 0.0f; S.lsf[2 * nl + l] = 0.0f;
+        S.lfl[l] = LF_SMALL;
+        S.lnew[l] = S.safety_guard;
+        S.vlink[6 * vneg + dn] = l;
+        S.vlink[6 * vpos + dp] = l;
+        // the new link's slots hold no force yet
+        for (int k = 0; k < 3; k++) {
+            S.sf[(size_t)(dn * 3 + k) * nv + vneg] = 0.0; S.sm[(size_t)(dn * 3 + k) * nv + vneg] = 0.0;
+            S.sf[(size_t)(dp * 3 + k) * nv + vpos] = 0.0; S.sm[(size_t)(dp * 3 + k) * nv + vpos] = 0.0;
+        }
+        S.ss[(size_t)dn * nv + vneg] = 0.0f;
+        S.ss[(size_t)dp * nv + vpos] = 0.0f;
+        uint32_t fa = S.vfl[vneg] | (1u << dn), fb = S.vfl[vpos] | (1u << dp);
+        if ((fa & VF_LINKS) == VF_LINKS) fa |= VF_INTERIOR;
+        if ((fb & VF_LINKS) == VF_LINKS) fb |= VF_INTERIOR;
+        S.vfl[vneg] = fa;
+        S.vfl[vpos] = fb;
+        drop_pair_contact(S, v1, v2);
+        drop_pair_contact(S, v2, v1);
+    }
+}
+
 // Second half of a step's VX3 signals, after every voxel's own signal work: each
 // voxel takes the signals its linked neighbours relayed this step, in direction order
 // (VX3_Voxel::propagateSignal, VX3_Voxel.cu:323-347, run from the receiving side).
@@ -960,7 +1119,6 @@ __global__ void __launch_bounds__(256) k_signals(const Sim* __restrict__ sims, C
         Ctl& c = ctl[w.sim];
         if (!c.sig_pending) continue;
         const Sim& S = sims[w.sim];
-        const double t = c.t_sig;
         const size_t nv = S.nv;
         for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) {
             const uint32_t f = S.vfl[v];
@@ -992,6 +1150,7 @@ __global__ void k_dt(const Sim* __restrict__ sims, Ctl* ctl, const int* __restri
     const Sim& S = sims[sim];
     float best = 0.0f;
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < S.nl; l += gridDim.x * blockDim.x) {
+        if (S.lfl[l] & LF_GONE) continue;   // free slots for links made at run time
         const int ng = S.lneg[l], pv = S.lpos[l];
         const LMat& m = S.lm[S.lmt[l]];
         const VMat& vN = S.vm[S.vmat[ng]];
@@ -1089,6 +1248,9 @@ inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, co
 inline void l_signals(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) {
     k_signals<<<g, b, 0, s>>>(sims, ctl, it, n, tk);
 }
+inline void l_attach(cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
+    if (n > 0) k_attach<<<n, 32, 0, s>>>(sims, ctl, slots, n);
+}
 inline void l_dt(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
     for (int k0 = 0; k0 < n; k0 += 65535) k_dt<<<dim3(g, (unsigned)std::min(65535, n - k0)), 256, 0, s>>>(sims, ctl, slots + k0, n - k0);
 }
@@ -1105,7 +1267,7 @@ inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int
     if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
 }
 inline KernelSet make_kernelset(const char* name) {
-    return KernelSet{name, l_links, l_contacts, l_voxels, l_signals, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
+    return KernelSet{name, l_links, l_contacts, l_voxels, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

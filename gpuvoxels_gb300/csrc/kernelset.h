@@ -15,6 +15,8 @@ struct KernelSet {
                    double* partials);
     // VX3 signals relayed between neighbours (after voxels, over the voxel items)
     void (*signals)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
+    // VX3 attachment: new links for this step's candidate pairs of n simulations (device slot list)
+    void (*attach)(cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
     // set-up of n newly uploaded simulations (device slot list), grid = blocks per simulation
     void (*dt)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
     void (*init_temp)(int grid, cudaStream_t s, const dev::Sim* sims, const int* slots, const float* initial, int n);

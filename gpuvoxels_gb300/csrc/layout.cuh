@@ -30,6 +30,7 @@ constexpr uint8_t LF_REMOVED = 64;        // VX3: removed with a voxel (left out
 constexpr uint32_t VF_FLOORC = 1u << 10;  // last step: the voxel touched the floor
 constexpr uint32_t VF_REMOVED = 1u << 11; // VX3: removed from the simulation (frozen, no links, no contacts)
 constexpr uint32_t VF_TGTHIT = 1u << 12;  // VX3: this step's contacts include a target voxel (non-target voxel)
+constexpr uint32_t VF_ATTACH = 1u << 13;  // VX3: enableAttach (every attach condition holds at the voxel)
 
 // sim flag bits
 constexpr int SF_FLOOR = 1, SF_COLLIDE = 2, SF_VARY = 4, SF_EXPAND = 8;
@@ -39,10 +40,11 @@ constexpr int SF_TARGETS = 128;                // target materials present (cont
 constexpr int SF_DETACH = 256;                 // failed links detach from their voxels
 constexpr int SF_REMOVE = 512;                 // secondary experiment: material removal, initial position reset
 constexpr int SF_FIXEDMAT = 1024;              // materials marked Fixed (their voxels never move)
-constexpr int SF_DYNSURF = SF_DETACH | SF_REMOVE;   // the surface set can change during the run
+constexpr int SF_ATTACH = 2048;                // touching sticky voxels may be joined by new links
+constexpr int SF_DYNSURF = SF_DETACH | SF_REMOVE | SF_ATTACH;   // the surface set can change during the run
 
 // VMat::vx3 bits
-constexpr int VM_TARGET = 1, VM_PACEMAKER = 2, VM_FIXED = 4;
+constexpr int VM_TARGET = 1, VM_PACEMAKER = 2, VM_FIXED = 4, VM_STICKY = 8;
 
 struct VMat {
     float E, nu, cte, mus, muk, eHat;
@@ -63,6 +65,8 @@ struct VMat {
     double cilia, ciliaOn, thermalOn;
     // signals: pacemaker period, relayed fraction, relay delay, refractory period; removal time
     double pmPeriod, sigDecay, sigDelay, sigInactive, removeAfter;
+    int32_t attachLmat;   // link material of a new link between two voxels of this material (-1: not sticky)
+    int32_t pad_vm;
 };
 
 // VX3 per-voxel signal state (SF_SIGNALS), one block of nv doubles each
@@ -115,9 +119,9 @@ struct Sim {
     double* sf;
     double* sm;
     float* ss;
-    // links
-    const int32_t *lneg, *lpos;
-    const uint8_t *lax, *lmt;
+    // links (written during the run only by VX3 attachment)
+    int32_t *lneg, *lpos;
+    uint8_t *lax, *lmt;
     double* lst;                // 9 blocks of nl: pos2 xyz, angle1v xyz, angle2v xyz
     float* lsf;                 // 3 blocks of nl: strain, maxStrain, strainOffset
     uint8_t* lfl;
@@ -136,13 +140,23 @@ struct Sim {
     const MathTree* ffield;     // x, y, z force-field formulas (SF_FFIELD)
     const double* shift_cilia;  // ShiftCiliaForce, 3 blocks of nv (SF_CILIA with SF_SIGNALS)
     double* sig;                // SG_FIELDS blocks of nv (SF_SIGNALS)
-    const int32_t* vlink;       // link per voxel direction, 6 per voxel, -1 if none (SF_SIGNALS, SF_REMOVE)
+    int32_t* vlink;             // link per voxel direction, 6 per voxel, -1 if none (SF_SIGNALS, SF_REMOVE, SF_ATTACH)
     const int32_t* targets;     // target voxel ids in index order (SF_TARGETS)
     int32_t n_targets;
     int32_t n_mats;
     double close_r;             // MaxDistInVoxelLengthsToCountAsPair * voxel size (0: closeness off)
     double reinit_after;        // ReinitializeInitialPositionAfterThisManySeconds (SF_REMOVE set: secondary experiment)
     double* init_pos;           // initial positions, 3 blocks of nv (secondary experiment)
+    // VX3 attachment (SF_ATTACH): link capacity (links nl..nl_cap-1 are created at run time),
+    // new-link damping counters, candidate pairs of this step, the attach conditions
+    int32_t nl_cap;
+    int32_t cand_cap;           // pairs
+    int32_t safety_guard;
+    int32_t attach_mask;        // bit k: AttachCondition k given (a missing one holds)
+    int32_t* lnew;              // per link: steps left with forces scaled by 0.01
+    int32_t* cand;              // 2 per candidate pair
+    int32_t* cpart;             // contact partners, kContactCap per voxel
+    const MathTree* attach_cond;   // 5 formulas
 };
 
 // Mutable per-simulation control block.
@@ -161,11 +175,12 @@ struct Ctl {
     // VX3 measures: target closeness and close pairs (at CoM samples), target contacts so far
     double closeness;
     int32_t num_close_pairs, hit_count;
-    double t_sig;               // currentTime of the step whose signal phase is pending
     int32_t sig_pending;        // 1 between a completed voxel update and its signal phase
     int32_t removed_mats;       // materials already removed (bit per palette index)
     int32_t reinit_done;        // initial centre of mass reset (secondary experiment)
-    int32_t pad_ctl2;
+    int32_t n_links;            // links in use (VX3 attachment appends)
+    int32_t n_cand;             // attachment candidates found this step
+    int32_t pad_ctl3;
     double init_com[3];         // initial centre of mass (host value, reset by the secondary experiment)
     MathTree stop;
 };

@@ -405,6 +405,7 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
             pm.is_target = get_i(mech, "isTarget", 0) != 0;
             pm.remove_after = get_d(mech, "RemoveFromSimulationAfterThisManySeconds", 0);
             pm.fixed = get_i(mech, "Fixed", 0) != 0;
+            pm.sticky = get_i(mech, "Sticky", 0) != 0;
             if (const XmlNode* ss = mech ? mech->child("SSData") : nullptr) {
                 if (const XmlNode* se = ss->child("StrainData"))
                     for (auto* c : se->children_named("Strain")) pm.strain_data.push_back(atof_s(c->text));
@@ -514,6 +515,17 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     d->enable_detach = ptree_bool(*root, "VXA.Simulator.AttachDetach.EnableDetach", false);
     d->secondary_experiment = (int)ptree_num(*root, "VXA.Simulator.SecondaryExperiment", 0);
     d->reinit_initial_after = ptree_num(*root, "VXA.Simulator.ReinitializeInitialPositionAfterThisManySeconds", 0.0);
+    d->enable_attach = ptree_bool(*root, "VXA.Simulator.AttachDetach.EnableAttach", false);
+    d->safety_guard = (int)ptree_num(*root, "VXA.Simulator.AttachDetach.SafetyGuard", 500);
+    d->attach_cond_mask = 0;
+    for (int k = 0; k < 5; k++) {
+        const std::string path = "VXA.Simulator.AttachDetach.AttachCondition.Condition_" + std::to_string(k);
+        if (const XmlNode* n = root->path(path.c_str())) {
+            parse_mathtree(n, &d->attach_cond[k]);
+            if (!d->attach_cond[k].valid) { *err = "invalid attach condition formula"; return false; }
+            d->attach_cond_mask |= 1 << k;
+        }
+    }
     const char* ff_paths[3] = {"VXA.Simulator.ForceField.x_forcefield", "VXA.Simulator.ForceField.y_forcefield",
                                "VXA.Simulator.ForceField.z_forcefield"};
     for (int k = 0; k < 3; k++) {
@@ -797,6 +809,24 @@ bool build_world(const SimDesc& d, SimWorld* w, std::string* err) {
             w->link_mat.push_back((uint8_t)lmi);
             w->vox_links[(size_t)i * 6 + dir] = li;
             w->vox_links[(size_t)b * 6 + (dir - dir % 2 + (dir + 1) % 2)] = li;
+        }
+    }
+    // VX3 attachment: a new link between two voxels of one sticky material takes the combined
+    // material of that material with itself (VX3_VoxelyzeKernel::combinedMaterial, :516-528)
+    w->loaded_lmats = (int)w->lmats.size();
+    w->attach_lmat.assign(w->vmats.size(), -1);
+    if (d.enable_attach) {
+        for (int m = 0; m < (int)d.mats.size(); m++) {
+            if (!d.mats[m].sticky) continue;
+            int lmi = -1;
+            for (int k = 0; k < (int)lm_pairs.size(); k++)
+                if (lm_pairs[k].first == m && lm_pairs[k].second == m) { lmi = k; break; }
+            if (lmi < 0) {
+                lmi = (int)lm_pairs.size();
+                lm_pairs.emplace_back(m, m);
+                w->lmats.push_back(make_link_material(w->vmats[m], w->vmats[m], m, m));
+            }
+            w->attach_lmat[m] = lmi;
         }
     }
     if (w->lmats.size() > 255 || w->vmats.size() > 255) { *err = "too many materials"; return false; }

@@ -33,8 +33,10 @@ struct PaletteMaterial {
     // material's voxels after a time (SecondaryExperiment, VX_Object.cpp:1427)
     int is_target = 0;
     double remove_after = 0;
-    // VX3 Fixed materials: their voxels never move (VX_Object.cpp:1435)
+    // VX3 Fixed materials: their voxels never move (VX_Object.cpp:1435); Sticky materials'
+    // touching voxels may be joined by new links (:1436)
     int fixed = 0;
+    int sticky = 0;
 };
 
 struct External {
@@ -84,6 +86,12 @@ struct SimDesc {
     int enable_detach = 0;
     int secondary_experiment = 0;
     double reinit_initial_after = 0;
+    // VX3 attachment (VXA.Simulator.AttachDetach: EnableAttach, SafetyGuard, and the voxel
+    // conditions AttachCondition/Condition_0..4; bit k of attach_cond_mask: condition k given)
+    int enable_attach = 0;
+    int safety_guard = 500;
+    MathTree attach_cond[5];
+    int attach_cond_mask = 0;
 };
 
 // Parses a base VXA plus an optional VXD (whose children carrying replace="VXA.a.b"
@@ -122,6 +130,8 @@ struct SimWorld {
     std::vector<uint8_t> vox_interior;               // all 6 links present
     std::vector<int32_t> vox_ext;                    // index into desc.externals or -1
     int surface_count = 0;
+    std::vector<int32_t> attach_lmat;                // per voxel material: link material of a new link between two of its voxels, or -1
+    int loaded_lmats = 0;                            // link materials of the loaded links (attachment's follow them)
 };
 
 bool build_world(const SimDesc& d, SimWorld* w, std::string* err);

@@ -136,6 +136,10 @@ int vx3_get_link_state(vx3_ctx* ctx, vx3_sim_id id, double* d9, float* f3, int32
  * packmakerNextPulse (VX3_Voxel members, VX3/VX3_Voxel.h:304-309; zeros without EnableSignals).
  * Either pointer may be NULL. */
 int vx3_get_extras(vx3_ctx* ctx, vx3_sim_id id, double* measures4, double* signals6);
+/* Every link in use, the loaded ones first, then those VX3 attachment created during the run
+ * (VX3_VoxelyzeKernel::d_v_links, VX3/VX3_VoxelyzeKernel.cuh): *n_links, and for the first
+ * `max` links negative-end voxel, positive-end voxel, axis and flag byte (ends4, may be NULL). */
+int vx3_get_links(vx3_ctx* ctx, vx3_sim_id id, int32_t* n_links, int32_t* ends4, int max);
 
 /* Replaces the .history stream the reference prints from its simulation loop when the VXA
  * sets Simulator/RecordHistory/RecordStepSize (VX3/VX3_SimulationManager.cu:40-114): settings

@@ -1,6 +1,6 @@
 """CPU restatement of the VX3 extras that have no counterpart in the reference's CPU
-path: voxel signals, target closeness and target contacts.  TEST INFRASTRUCTURE:
-only the tests use it, as the checker of the engine's results.
+path: voxel signals, target closeness and run-time attachment of touching voxels.
+TEST INFRASTRUCTURE: only the tests use it, as the checker of the engine's results.
 
 Signals follow VX3_Voxel's signal routines (Voxelyze3/src/VX3/VX3_Voxel.cu:271-347).
 The reference runs them inside the parallel voxel kernel and writes into the
@@ -11,8 +11,12 @@ due signal, pacemaker pulse, local decay, in the reference's order), then each v
 takes the signals its linked neighbours relayed, in link-direction order X+, X-, Y+,
 Y-, Z+, Z-.  A forced signal from touching a target voxel is taken before the step.
 
+Attachment is likewise racy in the reference (many threads create links at once);
+the engine and this restatement create them one pair at a time in increasing pair
+order.
+
 Pinning: the reference's GPU code does not build with this toolchain and its CPU path
-has no signals, so this restatement is pinned to VX3's source text, not to outputs.
+has neither feature, so this restatement is pinned to VX3's source text, not to outputs.
 """
 import math
 
@@ -118,3 +122,68 @@ def target_closeness(pos, targets, max_dist_voxels, vox_size):
                 pairs += 1
             ret += 1 / dist
     return ret, pairs
+
+
+def _qrotinv(q, f):
+    """Quat3D::RotateVec3DInv (Voxelyze3/src/old/Quat3D.h:192-199); q = (w, x, y, z)."""
+    w, x, y, z = (float(c) for c in q)
+    fx, fy, fz = (float(c) for c in f)
+    tw = x * fx + y * fy + z * fz
+    tx = w * fx - y * fz + z * fy
+    ty = w * fy + x * fz - z * fx
+    tz = w * fz - x * fy + y * fx
+    return (tw * x + tx * w + ty * z - tz * y, tw * y - tx * z + ty * w + tz * x, tw * z + tx * y - ty * x + tz * w)
+
+
+def attach_links(pos, orient, links, pairs, n_voxels):
+    """New links VX3 attachment makes in one step (handle_collision_attachment,
+    Voxelyze3/src/VX3/VX3_VoxelyzeKernel.cu:729-827), in the engine's deterministic order.
+
+    links: current links as (neg, pos, axis) rows (gone links left out); pairs: candidate
+    pairs (a < b) that touch and pass the material tests.  Returns the new links as
+    (neg, pos, axis) in creation order; `links` is not modified."""
+    slot = [[-1] * 6 for _ in range(n_voxels)]
+    lk = [list(map(int, l)) for l in links]
+    for i, (n, p, ax) in enumerate(lk):
+        slot[n][2 * ax] = i
+        slot[p][2 * ax + 1] = i
+
+    def within(a, b, depth):
+        # is_neighbor (VX3_VoxelyzeKernel.cu:651-680)
+        def rec(v, incoming, d):
+            if v == b:
+                return True
+            if d <= 0:
+                return False
+            for k in range(6):
+                l = slot[v][k]
+                if l >= 0 and l != incoming:
+                    n, p, _ = lk[l]
+                    if rec(p if n == v else n, l, d - 1):
+                        return True
+            return False
+        return rec(a, -1, depth)
+
+    made = []
+    for a, b in sorted(pairs):
+        v1, v2 = b, a                                   # voxel1: the later voxel of the pair
+        if within(v1, v2, 5):
+            continue
+        e = [float(pos[v1][k]) - float(pos[v2][k]) for k in range(3)]
+        ea = _qrotinv(orient[v1], (-e[0], -e[1], -e[2]))
+        f = [abs(c) for c in ea]
+        if f[0] >= f[1] and f[0] >= f[2]:
+            axis = 0
+        elif f[1] >= f[0] and f[1] >= f[2]:
+            axis = 1
+        else:
+            axis = 2
+        reverse = ea[axis] < 0
+        vneg, vpos = (v2, v1) if reverse else (v1, v2)
+        if slot[vneg][2 * axis] >= 0 or slot[vpos][2 * axis + 1] >= 0:
+            continue
+        lk.append([vneg, vpos, axis])
+        slot[vneg][2 * axis] = len(lk) - 1
+        slot[vpos][2 * axis + 1] = len(lk) - 1
+        made.append((vneg, vpos, axis))
+    return made

@@ -119,9 +119,11 @@ def sample_worlds():
         if "<Damping>" not in xml:
             i = xml.index("<Simulator>") + len("<Simulator>")
             xml = xml[:i] + DAMPING_DEFAULTS + xml[i:]
-        # cilia are a VX3-only force the reference's CPU path does not apply: switched off so that the
-        # reference's output is the expected one (the cilia themselves are tested on their own)
-        xml = re.sub(r"(<EnableCilia(?:\s[^>]*)?>)\s*1\s*(</EnableCilia>)", r"\g<1>0\g<2>", xml)
+        # cilia, run-time attachment and detachment are VX3-only behaviour the reference's CPU path
+        # does not have: switched off so that the reference's output is the expected one (they are
+        # tested on their own)
+        for key in ("EnableCilia", "EnableAttach", "EnableDetach"):
+            xml = re.sub(r"(<%s(?:\s[^>]*)?>)\s*1\s*(</%s>)" % (key, key), r"\g<1>0\g<2>", xml)
         w[name] = dict(vxa=xml, ext=[], snaps=snaps)
     return w
 

@@ -349,3 +349,95 @@ def test_fixed_material_voxels_never_move(ctx):
         assert vs["pos"][3, 2] < p0[3, 2] - 1e-5                    # the free end sags
     finally:
         ctx.free(sim)
+
+
+def _sticky_blocks(attach=True, cond="", same_material=True, sticky=True):
+    # a 3 x 3 x 2 block falling onto another, two voxel layers apart, one sticky material
+    grid = np.zeros((6, 3, 3), np.int32)
+    grid[0:2] = 1
+    grid[4:6] = 1 if same_material else 2
+    mech = "<Sticky>1</Sticky>" if sticky else ""
+    mats = [_mat(E=1e5, mech=mech), _mat(E=1e5, mech=mech)]
+    vxa = _world(grid, mats, gravity=-9.81, floor=True, collision=True, damping=(0.1, 1.0, 0.0))
+    ad = f"<EnableAttach>{1 if attach else 0}</EnableAttach><SafetyGuard>50</SafetyGuard>"
+    if cond:
+        ad += f"<AttachCondition><Condition_0>{cond}</Condition_0></AttachCondition>"
+    return vxa.replace("<EnableAttach>0</EnableAttach>", ad, 1)
+
+
+def _touch_set(st):
+    pos = st["pos"]
+    n = len(pos)
+    b = 0.01 * 1.0
+    bsa = (b + b + b) / 3.0
+    nom_dist = np.float32((bsa + bsa) * float(np.float32(0.625)))
+    out = set()
+    for a in range(n):
+        for c in range(a + 1, n):
+            o = [np.float32(pos[c][k] - pos[a][k]) for k in range(3)]
+            ln = np.sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2], dtype=np.float32)
+            if np.float32(nom_dist - ln) > 0:
+                out.add((a, c))
+    return out
+
+
+def test_attachment_joins_touching_sticky_voxels(ctx):
+    from oracle.vx3_extras import attach_links
+    vxa = _sticky_blocks()
+    top = g.inspect_vxa(vxa)
+    nv, nl0 = top["counts"]["voxels"], top["counts"]["links"]
+    lower = top["voxels"][:, 2] < 3
+    sim = ctx.load_vxa(vxa)
+    try:
+        made_total = 0
+        for k in range(1500):
+            st = ctx.voxel_state(sim)
+            links = ctx.links(sim)
+            touch = _touch_set(st)
+            # pairs within 5 links of the loaded topology (same block) never reach the contact set
+            cands = [(a, b) for (a, b) in touch if lower[a] != lower[b]]
+            cur = [(n, p, ax) for n, p, ax, fl in links if not fl & 32]
+            want = attach_links(st["pos"], st["orient"], cur, cands, nv)
+            ctx.step(sim, 1)
+            after = ctx.links(sim)
+            got = [tuple(int(x) for x in r[:3]) for r in after[len(links):]]
+            assert got == want, f"step {k}"
+            made_total += len(got)
+            if made_total and k > 600:
+                break
+        assert made_total > 0
+        after = ctx.links(sim)
+        fl = ctx.voxel_state(sim)["flags"]
+        for n, p, ax, lf in after[nl0:]:
+            assert lower[n] != lower[p]                       # new links join the two blocks
+            assert (fl[n] >> (2 * ax)) & 1 and (fl[p] >> (2 * ax + 1)) & 1
+    finally:
+        ctx.free(sim)
+
+
+@pytest.mark.parametrize("case", ["off", "condition_false", "not_sticky", "other_material"])
+def test_attachment_needs_every_condition(ctx, case):
+    kw = dict(off=dict(attach=False), condition_false=dict(cond="<mtCONST>-1</mtCONST>"),
+              not_sticky=dict(sticky=False), other_material=dict(same_material=False))[case]
+    vxa = _sticky_blocks(**kw)
+    nl0 = g.inspect_vxa(vxa)["counts"]["links"]
+    sim = ctx.load_vxa(vxa)
+    try:
+        ctx.step(sim, 1500)
+        assert len(ctx.links(sim)) == nl0
+    finally:
+        ctx.free(sim)
+
+
+def test_attachment_is_deterministic(ctx):
+    vxa = _sticky_blocks()
+    res = []
+    for _ in range(2):
+        sim = ctx.load_vxa(vxa)
+        try:
+            ctx.step(sim, 1200)
+            res.append((ctx.links(sim).copy(), ctx.voxel_state(sim)["pos"].copy()))
+        finally:
+            ctx.free(sim)
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    assert len(res[0][0]) > g.inspect_vxa(vxa)["counts"]["links"]
