@@ -8,6 +8,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <thread>
@@ -131,7 +132,10 @@ public:
     double* d_partials_ = nullptr;
     double* d_com4_ = nullptr;
     // tuning
-    int block_links_ = 256, block_voxels_ = 256, items_links_ = 256, items_voxels_ = 256, graph_steps_ = 64;
+    int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 256, graph_steps_ = 64;
+    // link binning: regrouped every bin_every_ steps (the first step after a batch change always)
+    int bin_every_ = 1, bin_phase_ = 0;
+    bool bins_dirty_ = true;
     int sm_count_ = 152;
     int profiling_ = 0;
     KernelSet ks_ = kernelset_exact();
@@ -146,7 +150,14 @@ public:
     int n_link_items_ = 0, n_contact_items_ = 0, n_vox_items_ = 0;
     bool any_collide_ = false;
     bool any_signals_ = false;
+    // batch-wide link binning (k_link_hist / k_link_scan / k_link_scatter)
+    int* d_link_hist_ = nullptr;
+    int* d_link_base_ = nullptr;
+    int* d_link_total_ = nullptr;
+    int2* d_link_perm_ = nullptr;
+    size_t cap_bins_ = 0, cap_perm_ = 0;
     int n_attach_ = 0, cap_attach_ = 0;     // simulations with VX3 attachment in the batch
+    int64_t graph_launches_ = 0;            // kernels one replay of the captured graph launches
     int* d_attach_slots_ = nullptr;
     std::vector<int> attach_slots_host_;
     cudaGraphExec_t graph_ = nullptr;
@@ -177,6 +188,7 @@ public:
         cudaFree(d_gather_);
         cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_partials_); cudaFree(d_com4_);
         cudaFree(d_attach_slots_);
+        cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
         cudaFree(arena_base_);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
@@ -188,6 +200,8 @@ public:
         device_ = device;
         CK(cudaSetDevice(device));
         CK(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
+        // GVX_LINK_BIN_EVERY: steps between regroupings of the links (tuning knob, default 1)
+        if (const char* e = getenv("GVX_LINK_BIN_EVERY")) bin_every_ = std::max(1, atoi(e));
         CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
         CK(cudaEventCreate(&ev0_));
         CK(cudaEventCreate(&ev1_));
@@ -804,6 +818,24 @@ public:
             for (int b = 0; b < nl; b += items_links_) items.push_back({s, b, std::min(nl, b + items_links_), 0});
         }
         n_link_items_ = (int)items.size();
+        bins_dirty_ = true;
+        size_t links_total = 0;
+        for (int s : slots) links_total += (size_t)link_capacity(slot_owner_[s]->w);
+        const size_t bins = (size_t)std::max(1, n_link_items_) * dev::kOrderKeysBins;
+        if (bins > cap_bins_ || !d_link_total_) {
+            cudaFree(d_link_hist_); cudaFree(d_link_base_);
+            d_link_hist_ = d_link_base_ = nullptr;
+            cap_bins_ = std::max(bins, 2 * cap_bins_);
+            CK(cudaMalloc(&d_link_hist_, sizeof(int) * cap_bins_));
+            CK(cudaMalloc(&d_link_base_, sizeof(int) * cap_bins_));
+            if (!d_link_total_) CK(cudaMalloc(&d_link_total_, sizeof(int)));
+        }
+        if (std::max<size_t>(1, links_total) > cap_perm_) {
+            cudaFree(d_link_perm_);
+            d_link_perm_ = nullptr;
+            cap_perm_ = std::max(std::max<size_t>(1, links_total), 2 * cap_perm_);
+            CK(cudaMalloc(&d_link_perm_, sizeof(int2) * cap_perm_));
+        }
         for (int s : slots) {
             SimRec* r = slot_owner_[s];
             if (r->w.desc.enable_signals) any_signals_ = true;
@@ -836,6 +868,7 @@ public:
         n_attach_ = (int)attach_slots.size();
         if (n_attach_ > cap_attach_) {
             cudaFree(d_attach_slots_);
+        cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
             cap_attach_ = std::max(n_attach_, 2 * cap_attach_);
             CK(cudaMalloc(&d_attach_slots_, sizeof(int) * cap_attach_));
         }
@@ -860,14 +893,24 @@ public:
         return std::max(1, std::min(n_items, sm_count_ * per_sm));
     }
 
-    int launches_per_step() const { return 2 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0); }
-
-    void launch_step(cudaStream_t st, bool prof) {
+    // One step of the batch; returns the number of kernels it launched.
+    int launch_step(cudaStream_t st, bool prof) {
+        int launched = 2 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
         const dev::Item* li = d_items_;
         const dev::Item* ci = d_items_ + n_link_items_;
         const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
+        if (bins_dirty_ || bin_phase_ % bin_every_ == 0) {
+            // windows of about 16k links: a window's link state stays in L2 while its key groups run
+            const int win = std::max(1, 16384 / std::max(1, items_links_));
+            ks_.link_bins(std::max(1, std::min(n_link_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, li, n_link_items_, win, d_link_hist_,
+                          d_link_base_, d_link_total_, d_link_perm_);
+            bins_dirty_ = false;
+            bin_phase_ = 0;
+            launched += 3;
+        }
+        bin_phase_++;
         if (prof) cudaEventRecord(evk_[0], st);
-        ks_.links(grid_for(n_link_items_, block_links_), block_links_, st, d_sims_, d_ctl_, li, n_link_items_, d_tickets_);
+        ks_.links(sm_count_ * 2 * std::max(1, 256 / block_links_), block_links_, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_, d_tickets_);
         if (prof) cudaEventRecord(evk_[1], st);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
@@ -876,6 +919,7 @@ public:
                    d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
         if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
         if (prof) cudaEventRecord(evk_[3], st);
+        return launched;
     }
 
     // Marks the slots running towards their target step counts (no_stop: vx3_step's fixed
@@ -958,11 +1002,11 @@ public:
                 std::vector<int> one{rs[i]->slot};
                 if (int e = build_items(one, err)) return e;
                 if (exact_steps_ >= 0) {
-                    for (int64_t k = 0; k < exact_steps_; k++) { launch_step(stream_, false); timing_.launches += launches_per_step(); }
+                    for (int64_t k = 0; k < exact_steps_; k++) { timing_.launches += launch_step(stream_, false); }
                     continue;
                 }
                 for (;;) {
-                    for (int k = 0; k < 16; k++) { launch_step(stream_, false); timing_.launches += launches_per_step(); }
+                    for (int k = 0; k < 16; k++) { timing_.launches += launch_step(stream_, false); }
                     dev::Ctl c;
                     if (int e = read_ctl(rs[i]->slot, &c, err)) return e;
                     if (c.status != SIM_RUNNING) break;
@@ -981,24 +1025,24 @@ public:
             if (!graph_) {
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-                for (int k = 0; k < graph_steps_; k++) launch_step(stream_, false);
+                bins_dirty_ = true;   // every replay starts by regrouping the links
+                graph_launches_ = 0;
+                for (int k = 0; k < graph_steps_; k++) graph_launches_ += launch_step(stream_, false);
                 CK(cudaStreamEndCapture(stream_, &g));
                 CK(cudaGraphInstantiate(&graph_, g, 0));
                 cudaGraphDestroy(g);
                 graph_len_ = graph_steps_;
             }
-            const int per_step = launches_per_step();
             if (exact_steps_ >= 0) {
                 // a known step count: whole graphs, then single steps for the remainder, no polling
                 int64_t left = exact_steps_;
                 while (left > 0) {
                     if (!profiling_ && left >= graph_len_) {
                         CK(cudaGraphLaunch(graph_, stream_));
-                        timing_.launches += (int64_t)graph_len_ * per_step;
+                        timing_.launches += graph_launches_;
                         left -= graph_len_;
                     } else {
-                        launch_step(stream_, profiling_ != 0);
-                        timing_.launches += per_step;
+                        timing_.launches += launch_step(stream_, profiling_ != 0);
                         left -= 1;
                     }
                 }
@@ -1008,11 +1052,10 @@ public:
                 std::vector<int32_t> st((size_t)(hi - lo + 1));
                 for (;;) {
                     if (profiling_) {
-                        launch_step(stream_, true);
-                        timing_.launches += per_step;
+                        timing_.launches += launch_step(stream_, true);
                     } else {
                         CK(cudaGraphLaunch(graph_, stream_));
-                        timing_.launches += (int64_t)graph_len_ * per_step;
+                        timing_.launches += graph_launches_;
                     }
                     // one strided copy of every status word, then a single synchronisation
                     CK(cudaMemcpy2DAsync(st.data(), sizeof(int32_t), &d_ctl_[lo].status, sizeof(dev::Ctl), sizeof(int32_t),
@@ -1250,14 +1293,16 @@ public:
             if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-            for (int s = 0; s < k; s++) launch_step(stream_, false);
+            bins_dirty_ = true;
+            graph_launches_ = 0;
+            for (int s = 0; s < k; s++) graph_launches_ += launch_step(stream_, false);
             CK(cudaStreamEndCapture(stream_, &g));
             CK(cudaGraphInstantiate(&graph_, g, 0));
             cudaGraphDestroy(g);
             graph_len_ = k;
         }
         CK(cudaGraphLaunch(graph_, stream_));
-        timing_.launches += (int64_t)k * (launches_per_step());
+        timing_.launches += graph_launches_;
         std::vector<int32_t> st(active_.size());
         {
             int lo = INT32_MAX, hi = -1;

@@ -237,7 +237,7 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
 // deterministic.  The order never changes results: every link writes only its own
 // state and its two direction slots, and voxel work is per voxel.
 constexpr int kOrderMax = 1024;   // elements per item that are reordered (larger items run in index order)
-constexpr int kOrderKeys = 10;
+constexpr int kOrderKeys = kOrderKeysBins;
 
 // perm[0..n) = element indices grouped by key(j) in increasing key order; wc holds
 // kOrderKeys x 8 warp counts.  Every thread of the block must call it.
@@ -289,14 +289,15 @@ __device__ __forceinline__ void order_by_key(int n, KeyFn key, int* perm, int* w
 
 // Link key: small-angle mode, then within each mode which rotation branches were taken
 // (small links: angle2's rotation-vector branch; large links: that, angle1's, and
-// FromAngleToPosX's).  10 groups.
+// FromAngleToPosX's).  10 groups, the costliest first (large links taking every
+// acos/sincos branch are key 0, plain small links key 9).
 struct LinkKey {
     const uint8_t* lfl;
     int begin;
     __device__ int operator()(int j) const {
         const uint8_t f = lfl[begin + j];
-        if (f & LF_SMALL) return 8 | ((f & LF_WIDE2) ? 1 : 0);
-        return ((f & LF_WIDE1) ? 4 : 0) | ((f & LF_ACOS1) ? 2 : 0) | ((f & LF_WIDE2) ? 1 : 0);
+        if (f & LF_SMALL) return (f & LF_WIDE2) ? 8 : 9;
+        return 7 - (((f & LF_WIDE1) ? 4 : 0) | ((f & LF_ACOS1) ? 2 : 0) | ((f & LF_WIDE2) ? 1 : 0));
     }
 };
 
@@ -309,32 +310,142 @@ struct LinkKey {
 #define GVX_VOXELS_MIN_BLOCKS 2
 #endif
 
-// Blocks claim work items (a link range of one simulation) and order each by key
-// across all of the block's warps.  (Per-warp items without block barriers were
-// measured slower: ordering 128 links per warp groups the paths less well than
-// 256 per block, and FP64 lane use fell from 84 % to 80 %.)
-__global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
-    __shared__ int s_item;
-    __shared__ int s_perm[kOrderMax];
-    __shared__ int s_warp[kOrderKeys * 8];
-    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; }
-    for (;;) {
-        const int it = claim(&tickets[0], &s_item);
-        if (it >= n_items) break;
+// ---------------------------------------------------------------- link binning
+// Every few steps the links of every running simulation are grouped by key within
+// windows of consecutive work items (three small passes: key counts per item, their
+// exclusive scan, a stable scatter of (simulation, link) pairs); keys change slowly,
+// so the grouping is reused for the steps in between.  Every
+// warp of k_links then runs one code path, and warps take 32-link chunks from one
+// queue in window order: no block barriers, no tail of uneven work items, and the
+// link state of a window (a few MB) stays in L2 while its key groups are processed.
+// (Earlier forms ordered each 256-link item inside its block, between block
+// barriers: warps of cheap small-angle links waited for warps of costly large-angle
+// ones.  Grouping across the whole batch at once made every key group a separate
+// pass over all link state and tripled k_links' DRAM traffic.)
+__global__ void __launch_bounds__(256) k_link_hist(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                   int n_items, int* hist) {
+    __shared__ int wc[kOrderKeys * 8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const Item w = items[it];
-        Ctl& c = ctl[w.sim];
-        if (c.status != 1) continue;
-        const Sim& S = sims[w.sim];
-        const float dt = c.dt;
-        bool div = false;
+        const bool run = ctl[w.sim].status == 1;
+        const LinkKey key{sims[w.sim].lfl, w.begin};
         const int n = w.end - w.begin;
-        if (n <= kOrderMax) {
-            order_by_key(n, LinkKey{S.lfl, w.begin}, s_perm, s_warp);
-            for (int k = threadIdx.x; k < n; k += blockDim.x) link_update(S, w.begin + s_perm[k], dt, &div);
-        } else {
-            for (int l = w.begin + threadIdx.x; l < w.end; l += blockDim.x) link_update(S, l, dt, &div);
+        int cnt = 0;   // thread k < kOrderKeys: links of key k
+        for (int j0 = 0; j0 < n; j0 += blockDim.x) {
+            const int j = j0 + threadIdx.x;
+            const int kj = (run && j < n) ? key(j) : -1;
+#pragma unroll
+            for (int k = 0; k < kOrderKeys; k++) {
+                const unsigned b = __ballot_sync(0xffffffffu, kj == k);
+                if (lane == 0) wc[k * 8 + wid] = __popc(b);
+            }
+            __syncthreads();
+            if (threadIdx.x < kOrderKeys)
+                for (int q = 0; q < nw; q++) cnt += wc[threadIdx.x * 8 + q];
+            __syncthreads();
         }
-        if (div) c.diverged = 1;
+        if (threadIdx.x < kOrderKeys) hist[(size_t)it * kOrderKeys + threadIdx.x] = cnt;
+    }
+}
+
+// One block: an exclusive scan of the per-item key counts taken window by window, key
+// by key, item by item, so base[item][key] = links of earlier windows + links of
+// smaller keys in the window + links of that key in earlier items of the window.
+// Each thread scans a contiguous run of that order; the runs are joined by a block scan.
+__global__ void __launch_bounds__(1024) k_link_scan(const int* __restrict__ hist, int* base, int n_items, int win, int* total) {
+    __shared__ int s_sum[1024];
+    const int n_win = (n_items + win - 1) / win;
+    const int N = n_win * win * kOrderKeys;
+    const int per = (N + blockDim.x - 1) / blockDim.x;
+    const int e0 = min(N, (int)threadIdx.x * per), e1 = min(N, e0 + per);
+    auto item_of = [win](int e, int* k) {
+        const int w = e / (win * kOrderKeys), r = e - w * (win * kOrderKeys);
+        *k = r / win;
+        return w * win + (r - *k * win);
+    };
+    int sum = 0;
+    for (int e = e0; e < e1; e++) {
+        int k;
+        const int it = item_of(e, &k);
+        if (it < n_items) sum += hist[(size_t)it * kOrderKeys + k];
+    }
+    s_sum[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {   // inclusive scan of the runs' sums
+        const int v = (int)threadIdx.x >= off ? s_sum[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_sum[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = threadIdx.x ? s_sum[threadIdx.x - 1] : 0;
+    for (int e = e0; e < e1; e++) {
+        int k;
+        const int it = item_of(e, &k);
+        if (it < n_items) {
+            base[(size_t)it * kOrderKeys + k] = run;
+            run += hist[(size_t)it * kOrderKeys + k];
+        }
+    }
+    if (threadIdx.x == blockDim.x - 1) *total = s_sum[blockDim.x - 1];
+}
+
+__global__ void __launch_bounds__(256) k_link_scatter(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                      int n_items, const int* __restrict__ base, int2* perm) {
+    __shared__ int wc[kOrderKeys * 8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const Item w = items[it];
+        if (ctl[w.sim].status != 1) continue;   // the same for the whole block
+        const LinkKey key{sims[w.sim].lfl, w.begin};
+        int start[kOrderKeys];
+        for (int k = 0; k < kOrderKeys; k++) start[k] = base[(size_t)it * kOrderKeys + k];
+        const int n = w.end - w.begin;
+        for (int j0 = 0; j0 < n; j0 += blockDim.x) {
+            const int j = j0 + threadIdx.x;
+            const int kj = j < n ? key(j) : -1;
+            unsigned mine = 0;
+#pragma unroll
+            for (int k = 0; k < kOrderKeys; k++) {
+                const unsigned b = __ballot_sync(0xffffffffu, kj == k);
+                if (kj == k) mine = b;
+                if (lane == 0) wc[k * 8 + wid] = __popc(b);
+            }
+            __syncthreads();
+            if (kj >= 0) {
+                int p = start[kj] + __popc(mine & below);
+                for (int q = 0; q < wid; q++) p += wc[kj * 8 + q];
+                perm[p] = make_int2(w.sim, w.begin + j);
+            }
+            for (int k = 0; k < kOrderKeys; k++)
+                for (int q = 0; q < nw; q++) start[k] += wc[k * 8 + q];
+            __syncthreads();
+        }
+    }
+}
+
+// Warps take 32-link chunks of the binned list (one atomic per chunk); each lane
+// updates one link of whatever simulation it belongs to.
+__global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
+                                                                     const int* __restrict__ total, int* tickets) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; }
+    const int n = *total;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(&tickets[0], 1);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        const int k = chunk * 32 + lane;
+        if (chunk * 32 >= n) break;
+        if (k < n) {
+            const int2 e = __ldg(perm + k);
+            Ctl& c = ctl[e.x];
+            if (c.status != 1) continue;   // stopped since the grouping was made
+            bool div = false;
+            link_update(sims[e.x], e.y, c.dt, &div);
+            if (div) c.diverged = 1;
+        }
     }
 }
 
@@ -1240,7 +1351,15 @@ __global__ void k_com(const Sim* __restrict__ sims, int sim, double* out4) {
 // ---------------------------------------------------------------- launch table
 namespace gvx {
 namespace GVX_KNS {
-inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_links<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
+inline void l_link_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int win, int* hist, int* base,
+                        int* total, int2* perm) {
+    k_link_hist<<<g, 256, 0, s>>>(sims, ctl, it, n, hist);
+    k_link_scan<<<1, 1024, 0, s>>>(hist, base, n, win, total);
+    k_link_scatter<<<g, 256, 0, s>>>(sims, ctl, it, n, base, perm);
+}
+inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int* tk) {
+    k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, tk);
+}
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk, double* p) {
     k_voxels<<<g, b, 0, s>>>(sims, ctl, it, n, tk, p);
@@ -1267,7 +1386,7 @@ inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int
     if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
 }
 inline KernelSet make_kernelset(const char* name) {
-    return KernelSet{name, l_links, l_contacts, l_voxels, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
+    return KernelSet{name, l_link_bins, l_links, l_contacts, l_voxels, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

@@ -9,7 +9,11 @@ namespace gvx {
 
 struct KernelSet {
     const char* name;
-    void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
+    // groups the links of the running simulations by key across the batch (hist, base: per
+    // link item and key; total: links listed; perm: (simulation, link) pairs)
+    void (*link_bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int win, int* hist,
+                      int* base, int* total, int2* perm);
+    void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int* tickets);
     void (*contacts)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
     void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets,
                    double* partials);

@@ -12,6 +12,7 @@ namespace dev {
 // ---------------------------------------------------------------- layouts
 constexpr int kContactCap = 32;       // contacts kept per voxel per step
 constexpr int kReachWords = 8;        // 231 offsets of the L1 ball of radius 5 -> 8 x 32 bits
+constexpr int kOrderKeysBins = 10;    // link ordering keys (the step kernels' kOrderKeys)
 
 // voxel flag bits
 constexpr uint32_t VF_LINKS = 0x3Fu;      // bits 0..5: link present in direction d
