@@ -129,10 +129,9 @@ public:
     int* d_tickets_ = nullptr;
     dev::Item* d_items_ = nullptr;
     int cap_items_ = 0;
-    double* d_partials_ = nullptr;
     double* d_com4_ = nullptr;
     // tuning
-    int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 256, graph_steps_ = 64;
+    int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 1024, graph_steps_ = 64;
     // link binning: regrouped every bin_every_ steps (the first step after a batch change always)
     int bin_every_ = 1, bin_phase_ = 0;
     bool bins_dirty_ = true;
@@ -150,12 +149,21 @@ public:
     int n_link_items_ = 0, n_contact_items_ = 0, n_vox_items_ = 0;
     bool any_collide_ = false;
     bool any_signals_ = false;
-    // batch-wide link binning (k_link_hist / k_link_scan / k_link_scatter)
+    // batch-wide grouping of links by key (k_bin_hist / k_bin_scan / k_bin_scatter)
     int* d_link_hist_ = nullptr;
     int* d_link_base_ = nullptr;
     int* d_link_total_ = nullptr;
     int2* d_link_perm_ = nullptr;
     size_t cap_bins_ = 0, cap_perm_ = 0;
+    // the same for the voxels, and the batch's slot list for k_sim_end
+    int* d_vox_hist_ = nullptr;
+    int* d_vox_base_ = nullptr;
+    int* d_vox_total_ = nullptr;
+    int2* d_vox_perm_ = nullptr;
+    size_t cap_vbins_ = 0, cap_vperm_ = 0;
+    int* d_batch_slots_ = nullptr;
+    int n_batch_ = 0, cap_batch_ = 0;
+    std::vector<int> batch_slots_host_;
     int n_attach_ = 0, cap_attach_ = 0;     // simulations with VX3 attachment in the batch
     int64_t graph_launches_ = 0;            // kernels one replay of the captured graph launches
     int* d_attach_slots_ = nullptr;
@@ -186,9 +194,10 @@ public:
             if (b->done) cudaEventDestroy(b->done);
         }
         cudaFree(d_gather_);
-        cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_partials_); cudaFree(d_com4_);
+        cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_com4_);
         cudaFree(d_attach_slots_);
         cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
+        cudaFree(d_vox_hist_); cudaFree(d_vox_base_); cudaFree(d_vox_total_); cudaFree(d_vox_perm_); cudaFree(d_batch_slots_);
         cudaFree(arena_base_);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
@@ -784,6 +793,8 @@ public:
             c.optdt = opt;
             c.cycle_step = r->cycle_step;
             c.maxf2_bits = bits;
+            // the first step ends at t = dt (currentTime starts at 0)
+            c.t_cycles = (w.desc.vary_temp && w.desc.temp_period > 0) ? (0.0 + (double)c.dt) / w.desc.temp_period : 0.0;
             CK(cudaMemcpyAsync(d_ctl_ + r->slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
         }
         CK(cudaEventRecord(rb_.done, stream_));
@@ -857,18 +868,43 @@ public:
             ctl_items.emplace_back(begin, cnt);
         }
         n_vox_items_ = (int)items.size() - n_link_items_ - n_contact_items_;
+        {
+            size_t vox_total = 0;
+            for (int s : slots) vox_total += (size_t)slot_owner_[s]->w.nv;
+            const size_t vb = (size_t)std::max(1, n_vox_items_) * dev::kOrderKeysBins;
+            if (vb > cap_vbins_ || !d_vox_total_) {
+                cudaFree(d_vox_hist_); cudaFree(d_vox_base_);
+                d_vox_hist_ = d_vox_base_ = nullptr;
+                cap_vbins_ = std::max(vb, 2 * cap_vbins_);
+                CK(cudaMalloc(&d_vox_hist_, sizeof(int) * cap_vbins_));
+                CK(cudaMalloc(&d_vox_base_, sizeof(int) * cap_vbins_));
+                if (!d_vox_total_) CK(cudaMalloc(&d_vox_total_, sizeof(int)));
+            }
+            if (std::max<size_t>(1, vox_total) > cap_vperm_) {
+                cudaFree(d_vox_perm_);
+                d_vox_perm_ = nullptr;
+                cap_vperm_ = std::max(std::max<size_t>(1, vox_total), 2 * cap_vperm_);
+                CK(cudaMalloc(&d_vox_perm_, sizeof(int2) * cap_vperm_));
+            }
+            n_batch_ = (int)slots.size();
+            if (n_batch_ > cap_batch_) {
+                cudaFree(d_batch_slots_);
+                cap_batch_ = std::max(n_batch_, 2 * cap_batch_);
+                CK(cudaMalloc(&d_batch_slots_, sizeof(int) * cap_batch_));
+            }
+            batch_slots_host_ = slots;   // kept alive for the asynchronous copy
+            if (n_batch_)
+                CK(cudaMemcpyAsync(d_batch_slots_, batch_slots_host_.data(), sizeof(int) * n_batch_, cudaMemcpyHostToDevice, stream_));
+        }
         if ((int)items.size() > cap_items_) {
             cudaFree(d_items_);
-            cudaFree(d_partials_);
             cap_items_ = std::max((int)items.size(), 2 * cap_items_);
             CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
-            CK(cudaMalloc(&d_partials_, sizeof(double) * 4 * cap_items_));
         }
         if (!items.empty()) CK(cudaMemcpyAsync(d_items_, items.data(), sizeof(dev::Item) * items.size(), cudaMemcpyHostToDevice, stream_));
         n_attach_ = (int)attach_slots.size();
         if (n_attach_ > cap_attach_) {
             cudaFree(d_attach_slots_);
-        cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
             cap_attach_ = std::max(n_attach_, 2 * cap_attach_);
             CK(cudaMalloc(&d_attach_slots_, sizeof(int) * cap_attach_));
         }
@@ -895,15 +931,15 @@ public:
 
     // One step of the batch; returns the number of kernels it launched.
     int launch_step(cudaStream_t st, bool prof) {
-        int launched = 2 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
+        int launched = 7 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
         const dev::Item* li = d_items_;
         const dev::Item* ci = d_items_ + n_link_items_;
         const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
         if (bins_dirty_ || bin_phase_ % bin_every_ == 0) {
             // windows of about 16k links: a window's link state stays in L2 while its key groups run
             const int win = std::max(1, 16384 / std::max(1, items_links_));
-            ks_.link_bins(std::max(1, std::min(n_link_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, li, n_link_items_, win, d_link_hist_,
-                          d_link_base_, d_link_total_, d_link_perm_);
+            ks_.bins(std::max(1, std::min(n_link_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, li, n_link_items_, 0, win, d_link_hist_,
+                     d_link_base_, d_link_total_, d_link_perm_);
             bins_dirty_ = false;
             bin_phase_ = 0;
             launched += 3;
@@ -915,10 +951,18 @@ public:
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
-        ks_.voxels(grid_for(n_vox_items_, block_voxels_), block_voxels_, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_,
-                   d_partials_ + 4 * (size_t)(n_link_items_ + n_contact_items_));
-        if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
+        {
+            // voxel grouping every step (floor contact changes often); windows of about 16k voxels
+            const int win = std::max(1, 16384 / std::max(1, items_voxels_));
+            ks_.bins(std::max(1, std::min(n_vox_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, vi, n_vox_items_, 1, win, d_vox_hist_,
+                     d_vox_base_, d_vox_total_, d_vox_perm_);
+        }
         if (prof) cudaEventRecord(evk_[3], st);
+        ks_.voxels(sm_count_ * 2 * std::max(1, 256 / block_voxels_), block_voxels_, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
+                   d_tickets_);
+        if (prof) cudaEventRecord(evk_[4], st);
+        ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_);
+        if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
         return launched;
     }
 
@@ -1075,9 +1119,9 @@ public:
         timing_.wall_ms = (now_s() - w0) * 1e3;
         if (profiling_) {
             float a = 0, b = 0, c = 0;
-            cudaEventElapsedTime(&a, evk_[0], evk_[1]);
-            cudaEventElapsedTime(&b, evk_[1], evk_[2]);
-            cudaEventElapsedTime(&c, evk_[2], evk_[3]);
+            cudaEventElapsedTime(&a, evk_[0], evk_[1]);   // k_links
+            cudaEventElapsedTime(&b, evk_[1], evk_[2]);   // k_contacts (and k_attach)
+            cudaEventElapsedTime(&c, evk_[3], evk_[4]);   // k_voxels
             timing_.link_kernel_ms = a; timing_.contact_kernel_ms = b; timing_.voxel_kernel_ms = c;
         }
         if (!rs.empty()) {

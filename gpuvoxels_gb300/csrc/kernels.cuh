@@ -301,6 +301,24 @@ struct LinkKey {
     }
 };
 
+// Voxel key: touched the floor last step (contact and friction branches) and, if so,
+// held by static friction (the kinetic branch forms the sliding direction), then
+// surface voxels (Poisson strain by pow) apart from interior ones.
+struct VoxelKey {
+    const uint32_t* vfl;
+    int begin;
+    __device__ int operator()(int j) const {
+        const uint32_t f = vfl[begin + j];
+        const int floor = (f & VF_FLOORC) ? ((f & VF_STATIC) ? 2 : 3) : 0;
+        return 2 * floor + ((f & VF_INTERIOR) ? 1 : 0);
+    }
+};
+
+// Grouping key of element j of a work item starting at `begin`: links (kind 0) or voxels (kind 1).
+__device__ __forceinline__ int bin_key(const Sim& S, int kind, int begin, int j) {
+    return kind == 0 ? LinkKey{S.lfl, begin}(j) : VoxelKey{S.vfl, begin}(j);
+}
+
 // Resident blocks per SM the register allocation of k_links / k_voxels is sized for
 // (a build-time tuning knob: -DGVX_LINKS_MIN_BLOCKS=3 trades registers for warps).
 #ifndef GVX_LINKS_MIN_BLOCKS
@@ -322,19 +340,19 @@ struct LinkKey {
 // barriers: warps of cheap small-angle links waited for warps of costly large-angle
 // ones.  Grouping across the whole batch at once made every key group a separate
 // pass over all link state and tripled k_links' DRAM traffic.)
-__global__ void __launch_bounds__(256) k_link_hist(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                   int n_items, int* hist) {
+__global__ void __launch_bounds__(256) k_bin_hist(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                  int n_items, int kind, int* hist) {
     __shared__ int wc[kOrderKeys * 8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const Item w = items[it];
         const bool run = ctl[w.sim].status == 1;
-        const LinkKey key{sims[w.sim].lfl, w.begin};
+        const Sim& S = sims[w.sim];
         const int n = w.end - w.begin;
-        int cnt = 0;   // thread k < kOrderKeys: links of key k
+        int cnt = 0;   // thread k < kOrderKeys: elements of key k
         for (int j0 = 0; j0 < n; j0 += blockDim.x) {
             const int j = j0 + threadIdx.x;
-            const int kj = (run && j < n) ? key(j) : -1;
+            const int kj = (run && j < n) ? bin_key(S, kind, w.begin, j) : -1;
 #pragma unroll
             for (int k = 0; k < kOrderKeys; k++) {
                 const unsigned b = __ballot_sync(0xffffffffu, kj == k);
@@ -353,7 +371,7 @@ __global__ void __launch_bounds__(256) k_link_hist(const Sim* __restrict__ sims,
 // by key, item by item, so base[item][key] = links of earlier windows + links of
 // smaller keys in the window + links of that key in earlier items of the window.
 // Each thread scans a contiguous run of that order; the runs are joined by a block scan.
-__global__ void __launch_bounds__(1024) k_link_scan(const int* __restrict__ hist, int* base, int n_items, int win, int* total) {
+__global__ void __launch_bounds__(1024) k_bin_scan(const int* __restrict__ hist, int* base, int n_items, int win, int* total) {
     __shared__ int s_sum[1024];
     const int n_win = (n_items + win - 1) / win;
     const int N = n_win * win * kOrderKeys;
@@ -390,21 +408,21 @@ __global__ void __launch_bounds__(1024) k_link_scan(const int* __restrict__ hist
     if (threadIdx.x == blockDim.x - 1) *total = s_sum[blockDim.x - 1];
 }
 
-__global__ void __launch_bounds__(256) k_link_scatter(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                      int n_items, const int* __restrict__ base, int2* perm) {
+__global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                     int n_items, int kind, const int* __restrict__ base, int2* perm) {
     __shared__ int wc[kOrderKeys * 8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const unsigned below = (1u << lane) - 1u;
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const Item w = items[it];
         if (ctl[w.sim].status != 1) continue;   // the same for the whole block
-        const LinkKey key{sims[w.sim].lfl, w.begin};
+        const Sim& S = sims[w.sim];
         int start[kOrderKeys];
         for (int k = 0; k < kOrderKeys; k++) start[k] = base[(size_t)it * kOrderKeys + k];
         const int n = w.end - w.begin;
         for (int j0 = 0; j0 < n; j0 += blockDim.x) {
             const int j = j0 + threadIdx.x;
-            const int kj = j < n ? key(j) : -1;
+            const int kj = j < n ? bin_key(S, kind, w.begin, j) : -1;
             unsigned mine = 0;
 #pragma unroll
             for (int k = 0; k < kOrderKeys; k++) {
@@ -975,19 +993,16 @@ __device__ __noinline__ void secondary_experiment(const Sim& S, Ctl& c, double t
 // recent-angle measure (VX3_VoxelyzeKernel.cu:314-334, 352), stop condition.
 // Kept out of line so the voxel loop does not carry its registers and stack.
 __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double t_next, int64_t stepno, bool com_step, int flags,
-                                         int nv, const double* partials) {
-    c.done_items = 0;
+                                         int nv, const double* s4) {
     if (div) { c.status = 3; return; }
     if (c.error) { c.status = 4; return; }
     const double t_now = c.t;
     if (flags & SF_SIGNALS) c.sig_pending = 1;   // k_signals completes this step's signals
     c.t = t_next;
     c.steps = stepno;
+    if (flags & SF_VARY) c.t_cycles = (c.t + c.dt) / S.temp_period;   // the next step's actuation phase
     if (flags & SF_COLLIDE) c.hash_parity ^= 1;
     if (com_step) {
-        double s4[4] = {0, 0, 0, 0};
-        for (int k = 0; k < c.n_vox_items; k++)
-            for (int j = 0; j < 4; j++) s4[j] += partials[(size_t)(c.item_begin + k) * 4 + j];
         c.angle_samples++;
         for (int j = 0; j < 3; j++) { c.com_hist[0][j] = c.com_hist[1][j]; c.com_hist[1][j] = c.com[j]; }
         if (s4[3] == 0) { c.com[0] = c.com[1] = c.com[2] = 0; }
@@ -1035,71 +1050,59 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
     if (stop) c.status = 2;
 }
 
-// Voxel key: touched the floor last step (contact and friction branches), then
-// surface voxels (Poisson strain by pow) apart from interior ones.
-struct VoxelKey {
-    const uint32_t* vfl;
-    int begin;
-    __device__ int operator()(int j) const {
-        const uint32_t f = vfl[begin + j];
-        return ((f & VF_FLOORC) ? 2 : 0) | ((f & VF_INTERIOR) ? 1 : 0);
-    }
-};
-
-__global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items,
-                                                int* tickets, double* partials) {
-    __shared__ int s_item, s_last;
-    __shared__ double red[256];
-    __shared__ double s_cycles;
-    __shared__ int s_perm[kOrderMax];
-    __shared__ int s_warp[kOrderKeys * 8];
+__global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
+                                                                       const int* __restrict__ total, int* tickets) {
+    // the voxels of the running simulations, grouped by key like the links (k_bin_*); warps
+    // take 32-voxel chunks, so no warp waits at a block barrier for a costlier one
     if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
+    const int n = *total;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        const int it = claim(&tickets[2], &s_item);
-        if (it >= n_items) break;
-        const Item w = items[it];
-        Ctl& c = ctl[w.sim];
-        if (c.status != 1) continue;
-        const Sim& S = sims[w.sim];
-        const bool div = c.diverged;
-        const float dt = c.dt;
-        const double t_next = c.t + dt;
-        // one FP64 division per item instead of one per voxel
-        if (threadIdx.x == 0) s_cycles = (S.flags & SF_VARY) ? t_next / S.temp_period : 0.0;
-        __syncthreads();
-        StepTimes st;
-        st.t_now = c.t; st.t_next = t_next; st.t_cycles = s_cycles; st.angle = c.recent_angle;
-        st.closeness = c.closeness; st.close_pairs = c.num_close_pairs; st.hits = c.hit_count;
-        const int64_t stepno = c.steps + 1;
-        const bool com_step = c.cycle_step > 0 && (stepno % c.cycle_step) == 0;
-        const int flags = S.flags;
-        int* hnext = (flags & SF_COLLIDE) ? S.hash_head + (size_t)(c.hash_parity ^ 1) * S.hash_size : nullptr;
-        double acc[4] = {0, 0, 0, 0};
-        if (!div && dt != 0.0f) {
-            const int n = w.end - w.begin;
-            if (n <= kOrderMax) {
-                order_by_key(n, VoxelKey{S.vfl, w.begin}, s_perm, s_warp);
-                for (int k = threadIdx.x; k < n; k += blockDim.x)
-                    voxel_update(S, w.begin + s_perm[k], dt, st, flags, com_step ? acc : nullptr, hnext);
-            } else {
-                for (int v = w.begin + threadIdx.x; v < w.end; v += blockDim.x) voxel_update(S, v, dt, st, flags, com_step ? acc : nullptr, hnext);
+        int chunk = 0;
+        if (lane == 0) chunk = atomicAdd(&tickets[2], 1);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        if (chunk * 32 >= n) break;
+        const int k = chunk * 32 + lane;
+        if (k < n) {
+            const int2 e = __ldg(perm + k);
+            const Ctl& c = ctl[e.x];
+            const float dt = c.dt;
+            if (c.status == 1 && !c.diverged && dt != 0.0f) {
+                const Sim& S = sims[e.x];
+                StepTimes st;
+                st.t_now = c.t; st.t_next = c.t + dt; st.t_cycles = c.t_cycles; st.angle = c.recent_angle;
+                st.closeness = c.closeness; st.close_pairs = c.num_close_pairs; st.hits = c.hit_count;
+                int* hnext = (S.flags & SF_COLLIDE) ? S.hash_head + (size_t)(c.hash_parity ^ 1) * S.hash_size : nullptr;
+                voxel_update(S, e.y, dt, st, S.flags, nullptr, hnext);
             }
-        }
-        if (com_step) {
-            for (int k = 0; k < 4; k++) {
-                const double r = block_sum(acc[k], red);
-                if (threadIdx.x == 0) partials[(size_t)it * 4 + k] = r;
-            }
-        }
-        __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) s_last = (atomicAdd(&c.done_items, 1) == c.n_vox_items - 1);
-        __syncthreads();
-        if (s_last && threadIdx.x == 0) {
-            __threadfence();
-            sim_control(S, c, div, t_next, stepno, com_step, flags, S.nv, partials);
         }
     }
+}
+
+// The end of a step for each simulation of the batch, one block each: on cycle steps the
+// centre of mass of the measured voxels (the fixed-order sum of k_com), then sim_control.
+__global__ void __launch_bounds__(256) k_sim_end(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
+    __shared__ double red[256];
+    if ((int)blockIdx.x >= n) return;
+    const int sim = slots[blockIdx.x];
+    Ctl& c = ctl[sim];
+    if (c.status != 1) return;
+    const Sim& S = sims[sim];
+    const bool div = c.diverged;
+    const double t_next = c.t + c.dt;
+    const int64_t stepno = c.steps + 1;
+    const bool com_step = c.cycle_step > 0 && (stepno % c.cycle_step) == 0;
+    double s4[4] = {0, 0, 0, 0};
+    if (com_step && !div) {
+        double a[4] = {0, 0, 0, 0};
+        for (int v = threadIdx.x; v < S.nv; v += blockDim.x) {
+            if (!(S.vfl[v] & VF_MEASURED)) continue;
+            const double w = S.vm[S.vmat[v]].mass;
+            a[0] += S.px[v] * w; a[1] += S.py[v] * w; a[2] += S.pz[v] * w; a[3] += w;
+        }
+        for (int k = 0; k < 4; k++) s4[k] = block_sum(a[k], red);
+    }
+    if (threadIdx.x == 0) sim_control(S, c, div, t_next, stepno, com_step, S.flags, S.nv, s4);
 }
 
 // VX3 attachment (handle_collision_attachment, VX3_VoxelyzeKernel.cu:729-827) for one
@@ -1351,18 +1354,21 @@ __global__ void k_com(const Sim* __restrict__ sims, int sim, double* out4) {
 // ---------------------------------------------------------------- launch table
 namespace gvx {
 namespace GVX_KNS {
-inline void l_link_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int win, int* hist, int* base,
-                        int* total, int2* perm) {
-    k_link_hist<<<g, 256, 0, s>>>(sims, ctl, it, n, hist);
-    k_link_scan<<<1, 1024, 0, s>>>(hist, base, n, win, total);
-    k_link_scatter<<<g, 256, 0, s>>>(sims, ctl, it, n, base, perm);
+inline void l_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int kind, int win, int* hist, int* base,
+                   int* total, int2* perm) {
+    k_bin_hist<<<g, 256, 0, s>>>(sims, ctl, it, n, kind, hist);
+    k_bin_scan<<<1, 1024, 0, s>>>(hist, base, n, win, total);
+    k_bin_scatter<<<g, 256, 0, s>>>(sims, ctl, it, n, kind, base, perm);
 }
 inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int* tk) {
     k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, tk);
 }
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
-inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk, double* p) {
-    k_voxels<<<g, b, 0, s>>>(sims, ctl, it, n, tk, p);
+inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int* tk) {
+    k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, tk);
+}
+inline void l_sim_end(cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
+    if (n > 0) k_sim_end<<<n, 256, 0, s>>>(sims, ctl, slots, n);
 }
 inline void l_signals(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) {
     k_signals<<<g, b, 0, s>>>(sims, ctl, it, n, tk);
@@ -1386,7 +1392,7 @@ inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int
     if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
 }
 inline KernelSet make_kernelset(const char* name) {
-    return KernelSet{name, l_link_bins, l_links, l_contacts, l_voxels, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
+    return KernelSet{name, l_bins, l_links, l_contacts, l_voxels, l_sim_end, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

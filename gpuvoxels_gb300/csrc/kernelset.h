@@ -9,14 +9,16 @@ namespace gvx {
 
 struct KernelSet {
     const char* name;
-    // groups the links of the running simulations by key across the batch (hist, base: per
-    // link item and key; total: links listed; perm: (simulation, link) pairs)
-    void (*link_bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int win, int* hist,
-                      int* base, int* total, int2* perm);
+    // groups the links (kind 0) or voxels (kind 1) of the running simulations by key in windows
+    // of `win` work items (hist, base: per item and key; total: elements listed; perm:
+    // (simulation, element) pairs)
+    void (*bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int kind, int win, int* hist,
+                 int* base, int* total, int2* perm);
     void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int* tickets);
     void (*contacts)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
-    void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets,
-                   double* partials);
+    void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int* tickets);
+    // the end of the step for n simulations (slot list): centre-of-mass sample, time, stop
+    void (*sim_end)(cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
     // VX3 signals relayed between neighbours (after voxels, over the voxel items)
     void (*signals)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
     // VX3 attachment: new links for this step's candidate pairs of n simulations (device slot list)

@@ -173,6 +173,7 @@ struct Ctl {
     int32_t sig_done_items;     // signal-phase items finished this step (SF_SIGNALS)
     double com[3], com_hist[2][3];
     double recent_angle;
+    double t_cycles;            // (t + dt) / TempPeriod for the coming step (actuation phase)
     // VX3 measures: target closeness and close pairs (at CoM samples), target contacts so far
     double closeness;
     int32_t num_close_pairs, hit_count;
