@@ -309,14 +309,14 @@ def run_ours(args):
     if rank == 0:
         c2 = g.Context(local, budget)
         c2.set_precision(prec)
+        h0, d0 = c2.transfer_bytes()
         t0 = time.perf_counter()
         ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
         c2.step(ids2, args.steps, g.BATCHED)
-        d2h = 0
         pos, q, fl, _ = c2.get_states(ids2)      # every creature's pose, one device pass and one copy
-        d2h += pos.nbytes + q.nbytes + fl.nbytes
         e2e_wall = time.perf_counter() - t0
-        h2d = c2.bytes_in_use()
+        h1, d1 = c2.transfer_bytes()             # bytes the engine copied each way in the timed region
+        h2d, d2h = h1 - h0, d1 - d0
         e2e_vs = sum(c2.info(i).num_voxel for i in ids2) * args.steps
         c2.close()
         e2e = dict(value=e2e_vs / e2e_wall, unit="voxel-steps/s", h2d_bytes_per_step=int(h2d / args.steps),

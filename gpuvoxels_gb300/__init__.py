@@ -36,7 +36,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
            "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states",
-           "vx3_get_extras", "vx3_get_links"]
+           "vx3_get_extras", "vx3_get_links", "vx3_transfer_bytes"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -98,6 +98,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_get_states": (I, [P, P, I, P, P, P]),
         "vx3_get_extras": (I, [P, I64, P, P]),
         "vx3_get_links": (I, [P, I64, P, P, I]),
+        "vx3_transfer_bytes": (I, [P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -318,6 +319,12 @@ class Context:
         self.L.vx3_last_timing(self.h, _p(o))
         return dict(device_ms=o[0], wall_ms=o[1], voxel_steps=int(o[2]), launches=int(o[3]), link_ms=o[4],
                     contact_ms=o[5], voxel_ms=o[6])
+
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes this context has copied so far."""
+        h = np.zeros(1, np.int64); d = np.zeros(1, np.int64)
+        self._check(self.L.vx3_transfer_bytes(self.h, _p(h), _p(d)))
+        return int(h[0]), int(d[0])
 
     def set_tuning(self, block_links=0, block_voxels=0, items_links=0, items_voxels=0, graph_steps=0):
         self.L.vx3_set_tuning(self.h, block_links, block_voxels, items_links, items_voxels, graph_steps)

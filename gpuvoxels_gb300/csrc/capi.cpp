@@ -383,6 +383,12 @@ int vx3_get_links(vx3_ctx* c, vx3_sim_id id, int32_t* n_links, int32_t* ends4, i
     return e ? fail(c, e, err) : VX3_OK;
 }
 
+int vx3_transfer_bytes(vx3_ctx* c, int64_t* h2d, int64_t* d2h) {
+    if (!c || !h2d || !d2h) return VX3_E_ARG;
+    c->eng->transfer_bytes(h2d, d2h);
+    return VX3_OK;
+}
+
 int vx3_get_extras(vx3_ctx* c, vx3_sim_id id, double* measures4, double* signals6) {
     if (!c) return VX3_E_ARG;
     std::string err;

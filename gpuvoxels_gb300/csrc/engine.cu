@@ -230,6 +230,27 @@ public:
     }
 
     // A pinned buffer of at least `bytes`, once its previous copy has finished.
+    // Every host<->device copy of the engine goes through these, which count the bytes
+    // (vx3_transfer_bytes).
+    int64_t h2d_bytes_ = 0, d2h_bytes_ = 0;
+    void count_copy(size_t n, cudaMemcpyKind k) {
+        if (k == cudaMemcpyHostToDevice) h2d_bytes_ += (int64_t)n;
+        else if (k == cudaMemcpyDeviceToHost) d2h_bytes_ += (int64_t)n;
+    }
+    cudaError_t copy_async(void* dst, const void* src, size_t n, cudaMemcpyKind k, cudaStream_t st) {
+        count_copy(n, k);
+        return cudaMemcpyAsync(dst, src, n, k, st);
+    }
+    cudaError_t copy2d_async(void* dst, size_t dp, const void* src, size_t sp, size_t w, size_t h, cudaMemcpyKind k, cudaStream_t st) {
+        count_copy(w * h, k);
+        return cudaMemcpy2DAsync(dst, dp, src, sp, w, h, k, st);
+    }
+    cudaError_t copy_sync(void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+        count_copy(n, k);
+        return cudaMemcpy(dst, src, n, k);
+    }
+    void transfer_bytes(int64_t* h2d, int64_t* d2h) const override { *h2d = h2d_bytes_; *d2h = d2h_bytes_; }
+
     int pinned(Pinned* b, size_t bytes, std::string* err) {
         CK(cudaEventSynchronize(b->done));
         if (b->cap >= bytes) return 0;
@@ -252,8 +273,8 @@ public:
         CK(cudaMemset(nctl, 0, sizeof(dev::Ctl) * nc));
         if (cap_slots_) {
             CK(cudaStreamSynchronize(stream_));
-            CK(cudaMemcpy(ns, d_sims_, sizeof(dev::Sim) * cap_slots_, cudaMemcpyDeviceToDevice));
-            CK(cudaMemcpy(nctl, d_ctl_, sizeof(dev::Ctl) * cap_slots_, cudaMemcpyDeviceToDevice));
+            CK(copy_sync(ns, d_sims_, sizeof(dev::Sim) * cap_slots_, cudaMemcpyDeviceToDevice));
+            CK(copy_sync(nctl, d_ctl_, sizeof(dev::Ctl) * cap_slots_, cudaMemcpyDeviceToDevice));
             cudaFree(d_sims_);
             cudaFree(d_ctl_);
         }
@@ -311,6 +332,7 @@ public:
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
         size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos, cilia, ffield;
         size_t shift, sig, vlink, targets, init_pos, lnew, cand, cpart, acond;
+        size_t zero_from;   // everything from here on starts as zeros
         int hash_size;
     };
     static void compute_layout(const SimWorld& w, Layout* L, Offs* o) {
@@ -318,28 +340,21 @@ public:
         const size_t nv = w.nv, nl = link_capacity(w);
         const bool col = w.desc.collisions;
         const SimDesc& d = w.desc;
+        // arrays with initial data first, then the ones that start as zeros (cleared on the
+        // device, so that the host builds and copies only the first part)
         t.vm = L->add(sizeof(dev::VMat) * w.vmats.size());
         t.lm = L->add(sizeof(dev::LMat) * std::max<size_t>(1, w.lmats.size()));
         t.ext = L->add(sizeof(dev::Ext) * std::max<size_t>(1, w.desc.externals.size()));
         for (int k = 0; k < 3; k++) t.pos[k] = L->add(8 * nv);
-        for (int k = 0; k < 3; k++) t.mom[k] = L->add(8 * nv);
-        for (int k = 0; k < 4; k++) t.q[k] = L->add(8 * nv);
-        for (int k = 0; k < 3; k++) t.am[k] = L->add(8 * nv);
-        t.temp = L->add(4 * nv);
-        t.ps = L->add(4 * 3 * nv);
+        t.q[0] = L->add(8 * nv);
         t.vfl = L->add(4 * nv);
         t.vmat = L->add(nv);
         t.vext = L->add(4 * nv);
         t.phase = L->add(8 * nv);
-        t.sf = L->add(8 * 18 * nv);
-        t.sm = L->add(8 * 18 * nv);
-        t.ss = L->add(4 * 6 * nv);
         t.lneg = L->add(4 * std::max<size_t>(1, nl));
         t.lpos = L->add(4 * std::max<size_t>(1, nl));
         t.lax = L->add(std::max<size_t>(1, nl));
         t.lmt = L->add(std::max<size_t>(1, nl));
-        t.lst = L->add(8 * 9 * std::max<size_t>(1, nl));
-        t.lsf = L->add(4 * 3 * std::max<size_t>(1, nl));
         t.lfl = L->add(std::max<size_t>(1, nl));
         t.ijk = L->add(2 * 3 * nv);
         if (col) {
@@ -349,25 +364,38 @@ public:
             t.hash_size = hs;
             t.surf = L->add(4 * ns);
             t.reach = L->add(4 * dev::kReachWords * nv);
-            t.ccount = L->add(4 * nv);
-            t.cforce = L->add(4 * 3 * dev::kContactCap * nv);
             t.hhead = L->add(4 * 2 * (size_t)hs);
-            t.hnext = L->add(4 * nv);
-            t.cpos = L->add(16 * nv);
         }
         if (w.desc.enable_cilia) t.cilia = L->add(8 * 3 * nv);
         if (w.desc.has_force_field) t.ffield = L->add(sizeof(MathTree) * 3);
         if (d.enable_signals && d.enable_cilia && !d.shift_cilia.empty()) t.shift = L->add(8 * 3 * nv);
-        if (d.enable_signals) t.sig = L->add(8 * dev::SG_FIELDS * nv);
         if (d.enable_signals || removes_materials(d) || attaches(d)) t.vlink = L->add(4 * 6 * nv);
+        if (attaches(d)) t.acond = L->add(sizeof(MathTree) * 5);
+        if (int nt = target_count(w)) t.targets = L->add(4 * (size_t)nt);
+        if (d.secondary_experiment) t.init_pos = L->add(8 * 3 * nv);
+        t.zero_from = L->total;
+        for (int k = 0; k < 3; k++) t.mom[k] = L->add(8 * nv);
+        for (int k = 1; k < 4; k++) t.q[k] = L->add(8 * nv);
+        for (int k = 0; k < 3; k++) t.am[k] = L->add(8 * nv);
+        t.temp = L->add(4 * nv);
+        t.ps = L->add(4 * 3 * nv);
+        t.sf = L->add(8 * 18 * nv);
+        t.sm = L->add(8 * 18 * nv);
+        t.ss = L->add(4 * 6 * nv);
+        t.lst = L->add(8 * 9 * std::max<size_t>(1, nl));
+        t.lsf = L->add(4 * 3 * std::max<size_t>(1, nl));
+        if (col) {
+            t.ccount = L->add(4 * nv);
+            t.cforce = L->add(4 * 3 * dev::kContactCap * nv);
+            t.hnext = L->add(4 * nv);
+            t.cpos = L->add(16 * nv);
+        }
+        if (d.enable_signals) t.sig = L->add(8 * dev::SG_FIELDS * nv);
         if (attaches(d)) {
             t.lnew = L->add(4 * nl);
             t.cand = L->add(8 * (size_t)dev::kContactCap / 2 * nv + 8);
             t.cpart = L->add(4 * (size_t)dev::kContactCap * nv);
-            t.acond = L->add(sizeof(MathTree) * 5);
         }
-        if (int nt = target_count(w)) t.targets = L->add(4 * (size_t)nt);
-        if (d.secondary_experiment) t.init_pos = L->add(8 * 3 * nv);
         if (o) *o = t;
     }
 
@@ -483,23 +511,25 @@ public:
         r->off = off;
         r->bytes = L.total;
         char* base = arena_base_ + off;
-        // host image of the region: built in a pinned staging buffer so that its copy runs
-        // asynchronously while the next simulation's image is filled (pageable for huge regions)
+        // host image of the region's initialised part (the rest starts as zeros and is cleared
+        // on the device): built in a pinned staging buffer so that its copy runs asynchronously
+        // while the next simulation's image is filled (pageable for huge regions)
+        const size_t img = o.zero_from;
         std::vector<char> hv;
         char* hp = nullptr;
         Pinned* stage = nullptr;
-        if (L.total <= kPinnedUploadMax) {
+        if (img <= kPinnedUploadMax) {
             stage = &up_[up_next_];
             up_next_ ^= 1;
-            if (int e = pinned(stage, L.total, err)) {
+            if (int e = pinned(stage, img, err)) {
                 arena_.release(off, L.total);
                 slot_owner_[slot] = nullptr;
                 return e;
             }
             hp = stage->p;
-            memset(hp, 0, L.total);
+            memset(hp, 0, img);
         } else {
-            hv.assign(L.total, 0);
+            hv.assign(img, 0);
             hp = hv.data();
         }
         const size_t nv = w.nv, nl = w.nl;
@@ -698,7 +728,8 @@ public:
         S.n_mats = (int)w.vmats.size();
         S.reinit_after = dd.reinit_initial_after;
         if (dd.secondary_experiment) S.init_pos = (double*)D(o.init_pos);
-        CK(cudaMemcpyAsync(base, hp, L.total, cudaMemcpyHostToDevice, stream_));
+        CK(copy_async(base, hp, img, cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemsetAsync(base + img, 0, L.total - img, stream_));
         if (stage) CK(cudaEventRecord(stage->done, stream_));
         // the descriptor and control block go to the device with the others in upload_finish
         r->pending_sim = S;
@@ -749,10 +780,10 @@ public:
             max_nv = std::max(max_nv, r->w.nv);
             max_nl = std::max(max_nl, r->w.nl);
             max_ns = std::max(max_ns, r->w.surface_count);
-            CK(cudaMemcpyAsync(d_sims_ + r->slot, &sim_img[k], sizeof(dev::Sim), cudaMemcpyHostToDevice, stream_));
-            CK(cudaMemcpyAsync(d_ctl_ + r->slot, &ctl0_img[k], sizeof(dev::Ctl), cudaMemcpyHostToDevice, stream_));
+            CK(copy_async(d_sims_ + r->slot, &sim_img[k], sizeof(dev::Sim), cudaMemcpyHostToDevice, stream_));
+            CK(copy_async(d_ctl_ + r->slot, &ctl0_img[k], sizeof(dev::Ctl), cudaMemcpyHostToDevice, stream_));
         }
-        CK(cudaMemcpyAsync(d_gather_ + o_slot, h + o_slot, o_bits - o_slot, cudaMemcpyHostToDevice, stream_));
+        CK(copy_async(d_gather_ + o_slot, h + o_slot, o_bits - o_slot, cudaMemcpyHostToDevice, stream_));
         const int* d_slots = (const int*)(d_gather_ + o_slot);
         const float* d_init = (const float*)(d_gather_ + o_init);
         // first actuation temperature (t = 0), then the stable step from it, then the collision hash
@@ -765,7 +796,7 @@ public:
         CK(cudaGetLastError());
         uint32_t* bits_all = (uint32_t*)(h + o_bits);
         dev::Ctl* ctl_img = (dev::Ctl*)(h + o_ctl);
-        CK(cudaMemcpy2DAsync(bits_all, sizeof(uint32_t), &d_ctl_[0].maxf2_bits, sizeof(dev::Ctl), sizeof(uint32_t), cap_slots_,
+        CK(copy2d_async(bits_all, sizeof(uint32_t), &d_ctl_[0].maxf2_bits, sizeof(dev::Ctl), sizeof(uint32_t), cap_slots_,
                              cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         for (size_t k = 0; k < rs.size(); k++) {
@@ -795,7 +826,7 @@ public:
             c.maxf2_bits = bits;
             // the first step ends at t = dt (currentTime starts at 0)
             c.t_cycles = (w.desc.vary_temp && w.desc.temp_period > 0) ? (0.0 + (double)c.dt) / w.desc.temp_period : 0.0;
-            CK(cudaMemcpyAsync(d_ctl_ + r->slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
+            CK(copy_async(d_ctl_ + r->slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
         }
         CK(cudaEventRecord(rb_.done, stream_));
         CK(cudaStreamSynchronize(stream_));
@@ -894,14 +925,14 @@ public:
             }
             batch_slots_host_ = slots;   // kept alive for the asynchronous copy
             if (n_batch_)
-                CK(cudaMemcpyAsync(d_batch_slots_, batch_slots_host_.data(), sizeof(int) * n_batch_, cudaMemcpyHostToDevice, stream_));
+                CK(copy_async(d_batch_slots_, batch_slots_host_.data(), sizeof(int) * n_batch_, cudaMemcpyHostToDevice, stream_));
         }
         if ((int)items.size() > cap_items_) {
             cudaFree(d_items_);
             cap_items_ = std::max((int)items.size(), 2 * cap_items_);
             CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
         }
-        if (!items.empty()) CK(cudaMemcpyAsync(d_items_, items.data(), sizeof(dev::Item) * items.size(), cudaMemcpyHostToDevice, stream_));
+        if (!items.empty()) CK(copy_async(d_items_, items.data(), sizeof(dev::Item) * items.size(), cudaMemcpyHostToDevice, stream_));
         n_attach_ = (int)attach_slots.size();
         if (n_attach_ > cap_attach_) {
             cudaFree(d_attach_slots_);
@@ -910,15 +941,15 @@ public:
         }
         if (n_attach_) {
             attach_slots_host_ = attach_slots;   // kept alive for the asynchronous copy
-            CK(cudaMemcpyAsync(d_attach_slots_, attach_slots_host_.data(), sizeof(int) * n_attach_, cudaMemcpyHostToDevice, stream_));
+            CK(copy_async(d_attach_slots_, attach_slots_host_.data(), sizeof(int) * n_attach_, cudaMemcpyHostToDevice, stream_));
         }
         for (size_t i = 0; i < slots.size(); i++) {
             int vals[2] = {ctl_items[i].second, ctl_items[i].first};   // n_vox_items, item_begin
-            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].n_vox_items, vals, sizeof(vals), cudaMemcpyHostToDevice, stream_));
+            CK(copy_async(&d_ctl_[slots[i]].n_vox_items, vals, sizeof(vals), cudaMemcpyHostToDevice, stream_));
             static const int zero = 0;
-            CK(cudaMemcpyAsync(&d_ctl_[slots[i]].done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+            CK(copy_async(&d_ctl_[slots[i]].done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
             if (slot_owner_[slots[i]]->w.desc.enable_signals)
-                CK(cudaMemcpyAsync(&d_ctl_[slots[i]].sig_done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
+                CK(copy_async(&d_ctl_[slots[i]].sig_done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
         }
         CK(cudaMemsetAsync(d_tickets_, 0, 4 * sizeof(int), stream_));
         return 0;
@@ -982,7 +1013,7 @@ public:
         }
         memcpy(rb_.p, slots.data(), 4 * n);
         memcpy(rb_.p + o_tg, targets.data(), 8 * n);
-        CK(cudaMemcpyAsync(d_gather_, rb_.p, total, cudaMemcpyHostToDevice, stream_));
+        CK(copy_async(d_gather_, rb_.p, total, cudaMemcpyHostToDevice, stream_));
         CK(cudaEventRecord(rb_.done, stream_));
         k_ctl_run<<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(d_ctl_, (const int*)d_gather_, (const int64_t*)(d_gather_ + o_tg),
                                                                    (int)n, no_stop);
@@ -1004,7 +1035,7 @@ public:
             cap_gather_ = 4 * n;
         }
         memcpy(rb_.p, slots.data(), 4 * n);
-        CK(cudaMemcpyAsync(d_gather_, rb_.p, 4 * n, cudaMemcpyHostToDevice, stream_));
+        CK(copy_async(d_gather_, rb_.p, 4 * n, cudaMemcpyHostToDevice, stream_));
         CK(cudaEventRecord(rb_.done, stream_));
         k_ctl_end_steps<<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(d_ctl_, (const int*)d_gather_, (int)n);
         CK(cudaGetLastError());
@@ -1012,7 +1043,7 @@ public:
     }
 
     int read_ctl(int slot, dev::Ctl* c, std::string* err) {
-        CK(cudaMemcpyAsync(c, d_ctl_ + slot, offsetof(dev::Ctl, stop), cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(c, d_ctl_ + slot, offsetof(dev::Ctl, stop), cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         return 0;
     }
@@ -1021,7 +1052,7 @@ public:
     // synchronisation); out[s - lo] holds slot s.
     int read_ctls(int lo, int hi, std::vector<dev::Ctl>* out, std::string* err) {
         out->resize((size_t)(hi - lo + 1));
-        CK(cudaMemcpy2DAsync(out->data(), sizeof(dev::Ctl), d_ctl_ + lo, sizeof(dev::Ctl), offsetof(dev::Ctl, stop),
+        CK(copy2d_async(out->data(), sizeof(dev::Ctl), d_ctl_ + lo, sizeof(dev::Ctl), offsetof(dev::Ctl, stop),
                              (size_t)(hi - lo + 1), cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         return 0;
@@ -1102,7 +1133,7 @@ public:
                         timing_.launches += graph_launches_;
                     }
                     // one strided copy of every status word, then a single synchronisation
-                    CK(cudaMemcpy2DAsync(st.data(), sizeof(int32_t), &d_ctl_[lo].status, sizeof(dev::Ctl), sizeof(int32_t),
+                    CK(copy2d_async(st.data(), sizeof(int32_t), &d_ctl_[lo].status, sizeof(dev::Ctl), sizeof(int32_t),
                                          (size_t)(hi - lo + 1), cudaMemcpyDeviceToHost, stream_));
                     CK(cudaStreamSynchronize(stream_));
                     bool running = false;
@@ -1217,7 +1248,7 @@ public:
         ks_.com(stream_, d_sims_, r->slot, d_com4_);
         CK(cudaGetLastError());
         double c4[4];
-        CK(cudaMemcpyAsync(c4, d_com4_, sizeof(c4), cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(c4, d_com4_, sizeof(c4), cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         if (c4[3] == 0) out[0] = out[1] = out[2] = 0;
         else for (int k = 0; k < 3; k++) out[k] = c4[k] / c4[3];
@@ -1248,12 +1279,12 @@ public:
         // (VX3_SimulationManager.cu:442-452)
         const size_t nv = r->w.nv;
         std::vector<double> p(3 * nv), ip;
-        CK(cudaMemcpyAsync(p.data(), r->dsim.px, 8 * nv, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(p.data() + nv, r->dsim.py, 8 * nv, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(p.data() + 2 * nv, r->dsim.pz, 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(p.data(), r->dsim.px, 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(p.data() + nv, r->dsim.py, 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(p.data() + 2 * nv, r->dsim.pz, 8 * nv, cudaMemcpyDeviceToHost, stream_));
         if (c.reinit_done) {
             ip.resize(3 * nv);
-            CK(cudaMemcpyAsync(ip.data(), r->dsim.init_pos, 8 * 3 * nv, cudaMemcpyDeviceToHost, stream_));
+            CK(copy_async(ip.data(), r->dsim.init_pos, 8 * 3 * nv, cudaMemcpyDeviceToHost, stream_));
         }
         CK(cudaStreamSynchronize(stream_));
         double tot = 0;
@@ -1402,12 +1433,12 @@ public:
         std::vector<double> buf(13 * (size_t)nv);
         double* srcs[13] = {r->dsim.px, r->dsim.py, r->dsim.pz, r->dsim.mx, r->dsim.my, r->dsim.mz, r->dsim.qw, r->dsim.qx,
                             r->dsim.qy, r->dsim.qz, r->dsim.ax, r->dsim.ay, r->dsim.az};
-        for (int k = 0; k < 13; k++) CK(cudaMemcpyAsync(buf.data() + (size_t)k * nv, srcs[k], 8 * nv, cudaMemcpyDeviceToHost, stream_));
+        for (int k = 0; k < 13; k++) CK(copy_async(buf.data() + (size_t)k * nv, srcs[k], 8 * nv, cudaMemcpyDeviceToHost, stream_));
         std::vector<float> tb((size_t)nv), ps(3 * (size_t)nv);
         std::vector<uint32_t> fl((size_t)nv);
-        CK(cudaMemcpyAsync(tb.data(), r->dsim.temp, 4 * nv, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(ps.data(), r->dsim.ps, 12 * nv, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(fl.data(), r->dsim.vfl, 4 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(tb.data(), r->dsim.temp, 4 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(ps.data(), r->dsim.ps, 12 * nv, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(fl.data(), r->dsim.vfl, 4 * nv, cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         for (int i = 0; i < nv; i++) {
             if (d13) for (int k = 0; k < 13; k++) d13[13 * (size_t)i + k] = buf[(size_t)k * nv + i];
@@ -1428,10 +1459,10 @@ public:
         if (n <= 0 || !ends4) return 0;
         std::vector<int32_t> ln((size_t)n), lp((size_t)n);
         std::vector<uint8_t> la((size_t)n), lf((size_t)n);
-        CK(cudaMemcpyAsync(ln.data(), r->dsim.lneg, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(lp.data(), r->dsim.lpos, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(la.data(), r->dsim.lax, (size_t)n, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(lf.data(), r->dsim.lfl, (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(ln.data(), r->dsim.lneg, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(lp.data(), r->dsim.lpos, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(la.data(), r->dsim.lax, (size_t)n, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(lf.data(), r->dsim.lfl, (size_t)n, cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         for (int i = 0; i < n; i++) {
             ends4[4 * i] = ln[i]; ends4[4 * i + 1] = lp[i]; ends4[4 * i + 2] = la[i]; ends4[4 * i + 3] = lf[i];
@@ -1452,7 +1483,7 @@ public:
         if (sig6) {
             if (!r->dsim.sig) { std::fill(sig6, sig6 + 6 * nv, 0.0); return 0; }
             std::vector<double> g(6 * nv);
-            CK(cudaMemcpyAsync(g.data(), r->dsim.sig, 8 * 6 * nv, cudaMemcpyDeviceToHost, stream_));
+            CK(copy_async(g.data(), r->dsim.sig, 8 * 6 * nv, cudaMemcpyDeviceToHost, stream_));
             CK(cudaStreamSynchronize(stream_));
             for (size_t i = 0; i < nv; i++)
                 for (int k = 0; k < 6; k++) sig6[6 * i + k] = g[(size_t)k * nv + i];
@@ -1470,9 +1501,9 @@ public:
         std::vector<double> st(9 * stride);
         std::vector<float> sf(3 * stride);
         std::vector<uint8_t> fl((size_t)nl);
-        CK(cudaMemcpyAsync(st.data(), r->dsim.lst, 72 * stride, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(sf.data(), r->dsim.lsf, 12 * stride, cudaMemcpyDeviceToHost, stream_));
-        CK(cudaMemcpyAsync(fl.data(), r->dsim.lfl, nl, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(st.data(), r->dsim.lst, 72 * stride, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(sf.data(), r->dsim.lsf, 12 * stride, cudaMemcpyDeviceToHost, stream_));
+        CK(copy_async(fl.data(), r->dsim.lfl, nl, cudaMemcpyDeviceToHost, stream_));
         CK(cudaStreamSynchronize(stream_));
         for (int i = 0; i < nl; i++) {
             if (d9) for (int k = 0; k < 9; k++) d9[9 * (size_t)i + k] = st[(size_t)k * stride + i];
@@ -1506,13 +1537,13 @@ public:
             CK(cudaMalloc(&d_gather_, need));
             cap_gather_ = need;
         }
-        if (int e = pinned(&rb_, need, err)) return e;
-        // the index tables go through the pinned buffer too
+        if (int e = pinned(&rb_, b_idx, err)) return e;
+        // the index tables go through the pinned buffer
         const size_t o_idx = (b_pos + b_q + b_fl + 15) & ~(size_t)15;
         char* h = rb_.p;
-        memcpy(h + o_idx, offs.data(), 8 * (size_t)n);
-        memcpy(h + o_idx + 8 * (size_t)n, slots.data(), 4 * (size_t)n);
-        CK(cudaMemcpyAsync(d_gather_ + o_idx, h + o_idx, b_idx, cudaMemcpyHostToDevice, stream_));
+        memcpy(h, offs.data(), 8 * (size_t)n);
+        memcpy(h + 8 * (size_t)n, slots.data(), 4 * (size_t)n);
+        CK(copy_async(d_gather_ + o_idx, h, b_idx, cudaMemcpyHostToDevice, stream_));
         double* dpos = (double*)d_gather_;
         double* dq = (double*)(d_gather_ + b_pos);
         uint8_t* dfl = (uint8_t*)(d_gather_ + b_pos + b_q);
@@ -1521,12 +1552,13 @@ public:
         for (int k0 = 0; k0 < n; k0 += 65535)
             ks_.gather(stream_, d_sims_, dslot + k0, doff + k0, std::min(65535, n - k0), dpos, dq, dfl);
         CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(h, d_gather_, b_pos + b_q + b_fl, cudaMemcpyDeviceToHost, stream_));
+        // straight into the caller's buffers: no staging copy on the host, and no pinned
+        // buffer to grow to the size of a whole generation
+        if (pos3) CK(copy_async(pos3, dpos, b_pos, cudaMemcpyDeviceToHost, stream_));
+        if (q4) CK(copy_async(q4, dq, b_q, cudaMemcpyDeviceToHost, stream_));
+        if (flags) CK(copy_async(flags, dfl, b_fl, cudaMemcpyDeviceToHost, stream_));
         CK(cudaEventRecord(rb_.done, stream_));
         CK(cudaEventSynchronize(rb_.done));
-        if (pos3) memcpy(pos3, h, b_pos);
-        if (q4) memcpy(q4, h + b_pos, b_q);
-        if (flags) memcpy(flags, h + b_pos + b_q, b_fl);
         return 0;
     }
 
@@ -1552,9 +1584,9 @@ public:
         if (p.empty()) {
             if (!r->resident) if (int e = upload(r, err)) return e;
             p.resize(3 * (size_t)nv);
-            CK(cudaMemcpyAsync(p.data(), r->dsim.px, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
-            CK(cudaMemcpyAsync(p.data() + nv, r->dsim.py, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
-            CK(cudaMemcpyAsync(p.data() + 2 * (size_t)nv, r->dsim.pz, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
+            CK(copy_async(p.data(), r->dsim.px, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
+            CK(copy_async(p.data() + nv, r->dsim.py, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
+            CK(copy_async(p.data() + 2 * (size_t)nv, r->dsim.pz, 8 * (size_t)nv, cudaMemcpyDeviceToHost, stream_));
             CK(cudaStreamSynchronize(stream_));
         }
         init->resize(3 * (size_t)nv);
@@ -1616,8 +1648,8 @@ public:
         std::vector<dev::Ctl> csnap(rs.size());
         for (size_t i = 0; i < rs.size(); i++) {
             snap[i].resize(rs[i]->bytes);
-            CK(cudaMemcpy(snap[i].data(), arena_base_ + rs[i]->off, rs[i]->bytes, cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(&csnap[i], d_ctl_ + rs[i]->slot, sizeof(dev::Ctl), cudaMemcpyDeviceToHost));
+            CK(copy_sync(snap[i].data(), arena_base_ + rs[i]->off, rs[i]->bytes, cudaMemcpyDeviceToHost));
+            CK(copy_sync(&csnap[i], d_ctl_ + rs[i]->slot, sizeof(dev::Ctl), cudaMemcpyDeviceToHost));
         }
         std::vector<int64_t> tg(slots.size(), (int64_t)1 << 40);
         for (const Cand& c : cands) {
@@ -1634,8 +1666,8 @@ public:
             if (ms < best) { best = ms; bc = c; }
         }
         for (size_t i = 0; i < rs.size(); i++) {
-            CK(cudaMemcpy(arena_base_ + rs[i]->off, snap[i].data(), rs[i]->bytes, cudaMemcpyHostToDevice));
-            CK(cudaMemcpy(d_ctl_ + rs[i]->slot, &csnap[i], sizeof(dev::Ctl), cudaMemcpyHostToDevice));
+            CK(copy_sync(arena_base_ + rs[i]->off, snap[i].data(), rs[i]->bytes, cudaMemcpyHostToDevice));
+            CK(copy_sync(d_ctl_ + rs[i]->slot, &csnap[i], sizeof(dev::Ctl), cudaMemcpyHostToDevice));
         }
         block_links_ = bc.bl; block_voxels_ = bc.bv; items_links_ = bc.il; items_voxels_ = bc.iv;
         batch_dirty_ = true;

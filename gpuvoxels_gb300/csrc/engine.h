@@ -79,6 +79,8 @@ public:
     // Every link in use (the loaded ones, then those VX3 attachment made): *n_links, and for
     // the first `max` of them negative end, positive end, axis and flag byte.
     virtual int links(int64_t id, int32_t* n_links, int32_t* ends4, int max, std::string* err) = 0;
+    // Bytes the context has copied host->device and device->host since it was created.
+    virtual void transfer_bytes(int64_t* h2d, int64_t* d2h) const = 0;
     // Poses of many simulations in one device pass and one copy: pos3/q4/flags hold the
     // simulations' voxels one after another in the order of ids (any pointer may be null).
     virtual int gather_states(const int64_t* ids, int n, double* pos3, double* q4, uint8_t* flags, std::string* err) = 0;

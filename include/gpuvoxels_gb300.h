@@ -167,6 +167,9 @@ int vx3_free_sim(vx3_ctx* ctx, vx3_sim_id id);
  * out[0] device ms (CUDA events), out[1] wall ms, out[2] voxel-steps, out[3] kernel launches,
  * out[4..6] link/contact/voxel kernel ms of the last profiled step. */
 int vx3_last_timing(vx3_ctx* ctx, double* out7);
+/* Bytes the context has copied host->device and device->host since vx3_create (uploads,
+ * control blocks, read-backs): what a caller's data movement costs. */
+int vx3_transfer_bytes(vx3_ctx* ctx, int64_t* h2d, int64_t* d2h);
 /* Tuning: threads per block and elements per work item for the link and voxel
  * launches, and steps per captured graph; 0 keeps the current value. */
 int vx3_set_tuning(vx3_ctx* ctx, int block_links, int block_voxels, int items_links, int items_voxels, int graph_steps);
