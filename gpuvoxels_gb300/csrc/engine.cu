@@ -135,6 +135,11 @@ public:
     // link binning: regrouped every bin_every_ steps (the first step after a batch change always)
     int bin_every_ = 1, bin_phase_ = 0;
     bool bins_dirty_ = true;
+    // Small batches (serving at low load) are bound by launch latency, not by the FP64 pipe:
+    // their links and voxels are regrouped only when the batch changes and at the start of
+    // every graph replay, not every step.
+    static constexpr size_t kRegroupEveryStepLinks = 200000;
+    size_t batch_links_ = 0, batch_voxels_ = 0;
     int sm_count_ = 152;
     int profiling_ = 0;
     KernelSet ks_ = kernelset_exact();
@@ -863,6 +868,7 @@ public:
         bins_dirty_ = true;
         size_t links_total = 0;
         for (int s : slots) links_total += (size_t)link_capacity(slot_owner_[s]->w);
+        batch_links_ = links_total;
         const size_t bins = (size_t)std::max(1, n_link_items_) * dev::kOrderKeysBins;
         if (bins > cap_bins_ || !d_link_total_) {
             cudaFree(d_link_hist_); cudaFree(d_link_base_);
@@ -870,7 +876,10 @@ public:
             cap_bins_ = std::max(bins, 2 * cap_bins_);
             CK(cudaMalloc(&d_link_hist_, sizeof(int) * cap_bins_));
             CK(cudaMalloc(&d_link_base_, sizeof(int) * cap_bins_));
-            if (!d_link_total_) CK(cudaMalloc(&d_link_total_, sizeof(int)));
+            if (!d_link_total_) {
+                CK(cudaMalloc(&d_link_total_, sizeof(int)));
+                CK(cudaMemsetAsync(d_link_total_, 0, sizeof(int), stream_));
+            }
         }
         if (std::max<size_t>(1, links_total) > cap_perm_) {
             cudaFree(d_link_perm_);
@@ -902,6 +911,7 @@ public:
         {
             size_t vox_total = 0;
             for (int s : slots) vox_total += (size_t)slot_owner_[s]->w.nv;
+            batch_voxels_ = vox_total;
             const size_t vb = (size_t)std::max(1, n_vox_items_) * dev::kOrderKeysBins;
             if (vb > cap_vbins_ || !d_vox_total_) {
                 cudaFree(d_vox_hist_); cudaFree(d_vox_base_);
@@ -909,7 +919,10 @@ public:
                 cap_vbins_ = std::max(vb, 2 * cap_vbins_);
                 CK(cudaMalloc(&d_vox_hist_, sizeof(int) * cap_vbins_));
                 CK(cudaMalloc(&d_vox_base_, sizeof(int) * cap_vbins_));
-                if (!d_vox_total_) CK(cudaMalloc(&d_vox_total_, sizeof(int)));
+                if (!d_vox_total_) {
+                    CK(cudaMalloc(&d_vox_total_, sizeof(int)));
+                    CK(cudaMemsetAsync(d_vox_total_, 0, sizeof(int), stream_));
+                }
             }
             if (std::max<size_t>(1, vox_total) > cap_vperm_) {
                 cudaFree(d_vox_perm_);
@@ -962,11 +975,13 @@ public:
 
     // One step of the batch; returns the number of kernels it launched.
     int launch_step(cudaStream_t st, bool prof) {
-        int launched = 7 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
+        int launched = 3 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
         const dev::Item* li = d_items_;
         const dev::Item* ci = d_items_ + n_link_items_;
         const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
-        if (bins_dirty_ || bin_phase_ % bin_every_ == 0) {
+        const bool regroup = bins_dirty_ || (batch_links_ >= kRegroupEveryStepLinks && bin_phase_ % bin_every_ == 0);
+        const bool regroup_voxels = regroup;
+        if (regroup) {
             // windows of about 16k links: a window's link state stays in L2 while its key groups run
             const int win = std::max(1, 16384 / std::max(1, items_links_));
             ks_.bins(std::max(1, std::min(n_link_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, li, n_link_items_, 0, win, d_link_hist_,
@@ -977,20 +992,28 @@ public:
         }
         bin_phase_++;
         if (prof) cudaEventRecord(evk_[0], st);
-        ks_.links(sm_count_ * 2 * std::max(1, 256 / block_links_), block_links_, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_, d_tickets_);
+        // persistent grids, but no more blocks than the batch has 256-element pieces: every warp
+        // of a block claims at least one chunk, and idle claims cost atomics in small batches
+        auto grid_chunks = [&](size_t elems, int block) {
+            const size_t full = (size_t)sm_count_ * 2 * std::max(1, 256 / block);
+            return (int)std::max<size_t>(1, std::min(full, (elems + 255) / 256));
+        };
+        ks_.links(grid_chunks(batch_links_, block_links_), block_links_, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
+                  (int)cap_perm_, cap_slots_, d_tickets_);
         if (prof) cudaEventRecord(evk_[1], st);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
-        {
-            // voxel grouping every step (floor contact changes often); windows of about 16k voxels
+        if (regroup_voxels) {
+            // voxel grouping with the links' (floor contact changes often); windows of about 16k voxels
             const int win = std::max(1, 16384 / std::max(1, items_voxels_));
             ks_.bins(std::max(1, std::min(n_vox_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, vi, n_vox_items_, 1, win, d_vox_hist_,
                      d_vox_base_, d_vox_total_, d_vox_perm_);
+            launched += 3;
         }
         if (prof) cudaEventRecord(evk_[3], st);
-        ks_.voxels(sm_count_ * 2 * std::max(1, 256 / block_voxels_), block_voxels_, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
-                   d_tickets_);
+        ks_.voxels(grid_chunks(batch_voxels_, block_voxels_), block_voxels_, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
+                   (int)cap_vperm_, cap_slots_, d_tickets_);
         if (prof) cudaEventRecord(evk_[4], st);
         ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_);
         if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
@@ -1001,6 +1024,7 @@ public:
     // count, the stop formula is not applied), one copy of the lists and one kernel.
     int set_running(const std::vector<int>& slots, const std::vector<int64_t>& targets, std::string* err, int no_stop = 0) {
         if (slots.empty()) return 0;
+        bins_dirty_ = true;   // simulations (re)started: the next step regroups with them
         const size_t n = slots.size(), o_tg = ((4 * n + 15) & ~(size_t)15), total = o_tg + 8 * n;
         if (int e = pinned(&rb_, total, err)) return e;
         if (total > cap_gather_) {
@@ -1104,6 +1128,7 @@ public:
                 graph_launches_ = 0;
                 for (int k = 0; k < graph_steps_; k++) graph_launches_ += launch_step(stream_, false);
                 CK(cudaStreamEndCapture(stream_, &g));
+                bins_dirty_ = true;   // captured kernels have not run: the next eager step regroups
                 CK(cudaGraphInstantiate(&graph_, g, 0));
                 cudaGraphDestroy(g);
                 graph_len_ = graph_steps_;
@@ -1372,6 +1397,7 @@ public:
             graph_launches_ = 0;
             for (int s = 0; s < k; s++) graph_launches_ += launch_step(stream_, false);
             CK(cudaStreamEndCapture(stream_, &g));
+            bins_dirty_ = true;   // captured kernels have not run: the next eager step regroups
             CK(cudaGraphInstantiate(&graph_, g, 0));
             cudaGraphDestroy(g);
             graph_len_ = k;

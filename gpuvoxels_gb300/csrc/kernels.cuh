@@ -446,9 +446,9 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sim
 // Warps take 32-link chunks of the binned list (one atomic per chunk); each lane
 // updates one link of whatever simulation it belongs to.
 __global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
-                                                                     const int* __restrict__ total, int* tickets) {
+                                                                     const int* __restrict__ total, int cap, int n_slots, int* tickets) {
     if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; }
-    const int n = *total;
+    const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
     for (;;) {
         int chunk = 0;
@@ -458,8 +458,10 @@ __global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* 
         if (chunk * 32 >= n) break;
         if (k < n) {
             const int2 e = __ldg(perm + k);
+            if ((unsigned)e.x >= (unsigned)n_slots) continue;   // never: the grouping lists running slots
             Ctl& c = ctl[e.x];
             if (c.status != 1) continue;   // stopped since the grouping was made
+            if ((unsigned)e.y >= (unsigned)sims[e.x].nl) continue;
             bool div = false;
             link_update(sims[e.x], e.y, c.dt, &div);
             if (div) c.diverged = 1;
@@ -1051,11 +1053,11 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
 }
 
 __global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
-                                                                       const int* __restrict__ total, int* tickets) {
+                                                                       const int* __restrict__ total, int cap, int n_slots, int* tickets) {
     // the voxels of the running simulations, grouped by key like the links (k_bin_*); warps
     // take 32-voxel chunks, so no warp waits at a block barrier for a costlier one
     if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
-    const int n = *total;
+    const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
     for (;;) {
         int chunk = 0;
@@ -1065,9 +1067,10 @@ __global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim
         const int k = chunk * 32 + lane;
         if (k < n) {
             const int2 e = __ldg(perm + k);
+            if ((unsigned)e.x >= (unsigned)n_slots) continue;   // never: the grouping lists running slots
             const Ctl& c = ctl[e.x];
             const float dt = c.dt;
-            if (c.status == 1 && !c.diverged && dt != 0.0f) {
+            if (c.status == 1 && !c.diverged && dt != 0.0f && (unsigned)e.y < (unsigned)sims[e.x].nv) {
                 const Sim& S = sims[e.x];
                 StepTimes st;
                 st.t_now = c.t; st.t_next = c.t + dt; st.t_cycles = c.t_cycles; st.angle = c.recent_angle;
@@ -1360,12 +1363,14 @@ inline void l_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item*
     k_bin_scan<<<1, 1024, 0, s>>>(hist, base, n, win, total);
     k_bin_scatter<<<g, 256, 0, s>>>(sims, ctl, it, n, kind, base, perm);
 }
-inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int* tk) {
-    k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, tk);
+inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
+                    int* tk) {
+    k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk);
 }
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
-inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int* tk) {
-    k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, tk);
+inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
+                     int* tk) {
+    k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk);
 }
 inline void l_sim_end(cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
     if (n > 0) k_sim_end<<<n, 256, 0, s>>>(sims, ctl, slots, n);

@@ -14,9 +14,12 @@ struct KernelSet {
     // (simulation, element) pairs)
     void (*bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int kind, int win, int* hist,
                  int* base, int* total, int2* perm);
-    void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int* tickets);
+    // perm holds at most `cap` entries; entries name slots below n_slots
+    void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int cap,
+                  int n_slots, int* tickets);
     void (*contacts)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
-    void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int* tickets);
+    void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int cap,
+                   int n_slots, int* tickets);
     // the end of the step for n simulations (slot list): centre-of-mass sample, time, stop
     void (*sim_end)(cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
     // VX3 signals relayed between neighbours (after voxels, over the voxel items)
