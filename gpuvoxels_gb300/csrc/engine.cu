@@ -980,12 +980,15 @@ public:
         const dev::Item* ci = d_items_ + n_link_items_;
         const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
         const bool regroup = bins_dirty_ || (batch_links_ >= kRegroupEveryStepLinks && bin_phase_ % bin_every_ == 0);
-        const bool regroup_voxels = regroup;
         if (regroup) {
-            // windows of about 16k links: a window's link state stays in L2 while its key groups run
-            const int win = std::max(1, 16384 / std::max(1, items_links_));
-            ks_.bins(std::max(1, std::min(n_link_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, li, n_link_items_, 0, win, d_link_hist_,
-                     d_link_base_, d_link_total_, d_link_perm_);
+            // links and voxels grouped together (the voxel keys come from the last voxel
+            // update, so nothing of this step changes them); windows of about 16k elements keep
+            // a window's state in L2 while its key groups run
+            dev::BinList lb{li, n_link_items_, 0, std::max(1, 16384 / std::max(1, items_links_)), 0, d_link_hist_, d_link_base_,
+                            d_link_total_, d_link_perm_};
+            dev::BinList vb{vi, n_vox_items_, 1, std::max(1, 16384 / std::max(1, items_voxels_)), 0, d_vox_hist_, d_vox_base_,
+                            d_vox_total_, d_vox_perm_};
+            ks_.bins(std::max(1, std::min(n_link_items_ + n_vox_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, lb, vb);
             bins_dirty_ = false;
             bin_phase_ = 0;
             launched += 3;
@@ -994,25 +997,18 @@ public:
         if (prof) cudaEventRecord(evk_[0], st);
         // persistent grids, but no more blocks than the batch has 256-element pieces: every warp
         // of a block claims at least one chunk, and idle claims cost atomics in small batches
-        auto grid_chunks = [&](size_t elems, int block) {
-            const size_t full = (size_t)sm_count_ * 2 * std::max(1, 256 / block);
+        auto grid_chunks = [&](size_t elems, int block, int which) {
+            const size_t full = (size_t)sm_count_ * ks_.resident_blocks(which) * std::max(1, 256 / block);
             return (int)std::max<size_t>(1, std::min(full, (elems + 255) / 256));
         };
-        ks_.links(grid_chunks(batch_links_, block_links_), block_links_, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
+        ks_.links(grid_chunks(batch_links_, block_links_, 0), block_links_, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
                   (int)cap_perm_, cap_slots_, d_tickets_);
         if (prof) cudaEventRecord(evk_[1], st);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
-        if (regroup_voxels) {
-            // voxel grouping with the links' (floor contact changes often); windows of about 16k voxels
-            const int win = std::max(1, 16384 / std::max(1, items_voxels_));
-            ks_.bins(std::max(1, std::min(n_vox_items_, 4 * sm_count_)), st, d_sims_, d_ctl_, vi, n_vox_items_, 1, win, d_vox_hist_,
-                     d_vox_base_, d_vox_total_, d_vox_perm_);
-            launched += 3;
-        }
         if (prof) cudaEventRecord(evk_[3], st);
-        ks_.voxels(grid_chunks(batch_voxels_, block_voxels_), block_voxels_, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
+        ks_.voxels(grid_chunks(batch_voxels_, block_voxels_, 1), block_voxels_, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
                    (int)cap_vperm_, cap_slots_, d_tickets_);
         if (prof) cudaEventRecord(evk_[4], st);
         ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_);

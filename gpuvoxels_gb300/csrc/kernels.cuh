@@ -340,12 +340,15 @@ __device__ __forceinline__ int bin_key(const Sim& S, int kind, int begin, int j)
 // barriers: warps of cheap small-angle links waited for warps of costly large-angle
 // ones.  Grouping across the whole batch at once made every key group a separate
 // pass over all link state and tripled k_links' DRAM traffic.)
-__global__ void __launch_bounds__(256) k_bin_hist(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                  int n_items, int kind, int* hist) {
+__global__ void __launch_bounds__(256) k_bin_hist(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, BinList la, BinList lb) {
     __shared__ int wc[kOrderKeys * 8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-        const Item w = items[it];
+    for (int g = blockIdx.x; g < la.n_items + lb.n_items; g += gridDim.x) {
+        const bool first = g < la.n_items;       // the two lists' items share the grid
+        const int it = first ? g : g - la.n_items;
+        const int kind = first ? la.kind : lb.kind;
+        int* hist = first ? la.hist : lb.hist;
+        const Item w = (first ? la.items : lb.items)[it];
         const bool run = ctl[w.sim].status == 1;
         const Sim& S = sims[w.sim];
         const int n = w.end - w.begin;
@@ -371,8 +374,13 @@ __global__ void __launch_bounds__(256) k_bin_hist(const Sim* __restrict__ sims, 
 // by key, item by item, so base[item][key] = links of earlier windows + links of
 // smaller keys in the window + links of that key in earlier items of the window.
 // Each thread scans a contiguous run of that order; the runs are joined by a block scan.
-__global__ void __launch_bounds__(1024) k_bin_scan(const int* __restrict__ hist, int* base, int n_items, int win, int* total) {
+__global__ void __launch_bounds__(1024) k_bin_scan(BinList la, BinList lb) {
     __shared__ int s_sum[1024];
+    const BinList& L = blockIdx.x == 0 ? la : lb;   // one block per list
+    const int* hist = L.hist;
+    int* base = L.base;
+    const int n_items = L.n_items, win = L.win;
+    int* total = L.total;
     const int n_win = (n_items + win - 1) / win;
     const int N = n_win * win * kOrderKeys;
     const int per = (N + blockDim.x - 1) / blockDim.x;
@@ -408,13 +416,17 @@ __global__ void __launch_bounds__(1024) k_bin_scan(const int* __restrict__ hist,
     if (threadIdx.x == blockDim.x - 1) *total = s_sum[blockDim.x - 1];
 }
 
-__global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                     int n_items, int kind, const int* __restrict__ base, int2* perm) {
+__global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, BinList la, BinList lb) {
     __shared__ int wc[kOrderKeys * 8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-        const Item w = items[it];
+    for (int g = blockIdx.x; g < la.n_items + lb.n_items; g += gridDim.x) {
+        const bool first = g < la.n_items;
+        const int it = first ? g : g - la.n_items;
+        const int kind = first ? la.kind : lb.kind;
+        const int* base = first ? la.base : lb.base;
+        int2* perm = first ? la.perm : lb.perm;
+        const Item w = (first ? la.items : lb.items)[it];
         if (ctl[w.sim].status != 1) continue;   // the same for the whole block
         const Sim& S = sims[w.sim];
         int start[kOrderKeys];
@@ -1357,11 +1369,10 @@ __global__ void k_com(const Sim* __restrict__ sims, int sim, double* out4) {
 // ---------------------------------------------------------------- launch table
 namespace gvx {
 namespace GVX_KNS {
-inline void l_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int kind, int win, int* hist, int* base,
-                   int* total, int2* perm) {
-    k_bin_hist<<<g, 256, 0, s>>>(sims, ctl, it, n, kind, hist);
-    k_bin_scan<<<1, 1024, 0, s>>>(hist, base, n, win, total);
-    k_bin_scatter<<<g, 256, 0, s>>>(sims, ctl, it, n, kind, base, perm);
+inline void l_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, BinList la, BinList lb) {
+    k_bin_hist<<<g, 256, 0, s>>>(sims, ctl, la, lb);
+    k_bin_scan<<<2, 1024, 0, s>>>(la, lb);
+    k_bin_scatter<<<g, 256, 0, s>>>(sims, ctl, la, lb);
 }
 inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
                     int* tk) {
@@ -1396,8 +1407,21 @@ inline void l_com(cudaStream_t s, const Sim* sims, int sim, double* out4) { k_co
 inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int64_t* off, int n, double* pos3, double* q4, uint8_t* fl) {
     if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
 }
+// Resident 256-thread blocks per SM of the persistent grids (what the register use allows).
+inline int l_resident_blocks(int which) {
+    static int cached[2] = {0, 0};
+    int& n = cached[which ? 1 : 0];
+    if (n == 0) {
+        int r = 0;
+        if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_links, 256, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_voxels, 256, 0);
+        n = r > 0 ? r : 1;
+    }
+    return n;
+}
 inline KernelSet make_kernelset(const char* name) {
-    return KernelSet{name, l_bins, l_links, l_contacts, l_voxels, l_sim_end, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com, l_gather};
+    return KernelSet{name, l_bins, l_links, l_contacts, l_voxels, l_sim_end, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com,
+                     l_gather, l_resident_blocks};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

@@ -9,11 +9,9 @@ namespace gvx {
 
 struct KernelSet {
     const char* name;
-    // groups the links (kind 0) or voxels (kind 1) of the running simulations by key in windows
-    // of `win` work items (hist, base: per item and key; total: elements listed; perm:
-    // (simulation, element) pairs)
-    void (*bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int kind, int win, int* hist,
-                 int* base, int* total, int2* perm);
+    // groups the elements of the running simulations by key for two lists at once (links and
+    // voxels), in windows of work items
+    void (*bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, dev::BinList links, dev::BinList voxels);
     // perm holds at most `cap` entries; entries name slots below n_slots
     void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int cap,
                   int n_slots, int* tickets);
@@ -35,6 +33,8 @@ struct KernelSet {
     // n simulations (slot[k], output offset off[k]) into pos3 / q4 / flags (one launch).
     void (*gather)(cudaStream_t s, const dev::Sim* sims, const int* slot, const int64_t* off, int n, double* pos3, double* q4,
                    uint8_t* flags);
+    // resident 256-thread blocks per SM of k_links (0) or k_voxels (1)
+    int (*resident_blocks)(int which);
 };
 
 KernelSet kernelset_exact();   // every multiply and add rounded separately (the reference's CPU rounding)

@@ -191,5 +191,17 @@ struct Item {
     int32_t sim, begin, end, seq;
 };
 
+// One list to group by key (k_bin_*): its work items, the element kind (0 links,
+// 1 voxels), the window in items, and the per-item counts / offsets, the listed
+// count and the (simulation, element) list.
+struct BinList {
+    const Item* items;
+    int32_t n_items, kind, win, pad;
+    int32_t* hist;
+    int32_t* base;
+    int32_t* total;
+    int2* perm;
+};
+
 }  // namespace dev
 }  // namespace gvx
