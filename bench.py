@@ -50,11 +50,11 @@ def measured_peaks():
 # FP64-pipe thread instructions (DADD/DMUL/DFMA, compares, conversions; predicated-on lanes)
 # per link and per voxel of one step of the batch workload, read by ncu at step 205
 # (sm__thread_inst_executed_pipe_fp64_pred_on.sum ÷ links or voxels; profiles/k_links_k_voxels_batch512_steady.md).
-FP64_INSTR_PER_LINK = 684887264 / 1627115      # 420.9
-FP64_INSTR_PER_VOXEL = 240932736 / 844972      # 285.1
+FP64_INSTR_PER_LINK = 684878336 / 1627115      # 420.9
+FP64_INSTR_PER_VOXEL = 236663360 / 844972      # 280.1
 # DRAM bytes per link of one k_links launch at the same step (ncu dram__bytes_read.sum +
 # dram__bytes_write.sum = 410.2 MB + 358.0 MB for 1,627,115 links).
-LINK_TRAFFIC_PER_LINK = (410241536 + 357970176) / 1627115
+LINK_TRAFFIC_PER_LINK = (410284544 + 358874112) / 1627115
 
 
 def fp64_peak_fma_per_s(device=0):

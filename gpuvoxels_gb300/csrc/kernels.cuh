@@ -304,13 +304,18 @@ struct LinkKey {
 // Voxel key: touched the floor last step (contact and friction branches) and, if so,
 // held by static friction (the kinetic branch forms the sliding direction), then
 // surface voxels (Poisson strain by pow) apart from interior ones.
+// Voxel key: floor contact with kinetic (0, 1) or static (2, 3) friction, else surface
+// (4, 6) or interior (5, 7) voxel; the lower key of each pair when the last orientation
+// update took the sin/cos branch.  (Voxels touching the floor are not told apart by
+// interior: they are almost always surface voxels.)
 struct VoxelKey {
     const uint32_t* vfl;
     int begin;
     __device__ int operator()(int j) const {
         const uint32_t f = vfl[begin + j];
-        const int floor = (f & VF_FLOORC) ? ((f & VF_STATIC) ? 2 : 3) : 0;
-        return 2 * floor + ((f & VF_INTERIOR) ? 1 : 0);
+        const int narrow = (f & VF_WROT) ? 0 : 1;
+        if (f & VF_FLOORC) return ((f & VF_STATIC) ? 2 : 0) + narrow;
+        return 4 + 2 * narrow + ((f & VF_INTERIOR) ? 1 : 0);
     }
 };
 
@@ -781,10 +786,11 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         lm = am = D3(0, 0, 0);
     } else {
         // force()
-        d3 F = D3(0, 0, 0);
+        // the sum starts at +0, so its first term (direction 0) adds exactly as plus_zero
         const double* sf = S.sf;
+        d3 F = (fl & 1u) ? D3(fp64i::plus_zero(sf[v]), fp64i::plus_zero(sf[nv + v]), fp64i::plus_zero(sf[2 * nv + v])) : D3(0, 0, 0);
 #pragma unroll
-        for (int d = 0; d < 6; d++)
+        for (int d = 1; d < 6; d++)
             if (fl & (1u << d)) F = D3(F.x + sf[(d * 3) * nv + v], F.y + sf[(d * 3 + 1) * nv + v], F.z + sf[(d * 3 + 2) * nv + v]);
         F = qrot(q, F);
         if (e) { F.x += e->f[0]; F.y += e->f[1]; F.z += e->f[2]; }
@@ -860,10 +866,10 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         }
         pos = D3(pos.x + tr.x, pos.y + tr.y, pos.z + tr.z);
         // moment()
-        d3 M = D3(0, 0, 0);
         const double* sm = S.sm;
+        d3 M = (fl & 1u) ? D3(fp64i::plus_zero(sm[v]), fp64i::plus_zero(sm[nv + v]), fp64i::plus_zero(sm[2 * nv + v])) : D3(0, 0, 0);
 #pragma unroll
-        for (int d = 0; d < 6; d++)
+        for (int d = 1; d < 6; d++)
             if (fl & (1u << d)) M = D3(M.x + sm[(d * 3) * nv + v], M.y + sm[(d * 3 + 1) * nv + v], M.z + sm[(d * 3 + 2) * nv + v]);
         M = qrot(q, M);
         if (e) { M.x += e->m[0]; M.y += e->m[1]; M.z += e->m[2]; }
@@ -871,7 +877,9 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         M = D3(M.x - m.gDampRD * wx, M.y - m.gDampRD * wy, M.z - m.gDampRD * wz);
         am = D3(am.x + dtd * M.x, am.y + dtd * M.y, am.z + dtd * M.z);
         const double sI = f2d(dt * m.Iinv);
-        q = qmul(q_from_rotvec(D3(sI * am.x, sI * am.y, sI * am.z)), q);
+        bool wrot = false;
+        q = qmul(q_from_rotvec(D3(sI * am.x, sI * am.y, sI * am.z), &wrot), q);
+        fl = wrot ? (fl | VF_WROT) : (fl & ~VF_WROT);
         if (e) {
             const int d = e->dof;
             if (d & 1) { pos.x = S.ijk[v] * m.nom + e->tr[0]; lm.x = 0; }

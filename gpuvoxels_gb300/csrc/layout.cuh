@@ -32,6 +32,7 @@ constexpr uint32_t VF_FLOORC = 1u << 10;  // last step: the voxel touched the fl
 constexpr uint32_t VF_REMOVED = 1u << 11; // VX3: removed from the simulation (frozen, no links, no contacts)
 constexpr uint32_t VF_TGTHIT = 1u << 12;  // VX3: this step's contacts include a target voxel (non-target voxel)
 constexpr uint32_t VF_ATTACH = 1u << 13;  // VX3: enableAttach (every attach condition holds at the voxel)
+constexpr uint32_t VF_WROT = 1u << 14;    // last step: the orientation update took the sin/cos branch (grouping key only)
 
 // sim flag bits
 constexpr int SF_FLOOR = 1, SF_COLLIDE = 2, SF_VARY = 4, SF_EXPAND = 8;

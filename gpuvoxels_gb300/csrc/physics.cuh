@@ -135,7 +135,8 @@ __device__ __forceinline__ d3 q_to_rotvec(const q4& q, bool* wide = nullptr) {
     return D3(kX0 ? times_zero(inv, times_zero(a, q.x)) : (mul2(q.x) * a) * inv, (mul2(q.y) * a) * inv, (mul2(q.z) * a) * inv);
 }
 // Quat3D::FromRotationVector  Quat3D.h:128-143
-__device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
+// *wide = the sin/cos branch was taken
+__device__ __forceinline__ q4 q_from_rotvec(const d3& v, bool* wide = nullptr) {
     double tx = half(v.x), ty = half(v.y), tz = half(v.z);
     double m2 = tx * tx + ty * ty + tz * tz;
     double w, s;
@@ -143,6 +144,7 @@ __device__ __forceinline__ q4 q_from_rotvec(const d3& v) {
         w = 1.0 - half(m2);
         s = 1.0 - m2 / 6.0;
     } else {
+        if (wide) *wide = true;
         double m = sqrt(m2);
         double sn, cs;
         sincos(m, &sn, &cs);
