@@ -995,20 +995,21 @@ public:
         }
         bin_phase_++;
         if (prof) cudaEventRecord(evk_[0], st);
-        // persistent grids, but no more blocks than the batch has 256-element pieces: every warp
+        // persistent grids, but no more blocks than the batch has block-sized pieces: every warp
         // of a block claims at least one chunk, and idle claims cost atomics in small batches
+        const int bl = std::min(block_links_, ks_.max_block), bv = std::min(block_voxels_, ks_.max_block);
         auto grid_chunks = [&](size_t elems, int block, int which) {
-            const size_t full = (size_t)sm_count_ * ks_.resident_blocks(which) * std::max(1, 256 / block);
-            return (int)std::max<size_t>(1, std::min(full, (elems + 255) / 256));
+            const size_t full = (size_t)sm_count_ * ks_.resident_blocks(which, block);
+            return (int)std::max<size_t>(1, std::min(full, (elems + block - 1) / block));
         };
-        ks_.links(grid_chunks(batch_links_, block_links_, 0), block_links_, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
+        ks_.links(grid_chunks(batch_links_, bl, 0), bl, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
                   (int)cap_perm_, cap_slots_, d_tickets_);
         if (prof) cudaEventRecord(evk_[1], st);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
         if (prof) cudaEventRecord(evk_[3], st);
-        ks_.voxels(grid_chunks(batch_voxels_, block_voxels_, 1), block_voxels_, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
+        ks_.voxels(grid_chunks(batch_voxels_, bv, 1), bv, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
                    (int)cap_vperm_, cap_slots_, d_tickets_);
         if (prof) cudaEventRecord(evk_[4], st);
         ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_);

@@ -326,6 +326,9 @@ __device__ __forceinline__ int bin_key(const Sim& S, int kind, int begin, int j)
 
 // Resident blocks per SM the register allocation of k_links / k_voxels is sized for
 // (a build-time tuning knob: -DGVX_LINKS_MIN_BLOCKS=3 trades registers for warps).
+#ifndef GVX_STEP_BLOCK
+#define GVX_STEP_BLOCK 256   // largest block of k_links / k_voxels (the register budget is sized for it)
+#endif
 #ifndef GVX_LINKS_MIN_BLOCKS
 #define GVX_LINKS_MIN_BLOCKS 2
 #endif
@@ -462,7 +465,7 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sim
 
 // Warps take 32-link chunks of the binned list (one atomic per chunk); each lane
 // updates one link of whatever simulation it belongs to.
-__global__ void __launch_bounds__(256, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
+__global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
                                                                      const int* __restrict__ total, int cap, int n_slots, int* tickets) {
     if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; }
     const int n = min(*total, cap);
@@ -1072,7 +1075,7 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
     if (stop) c.status = 2;
 }
 
-__global__ void __launch_bounds__(256, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
+__global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
                                                                        const int* __restrict__ total, int cap, int n_slots, int* tickets) {
     // the voxels of the running simulations, grouped by key like the links (k_bin_*); warps
     // take 32-voxel chunks, so no warp waits at a block barrier for a costlier one
@@ -1415,21 +1418,22 @@ inline void l_com(cudaStream_t s, const Sim* sims, int sim, double* out4) { k_co
 inline void l_gather(cudaStream_t s, const Sim* sims, const int* slot, const int64_t* off, int n, double* pos3, double* q4, uint8_t* fl) {
     if (n > 0) k_gather<<<dim3(8, (unsigned)n), 256, 0, s>>>(sims, slot, off, n, pos3, q4, fl);
 }
-// Resident 256-thread blocks per SM of the persistent grids (what the register use allows).
-inline int l_resident_blocks(int which) {
-    static int cached[2] = {0, 0};
-    int& n = cached[which ? 1 : 0];
+// Resident blocks per SM of the persistent grids at a block size (what the register use allows).
+inline int l_resident_blocks(int which, int block) {
+    static int cached[2][33] = {};
+    block = block < 32 ? 32 : (block > 1024 ? 1024 : block & ~31);
+    int& n = cached[which ? 1 : 0][block >> 5];
     if (n == 0) {
         int r = 0;
-        if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_links, 256, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_voxels, 256, 0);
+        if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_links, block, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_voxels, block, 0);
         n = r > 0 ? r : 1;
     }
     return n;
 }
 inline KernelSet make_kernelset(const char* name) {
     return KernelSet{name, l_bins, l_links, l_contacts, l_voxels, l_sim_end, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com,
-                     l_gather, l_resident_blocks};
+                     l_gather, l_resident_blocks, GVX_STEP_BLOCK};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

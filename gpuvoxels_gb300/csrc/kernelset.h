@@ -33,8 +33,9 @@ struct KernelSet {
     // n simulations (slot[k], output offset off[k]) into pos3 / q4 / flags (one launch).
     void (*gather)(cudaStream_t s, const dev::Sim* sims, const int* slot, const int64_t* off, int n, double* pos3, double* q4,
                    uint8_t* flags);
-    // resident 256-thread blocks per SM of k_links (0) or k_voxels (1)
-    int (*resident_blocks)(int which);
+    // resident blocks per SM of k_links (0) or k_voxels (1) at a block size
+    int (*resident_blocks)(int which, int block);
+    int max_block;   // largest block k_links / k_voxels are compiled for
 };
 
 KernelSet kernelset_exact();   // every multiply and add rounded separately (the reference's CPU rounding)
