@@ -307,23 +307,26 @@ def run_ours(args):
     # ---- end to end through the C ABI with host buffers: parse+load, upload, K steps, read back
     e2e = None
     if rank == 0:
-        c2 = g.Context(local, budget)
-        c2.set_precision(prec)
-        h0, d0 = c2.transfer_bytes()
-        t0 = time.perf_counter()
-        ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
-        c2.step(ids2, args.steps, g.BATCHED)
-        pos, q, fl, _ = c2.get_states(ids2)      # every creature's pose, one device pass and one copy
-        e2e_wall = time.perf_counter() - t0
-        h1, d1 = c2.transfer_bytes()             # bytes the engine copied each way in the timed region
-        h2d, d2h = h1 - h0, d1 - d0
-        e2e_vs = sum(c2.info(i).num_voxel for i in ids2) * args.steps
-        c2.close()
+        walls = []
+        for _ in range(args.e2e_reps):           # each a fresh context: parse, upload, steps, read-back
+            c2 = g.Context(local, budget)
+            c2.set_precision(prec)
+            h0, d0 = c2.transfer_bytes()
+            t0 = time.perf_counter()
+            ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
+            c2.step(ids2, args.steps, g.BATCHED)
+            pos, q, fl, _ = c2.get_states(ids2)      # every creature's pose, one device pass and one copy
+            walls.append(time.perf_counter() - t0)
+            h1, d1 = c2.transfer_bytes()             # bytes the engine copied each way in the timed region
+            h2d, d2h = h1 - h0, d1 - d0
+            e2e_vs = sum(c2.info(i).num_voxel for i in ids2) * args.steps
+            c2.close()
+        e2e_wall = sorted(walls)[len(walls) // 2]
         e2e = dict(value=e2e_vs / e2e_wall, unit="voxel-steps/s", h2d_bytes_per_step=int(h2d / args.steps),
-                   d2h_bytes_per_step=int(d2h / args.steps),
-                   note="wall clock of vx3_load_vxa_many (host VXA parse + topology for every creature, on "
-                        f"host threads), the upload, {args.steps} batched steps and vx3_get_states (every voxel's "
-                        "pose, one device pass and one copy)")
+                   d2h_bytes_per_step=int(d2h / args.steps), runs_s=[round(w, 4) for w in walls],
+                   note=f"median of {len(walls)} runs, each the wall clock of vx3_load_vxa_many (host VXA parse + "
+                        "topology for every creature, on host threads), the upload, "
+                        f"{args.steps} batched steps and vx3_get_states (every voxel's pose, one device pass and one copy)")
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -460,6 +463,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--e2e-reps", type=int, default=3, help="end-to-end runs (fresh contexts); the median is reported")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "slab", "collide", "plain", "serve"])

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <deque>
 #include <thread>
+#include <unordered_set>
 
 namespace gvx {
 
@@ -185,6 +186,7 @@ public:
     };
     Pinned up_[2];
     int up_next_ = 0;
+    Pinned gen_;   // the images of one generation of uploads (upload_many)
     Pinned rb_;
     char* d_gather_ = nullptr;
     size_t cap_gather_ = 0;
@@ -194,7 +196,7 @@ public:
         if (graph_) cudaGraphExecDestroy(graph_);
         cudaSetDevice(device_);
         if (stream_) cudaStreamSynchronize(stream_);
-        for (Pinned* b : {&up_[0], &up_[1], &rb_}) {
+        for (Pinned* b : {&up_[0], &up_[1], &rb_, &gen_}) {
             if (b->p) cudaFreeHost(b->p);
             if (b->done) cudaEventDestroy(b->done);
         }
@@ -230,7 +232,7 @@ public:
         CK(cudaMalloc(&d_tickets_, 4 * sizeof(int)));
         CK(cudaMemset(d_tickets_, 0, 4 * sizeof(int)));
         CK(cudaMalloc(&d_com4_, 4 * sizeof(double)));
-        for (Pinned* b : {&up_[0], &up_[1], &rb_}) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+        for (Pinned* b : {&up_[0], &up_[1], &rb_, &gen_}) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
         return grow_slots(64, err);
     }
 
@@ -415,6 +417,7 @@ public:
     }
 
     int add_sims(const SimDesc* const* descs, int n, int64_t* ids, std::string* errs) override {
+        TraceClock tc;
         std::vector<std::unique_ptr<SimRec>> recs((size_t)std::max(n, 0));
         std::vector<char> ok((size_t)std::max(n, 0), 0);
         std::atomic<int> next{0};
@@ -429,6 +432,7 @@ public:
         for (int t = 1; t < nt; t++) pool.emplace_back(work);
         work();
         for (auto& t : pool) t.join();
+        tc.mark("add_sims: topology (threads)");
         int rejected = 0;
         const double now = now_s() - t0_;
         for (int i = 0; i < n; i++) {
@@ -492,15 +496,20 @@ public:
         return upload_finish(one, err);
     }
 
-    // First half of an upload, without waiting for the device: region image, copies and
-    // the initial temperature / stable-step / hash kernels.  Many simulations are begun
-    // and then finished together (one synchronisation for the whole generation).
-    int upload_begin(SimRec* r, std::string* err) {
-        SimWorld& w = r->w;
+    // Region of one simulation being uploaded: its layout and where it sits in the arena.
+    struct UpPlan {
         Layout L;
         Offs o;
+        size_t off = 0;
+    };
+
+    // Serial part of an upload: layout, arena region and slot.
+    int upload_reserve(SimRec* r, UpPlan* p, std::string* err) {
+        SimWorld& w = r->w;
+        Layout& L = p->L;
+        Offs& o = p->o;
         compute_layout(w, &L, &o);
-        size_t off;
+        size_t& off = p->off;
         if (!arena_.alloc(L.total, &off)) {
             if (err) *err = "HBM budget exhausted";
             return -2;
@@ -515,28 +524,19 @@ public:
         r->slot = slot;
         r->off = off;
         r->bytes = L.total;
-        char* base = arena_base_ + off;
-        // host image of the region's initialised part (the rest starts as zeros and is cleared
-        // on the device): built in a pinned staging buffer so that its copy runs asynchronously
-        // while the next simulation's image is filled (pageable for huge regions)
-        const size_t img = o.zero_from;
-        std::vector<char> hv;
-        char* hp = nullptr;
-        Pinned* stage = nullptr;
-        if (img <= kPinnedUploadMax) {
-            stage = &up_[up_next_];
-            up_next_ ^= 1;
-            if (int e = pinned(stage, img, err)) {
-                arena_.release(off, L.total);
-                slot_owner_[slot] = nullptr;
-                return e;
-            }
-            hp = stage->p;
-            memset(hp, 0, img);
-        } else {
-            hv.assign(img, 0);
-            hp = hv.data();
-        }
+        return 0;
+    }
+
+    // Host image of a reserved region's initialised part at hp (o.zero_from bytes), and the
+    // simulation's device descriptor and first control block.  Writes only hp and r, so the
+    // images of many simulations are filled at once on host threads.
+    void upload_fill(SimRec* r, const UpPlan& p, char* hp) const {
+        SimWorld& w = r->w;
+        const Layout& L = p.L;
+        const Offs& o = p.o;
+        char* base = arena_base_ + p.off;
+        (void)L;
+        memset(hp, 0, o.zero_from);
         const size_t nv = w.nv, nl = w.nl;
         auto P = [&](size_t o2) { return hp + o2; };
         // materials
@@ -733,9 +733,6 @@ public:
         S.n_mats = (int)w.vmats.size();
         S.reinit_after = dd.reinit_initial_after;
         if (dd.secondary_experiment) S.init_pos = (double*)D(o.init_pos);
-        CK(copy_async(base, hp, img, cudaMemcpyHostToDevice, stream_));
-        CK(cudaMemsetAsync(base + img, 0, L.total - img, stream_));
-        if (stage) CK(cudaEventRecord(stage->done, stream_));
         // the descriptor and control block go to the device with the others in upload_finish
         r->pending_sim = S;
         dev::Ctl c{};
@@ -746,6 +743,130 @@ public:
         for (int k = 0; k < 3; k++) c.com[k] = c.init_com[k] = r->init_com[k];
         c.n_links = w.nl;
         r->pending_ctl = c;
+    }
+
+    // Copies a filled image to its region and clears the rest of the region on the device.
+    int upload_copy(SimRec* r, const UpPlan& p, const char* hp, std::string* err) {
+        char* base = arena_base_ + p.off;
+        const size_t img = p.o.zero_from;
+        CK(copy_async(base, hp, img, cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemsetAsync(base + img, 0, p.L.total - img, stream_));
+        (void)r;
+        return 0;
+    }
+
+    // First half of an upload of one simulation, without waiting for the device: region
+    // image in a pinned staging buffer (pageable for huge regions) whose copy runs while the
+    // next simulation's image is filled.  Many simulations are begun and then finished
+    // together (one synchronisation for the whole generation); upload_many fills the images
+    // of a whole generation at once on host threads.
+    int upload_begin(SimRec* r, std::string* err) {
+        UpPlan p;
+        if (int e = upload_reserve(r, &p, err)) return e;
+        const size_t img = p.o.zero_from;
+        std::vector<char> hv;
+        char* hp = nullptr;
+        Pinned* stage = nullptr;
+        if (img <= kPinnedUploadMax) {
+            stage = &up_[up_next_];
+            up_next_ ^= 1;
+            if (int e = pinned(stage, img, err)) {
+                arena_.release(p.off, p.L.total);
+                slot_owner_[r->slot] = nullptr;
+                return e;
+            }
+            hp = stage->p;
+        } else {
+            hv.resize(img);
+            hp = hv.data();
+        }
+        upload_fill(r, p, hp);
+        if (int e = upload_copy(r, p, hp, err)) return e;
+        if (stage) CK(cudaEventRecord(stage->done, stream_));
+        return 0;
+    }
+
+    // Begins the uploads of many simulations: regions reserved in order, every image filled
+    // on host threads into one pinned generation buffer, then the copies in order.  Returns
+    // the number begun (those before a failure) through *begun.
+    int upload_many(const std::vector<SimRec*>& rs, std::vector<SimRec*>* begun, std::string* err) {
+        std::vector<UpPlan> plans(rs.size());
+        std::vector<size_t> at(rs.size());
+        size_t total = 0;
+        size_t k = 0;
+        int rc = 0;
+        for (; k < rs.size(); k++) {
+            if ((rc = upload_reserve(rs[k], &plans[k], err))) break;
+            at[k] = total;
+            total += (plans[k].o.zero_from + 255) & ~(size_t)255;
+        }
+        const size_t n = k;
+        if (n == 0) return rc;
+        // on a failure below, the regions reserved but not begun are given back
+        auto unreserve_from = [&](size_t i0) {
+            for (size_t i = i0; i < n; i++) {
+                arena_.release(plans[i].off, plans[i].L.total);
+                slot_owner_[rs[i]->slot] = nullptr;
+            }
+        };
+        if (total > kPinnedUploadMax) {
+            // too large for one staging buffer: the regions are already reserved, so fill and
+            // copy them one at a time through the double-buffered staging
+            for (size_t i = 0; i < n; i++) {
+                const size_t img = plans[i].o.zero_from;
+                std::vector<char> hv;
+                char* hp;
+                Pinned* stage = nullptr;
+                if (img <= kPinnedUploadMax) {
+                    stage = &up_[up_next_];
+                    up_next_ ^= 1;
+                    if (int e = pinned(stage, img, err)) { unreserve_from(i); return e; }
+                    hp = stage->p;
+                } else {
+                    hv.resize(img);
+                    hp = hv.data();
+                }
+                upload_fill(rs[i], plans[i], hp);
+                if (int e = upload_copy(rs[i], plans[i], hp, err)) { unreserve_from(i); return e; }
+                if (stage) CK(cudaEventRecord(stage->done, stream_));
+                begun->push_back(rs[i]);
+            }
+            return rc;
+        }
+        TraceClock tc;
+        tc.mark("upload_many: reserve");
+        if (int e = pinned(&gen_, total, err)) { unreserve_from(0); return e; }
+        tc.mark("upload_many: pinned buffer");
+        std::atomic<size_t> next{0};
+        auto work = [&]() {
+            for (size_t i = next++; i < n; i = next++) upload_fill(rs[i], plans[i], gen_.p + at[i]);
+        };
+        const int nt = (int)std::max<size_t>(1, std::min<size_t>(n / 8, std::max(1u, std::thread::hardware_concurrency())));
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; t++) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+        tc.mark("upload_many: fill (threads)");
+        for (size_t i = 0; i < n; i++) {
+            if (int e = upload_copy(rs[i], plans[i], gen_.p + at[i], err)) { unreserve_from(i); return e; }
+            begun->push_back(rs[i]);
+        }
+        CK(cudaEventRecord(gen_.done, stream_));
+        tc.mark("upload_many: copies issued");
+        return rc;
+    }
+
+    // Copies per-simulation records img[k] to dev[slot of rs[k]]: one copy per run of
+    // consecutive slots (a fresh batch takes consecutive slots, so usually one in all).
+    template <typename T>
+    int copy_runs(T* dev, const T* img, const std::vector<SimRec*>& rs, std::string* err) {
+        size_t k = 0;
+        while (k < rs.size()) {
+            size_t e = k + 1;
+            while (e < rs.size() && rs[e]->slot == rs[e - 1]->slot + 1) e++;
+            CK(copy_async(dev + rs[k]->slot, img + k, sizeof(T) * (e - k), cudaMemcpyHostToDevice, stream_));
+            k = e;
+        }
         return 0;
     }
 
@@ -785,9 +906,9 @@ public:
             max_nv = std::max(max_nv, r->w.nv);
             max_nl = std::max(max_nl, r->w.nl);
             max_ns = std::max(max_ns, r->w.surface_count);
-            CK(copy_async(d_sims_ + r->slot, &sim_img[k], sizeof(dev::Sim), cudaMemcpyHostToDevice, stream_));
-            CK(copy_async(d_ctl_ + r->slot, &ctl0_img[k], sizeof(dev::Ctl), cudaMemcpyHostToDevice, stream_));
         }
+        if (int e = copy_runs(d_sims_, sim_img, rs, err)) return e;
+        if (int e = copy_runs(d_ctl_, ctl0_img, rs, err)) return e;
         CK(copy_async(d_gather_ + o_slot, h + o_slot, o_bits - o_slot, cudaMemcpyHostToDevice, stream_));
         const int* d_slots = (const int*)(d_gather_ + o_slot);
         const float* d_init = (const float*)(d_gather_ + o_init);
@@ -803,7 +924,9 @@ public:
         dev::Ctl* ctl_img = (dev::Ctl*)(h + o_ctl);
         CK(copy2d_async(bits_all, sizeof(uint32_t), &d_ctl_[0].maxf2_bits, sizeof(dev::Ctl), sizeof(uint32_t), cap_slots_,
                              cudaMemcpyDeviceToHost, stream_));
+        TraceClock tc;
         CK(cudaStreamSynchronize(stream_));
+        tc.mark("upload_finish: wait for copies");
         for (size_t k = 0; k < rs.size(); k++) {
             SimRec* r = rs[k];
             const SimWorld& w = r->w;
@@ -831,8 +954,8 @@ public:
             c.maxf2_bits = bits;
             // the first step ends at t = dt (currentTime starts at 0)
             c.t_cycles = (w.desc.vary_temp && w.desc.temp_period > 0) ? (0.0 + (double)c.dt) / w.desc.temp_period : 0.0;
-            CK(copy_async(d_ctl_ + r->slot, &c, sizeof(c), cudaMemcpyHostToDevice, stream_));
         }
+        if (int e = copy_runs(d_ctl_, ctl_img, rs, err)) return e;
         CK(cudaEventRecord(rb_.done, stream_));
         CK(cudaStreamSynchronize(stream_));
         for (SimRec* r : rs) {
@@ -1112,11 +1235,13 @@ public:
         } else {
             std::vector<int> slots;
             for (auto* r : rs) slots.push_back(r->slot);
+            TraceClock tc;
             if (batch_dirty_ || slots != batch_slots_) {
                 if (int e = build_items(slots, err)) return e;
                 batch_slots_ = slots;
                 if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
                 batch_dirty_ = false;
+                tc.mark("drive: build_items");
             }
             if (!graph_) {
                 cudaGraph_t g;
@@ -1126,9 +1251,11 @@ public:
                 for (int k = 0; k < graph_steps_; k++) graph_launches_ += launch_step(stream_, false);
                 CK(cudaStreamEndCapture(stream_, &g));
                 bins_dirty_ = true;   // captured kernels have not run: the next eager step regroups
+                tc.mark("drive: graph capture");
                 CK(cudaGraphInstantiate(&graph_, g, 0));
                 cudaGraphDestroy(g);
                 graph_len_ = graph_steps_;
+                tc.mark("drive: graph instantiate");
             }
             if (exact_steps_ >= 0) {
                 // a known step count: whole graphs, then single steps for the remainder, no polling
@@ -1190,22 +1317,47 @@ public:
     }
 
     int prepare(const int64_t* ids, int n, std::vector<SimRec*>* rs, std::string* err) {
-        std::vector<SimRec*> begun;
+        std::vector<SimRec*> fresh, begun;
+        std::unordered_set<SimRec*> seen;
         for (int i = 0; i < n; i++) {
             SimRec* r = find(ids[i]);
             if (!r) { *err = "unknown simulation id"; return -6; }
-            if (!r->resident) {
-                if (int e = upload_begin(r, err)) { upload_finish(begun, err); return e; }
-                begun.push_back(r);
-            }
+            if (!r->resident && seen.insert(r).second) fresh.push_back(r);
             rs->push_back(r);
         }
-        return upload_finish(begun, err);
+        TraceClock tc;
+        int e_many = upload_many(fresh, &begun, err);
+        tc.mark("prepare: upload_many");
+        if (int e = e_many) {
+            std::string e2;
+            upload_finish(begun, &e2);
+            return e;
+        }
+        const int ef = upload_finish(begun, err);
+        tc.mark("prepare: upload_finish");
+        return ef;
     }
+
+    // GVX_TRACE=1: host time of the phases of each call on stderr
+    static bool trace_on() {
+        static const bool on = [] { const char* v = std::getenv("GVX_TRACE"); return v && *v && *v != '0'; }();
+        return on;
+    }
+    struct TraceClock {
+        double t = now_s();
+        void mark(const char* what) {
+            if (!trace_on()) return;
+            const double u = now_s();
+            std::fprintf(stderr, "[gvx] %-28s %8.3f ms\n", what, 1e3 * (u - t));
+            t = u;
+        }
+    };
 
     int step(const int64_t* ids, int n, int mode, int64_t steps, std::string* err) override {
         std::vector<SimRec*> rs;
+        TraceClock tc;
         if (int e = prepare(ids, n, &rs, err)) return e;
+        tc.mark("step: prepare (uploads)");
         std::vector<int> slots;
         std::vector<int64_t> targets;
         std::vector<SimRec*> act;
@@ -1225,12 +1377,15 @@ public:
         // the stop formula is not applied by step() (no_stop), and reaching the target leaves the
         // simulation IDLE for the next call
         if (int e = set_running(slots, targets, err, 1)) return e;
+        tc.mark("step: read/set control");
         exact_steps_ = steps;
         int e = drive(act, mode, err);
+        tc.mark("step: drive");
         exact_steps_ = -1;
         if (int e2 = end_fixed_steps(slots, err)) return e2;
         if (int e2 = read_ctls(lo, hi, &cs, err)) return e2;
         for (auto* r : act) r->status = cs[(size_t)(r->slot - lo)].status;
+        tc.mark("step: end");
         return e;
     }
 
