@@ -31,7 +31,7 @@ ERRORS = {-1: "VX3_E_PARSE", -2: "VX3_E_OOM_BUDGET", -3: "VX3_E_DIVERGED", -4: "
 
 # Every symbol include/gpuvoxels_gb300.h declares.
 EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_set_external", "vx3_run", "vx3_step",
-           "vx3_submit", "vx3_poll", "vx3_pending", "vx3_get_result", "vx3_sim_info_get", "vx3_get_state",
+           "vx3_submit", "vx3_poll", "vx3_pending", "vx3_get_result", "vx3_sim_info_get", "vx3_sim_sizes", "vx3_get_state",
            "vx3_get_voxel_state", "vx3_get_link_state", "vx3_write_report", "vx3_free_sim", "vx3_last_timing",
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
@@ -82,6 +82,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_run": (I, [P, P, I, I, I64]), "vx3_step": (I, [P, P, I, I, I64]),
         "vx3_submit": (I, [P, I64, I64]), "vx3_poll": (I, [P, P, I, I]), "vx3_pending": (I, [P]),
         "vx3_get_result": (I, [P, I64, ctypes.POINTER(Result)]), "vx3_sim_info_get": (I, [P, I64, ctypes.POINTER(SimInfo)]),
+        "vx3_sim_sizes": (I, [P, P, I, P, P]),
         "vx3_get_state": (I, [P, I64, P, P, P]), "vx3_get_voxel_state": (I, [P, I64, P, P, P]),
         "vx3_get_link_state": (I, [P, I64, P, P, P]), "vx3_write_report": (I, [P, P, I, S, S]),
         "vx3_free_sim": (I, [P, I64]), "vx3_last_timing": (I, [P, P]), "vx3_set_tuning": (I, [P, I, I, I, I, I]),
@@ -252,6 +253,13 @@ class Context:
         self._check(self.L.vx3_get_result(self.h, sim, ctypes.byref(r)))
         return r
 
+    def sizes(self, ids):
+        """(voxel counts, link counts) of many simulations, without reading the device."""
+        a = self._ids(ids)
+        nv = np.zeros(len(a), np.int32); nl = np.zeros(len(a), np.int32)
+        self._check(self.L.vx3_sim_sizes(self.h, _p(a), len(a), _p(nv), _p(nl)))
+        return nv, nl
+
     def info(self, sim: int) -> SimInfo:
         r = SimInfo()
         self._check(self.L.vx3_sim_info_get(self.h, sim, ctypes.byref(r)))
@@ -300,7 +308,7 @@ class Context:
         """Poses of many simulations in one device pass: (pos, orient, flags, offsets) with the
         simulations' voxels one after another; simulation k owns rows offsets[k]:offsets[k+1]."""
         a = self._ids(ids)
-        counts = [self.info(int(i)).num_voxel for i in a]
+        counts = self.sizes(a)[0]
         offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
         tot = int(offsets[-1])
         pos = np.zeros((tot, 3)); q = np.zeros((tot, 4)); fl = np.zeros(tot, np.uint8)

@@ -321,6 +321,17 @@ int vx3_get_result(vx3_ctx* c, vx3_sim_id id, vx3_result* out) {
     return VX3_OK;
 }
 
+int vx3_sim_sizes(vx3_ctx* c, const vx3_sim_id* ids, int n, int32_t* num_voxel, int32_t* num_link) {
+    if (!c || (!ids && n > 0) || n < 0) return VX3_E_ARG;
+    for (int k = 0; k < n; k++) {
+        const gvx::SimWorld* w = c->eng->world(ids[k]);
+        if (!w) return fail(c, VX3_E_ARG, "unknown simulation id");
+        if (num_voxel) num_voxel[k] = w->nv;
+        if (num_link) num_link[k] = w->nl;
+    }
+    return VX3_OK;
+}
+
 int vx3_sim_info_get(vx3_ctx* c, vx3_sim_id id, vx3_sim_info* out) {
     if (!c || !out) return VX3_E_ARG;
     int nv, nl, st;

@@ -1730,8 +1730,44 @@ public:
         for (int k0 = 0; k0 < n; k0 += 65535)
             ks_.gather(stream_, d_sims_, dslot + k0, doff + k0, std::min(65535, n - k0), dpos, dq, dfl);
         CK(cudaGetLastError());
-        // straight into the caller's buffers: no staging copy on the host, and no pinned
-        // buffer to grow to the size of a whole generation
+        const size_t b_all = b_pos + b_q + b_fl;
+        if (gen_.p && gen_.cap >= b_all) {
+            // the generation upload buffer is large enough: one copy into pinned memory, then
+            // host threads copy into the caller's arrays (and take their first-touch faults)
+            if (int e = pinned(&gen_, b_all, err)) return e;   // waits for the buffer's last use
+            char* hs = gen_.p;
+            if (pos3 && q4 && flags) {
+                CK(copy_async(hs, dpos, b_all, cudaMemcpyDeviceToHost, stream_));
+            } else {
+                if (pos3) CK(copy_async(hs, dpos, b_pos, cudaMemcpyDeviceToHost, stream_));
+                if (q4) CK(copy_async(hs + b_pos, dq, b_q, cudaMemcpyDeviceToHost, stream_));
+                if (flags) CK(copy_async(hs + b_pos + b_q, dfl, b_fl, cudaMemcpyDeviceToHost, stream_));
+            }
+            CK(cudaEventRecord(gen_.done, stream_));
+            CK(cudaEventSynchronize(gen_.done));
+            struct Piece { char* dst; const char* src; size_t n; };
+            std::vector<Piece> pieces;
+            auto cut = [&](void* dst, const char* src, size_t n) {
+                if (!dst) return;
+                for (size_t o = 0; o < n; o += kReadPiece)
+                    pieces.push_back(Piece{(char*)dst + o, src + o, std::min(kReadPiece, n - o)});
+            };
+            cut(pos3, hs, b_pos);
+            cut(q4, hs + b_pos, b_q);
+            cut(flags, hs + b_pos + b_q, b_fl);
+            std::atomic<size_t> next{0};
+            auto work = [&]() {
+                for (size_t i = next++; i < pieces.size(); i = next++) memcpy(pieces[i].dst, pieces[i].src, pieces[i].n);
+            };
+            const int nt = (int)std::max<size_t>(1, std::min<size_t>(pieces.size(), std::max(1u, std::thread::hardware_concurrency())));
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nt; t++) pool.emplace_back(work);
+            work();
+            for (auto& t : pool) t.join();
+            return 0;
+        }
+        // straight into the caller's buffers: no pinned buffer grown to the size of a whole
+        // generation just for this
         if (pos3) CK(copy_async(pos3, dpos, b_pos, cudaMemcpyDeviceToHost, stream_));
         if (q4) CK(copy_async(q4, dq, b_q, cudaMemcpyDeviceToHost, stream_));
         if (flags) CK(copy_async(flags, dfl, b_fl, cudaMemcpyDeviceToHost, stream_));
@@ -1739,6 +1775,7 @@ public:
         CK(cudaEventSynchronize(rb_.done));
         return 0;
     }
+    static constexpr size_t kReadPiece = 1u << 20;   // bytes per host copy task of a staged read-back
 
     const SimWorld* world(int64_t id) override {
         SimRec* r = find(id);

@@ -117,6 +117,10 @@ int vx3_pending(vx3_ctx* ctx);
 /* Replaces VX3_SimulationManager::collectResults for one simulation (VX3_SimulationManager.cu:416-458). */
 int vx3_get_result(vx3_ctx* ctx, vx3_sim_id id, vx3_result* out);
 int vx3_sim_info_get(vx3_ctx* ctx, vx3_sim_id id, vx3_sim_info* out);
+/* Voxel and link counts of many simulations, from the host-side description only (no
+ * device read): what VX3_VoxelyzeKernel keeps as num_d_voxels / num_d_links
+ * (Voxelyze3/src/VX3/VX3_VoxelyzeKernel.cuh:72,79).  Either output may be NULL. */
+int vx3_sim_sizes(vx3_ctx* ctx, const vx3_sim_id* ids, int n, int32_t* num_voxel, int32_t* num_link);
 
 /* Voxel state in the reference's CVX_Voxel member layout (Voxelyze3/src/old/VX_Voxel.h:166-182):
  * pos[3*nv], orient[4*nv] (w,x,y,z) and flags[nv]; any pointer may be NULL. */

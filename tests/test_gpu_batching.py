@@ -53,6 +53,9 @@ def test_get_states_equals_per_simulation_readback(ctx):
             assert np.array_equal(_bits(pos[off[k]:off[k + 1]]), _bits(p1))
             assert np.array_equal(_bits(q[off[k]:off[k + 1]]), _bits(q1))
             assert np.array_equal(fl[off[k]:off[k + 1]], f1)
+        nv, nl = ctx.sizes(order)                  # host-side counts, no device read
+        assert list(nv) == [ctx.info(i).num_voxel for i in order]
+        assert list(nl) == [ctx.info(i).num_link for i in order]
     finally:
         for s in ids:
             ctx.free(s)
