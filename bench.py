@@ -1,17 +1,31 @@
 #!/usr/bin/env python
 """Voxel-steps/s of the Voxelyze3 soft-body step on GB300.
 
-Default workload (N=1): the batched plain-physics configuration — 512
-independent seeded creatures (cubic lattice side U{6..20}, fill U(0.3, 0.9),
-largest 6-connected component, four materials with E log-uniform in
-[1e5, 1e7] Pa, rho=1000, nu=0.35, one or two actuated at 5 Hz), gravity and
-floor on, no self-collision, FP64, all creatures packed into shared launches.
-A "step" is one physics step of the whole batch.  The batch's device state
-(~1 GB) is larger than L2, so no flush is needed between timed iterations.
+Default run (N=1) prints one JSON line whose value is the batched
+plain-physics configuration — 512 independent seeded creatures (cubic
+lattice side U{6..20}, fill U(0.3, 0.9), largest 6-connected component, four
+materials with E log-uniform in [1e5, 1e7] Pa, rho=1000, nu=0.35, one or two
+actuated at 5 Hz), gravity and floor on, no self-collision, FP64, all creatures
+packed into shared launches.  A "step" is one physics step of the whole batch.
+The batch's device state (~1 GB) is larger than L2, so no flush is needed
+between timed iterations.  The launch shape is picked by the autotuner
+(vx3_autotune) first and recorded in config.tuning.
 
-Other workloads (--workload): slab (a solid 200x200x100 body, 4M voxels),
-collide (40^3 creatures at fill 0.5 with self-collision), serve (Poisson
-request stream through the serving loop), plain (one 10^3 creature).
+The same line carries, under "modes":
+  plain_vs_batched  the one-simulation-per-launch form against the batched form on
+                    the same sample of creatures;
+  serve             the serving stream: Poisson arrivals at 50, 200 and 2,000 req/s
+                    of creatures with V log-uniform in [100, 1e5] and horizons
+                    U[1e3, 5e4] steps, 20% with self-collision, through the
+                    continuous-batching loop (vx3_submit / vx3_poll), against the
+                    plain per-simulation path on the same requests;
+  collide           64 creatures of 40^3 at fill 0.5 with self-collision, all in one
+                    batch, for a bounded share of their 20,000 steps;
+  slab              the single 200x200x100 body (4M voxels) for its 2,000 steps
+                    (or a bounded share), with its HBM and FP64 rooflines.
+
+Other workloads (--workload): slab, collide, plain (one 10^3 creature) as the
+line's value, serve (the serving block alone, more requests).
 
 --impl reference times the reference's CPU implementation of the step on this
 machine's host cores: the reference compiled from its own sources
@@ -48,13 +62,17 @@ def measured_peaks():
 
 
 # FP64-pipe thread instructions (DADD/DMUL/DFMA, compares, conversions; predicated-on lanes)
-# per link and per voxel of one step of the batch workload, read by ncu at step 205
-# (sm__thread_inst_executed_pipe_fp64_pred_on.sum ÷ links or voxels; profiles/k_links_k_voxels_batch512_steady.md).
-FP64_INSTR_PER_LINK = 684878336 / 1627115      # 420.9
-FP64_INSTR_PER_VOXEL = 236663360 / 844972      # 280.1
-# DRAM bytes per link of one k_links launch at the same step (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum = 410.2 MB + 358.0 MB for 1,627,115 links).
-LINK_TRAFFIC_PER_LINK = (410284544 + 358874112) / 1627115
+# per link (k_links) and per voxel (k_voxels) of one step, read by ncu per workload
+# (sm__thread_inst_executed_pipe_fp64_pred_on.sum / links or voxels), and DRAM bytes per
+# link of one k_links launch (dram__bytes_read.sum + dram__bytes_write.sum / links).
+# Sources: profiles/k_links_k_voxels_batch512_steady.md (batch, step 205).
+FP64_COUNTS = {
+    "batch": dict(per_link=684878336 / 1627115, per_voxel=236663360 / 844972,
+                  traffic_per_link=(410284544 + 358874112) / 1627115, source="ncu, 512-creature batch, step 205"),
+}
+FP64_INSTR_PER_LINK = FP64_COUNTS["batch"]["per_link"]
+FP64_INSTR_PER_VOXEL = FP64_COUNTS["batch"]["per_voxel"]
+LINK_TRAFFIC_PER_LINK = FP64_COUNTS["batch"]["traffic_per_link"]
 
 
 def fp64_peak_fma_per_s(device=0):
@@ -135,7 +153,7 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------- workloads
-def make_workload(name, rank=0, n_batch=512):
+def make_workload(name, rank=0, n_batch=512, n_collide=64):
     from gpuvoxels_gb300 import synth
     if name == "batch":
         cs = synth.config1_batch(n_batch, seed=1 + 1000 * rank, sim_time=0.5)
@@ -145,9 +163,9 @@ def make_workload(name, rank=0, n_batch=512):
         cs = [synth.slab(200, 200, 100, seed=3 + rank)]
         desc = dict(workload="single large body: solid 200x200x100 slab (4M voxels), E=1e6, nu=0.35, per-voxel CTE actuation")
     elif name == "collide":
-        cs = synth.config2_batch(16, seed=2 + rank)
-        desc = dict(workload="collision-heavy: 16 creatures 40^3 fill 0.5, 3 materials incl. E=1e5, self-collision on "
-                    "(64 in the full configuration)")
+        cs = synth.config2_batch(n_collide, seed=2 + rank)
+        desc = dict(workload="collision-heavy: %d creatures 40^3 fill 0.5, 3 materials incl. E=1e5, self-collision on "
+                    "(radius 0.75), contraction-only actuation at 5 Hz" % len(cs))
     elif name == "plain":
         cs = [synth.config0_creature(0)]
         desc = dict(workload="plain single creature: 10^3 lattice, fill 0.6, passive+active, 5 Hz +-39 C")
@@ -228,6 +246,196 @@ def reduce_timing(dist, dev_s, vsteps):
     return float(mx[0]), int(sm[1])
 
 
+def kernel_times(ctx, ids, reps=5):
+    """Median per-kernel device times over `reps` profiled steps (one launch per kernel, CUDA
+    events on the context's stream): (k_links ms, contacts ms, k_voxels ms)."""
+    import gpuvoxels_gb300 as g
+    ctx.set_profiling(True)
+    lk, ck, vk = [], [], []
+    for _ in range(reps):
+        ctx.step(ids, 1, g.BATCHED)
+        t = ctx.timing()
+        lk.append(t["link_ms"]); ck.append(t["contact_ms"]); vk.append(t["voxel_ms"])
+    ctx.set_profiling(False)
+    return statistics.median(lk), statistics.median(ck), statistics.median(vk)
+
+
+def rooflines(ctx, ids, workload, link_ms, con_ms, vox_ms, peak64):
+    """HBM roofline of the dominant step kernel (algorithmic bytes over its event-timed duration
+    against the measured copy bandwidth) and, beside it, the FP64-pipe roofline that binds."""
+    link_b, vox_b = algorithmic_bytes(ctx, ids)
+    dom = "k_links" if link_ms >= vox_ms else "k_voxels"
+    dom_ms, dom_b = (link_ms, link_b) if dom == "k_links" else (vox_ms, vox_b)
+    peak, peak_kind = measured_peaks()
+    achieved = dom_b / (dom_ms / 1e3) / 1e9
+    n_links = sum(ctx.info(i).num_link for i in ids)
+    n_vox = sum(ctx.info(i).num_voxel for i in ids)
+    counts = FP64_COUNTS.get(workload)
+    if counts is None or peak64 is None:
+        fp64 = {"unavailable": "no ncu count of FP64 instructions for this workload" if counts is None else "no DGEMM peak"}
+    else:
+        ach_l = counts["per_link"] * n_links / (link_ms / 1e3)
+        ach_v = counts["per_voxel"] * n_vox / (vox_ms / 1e3)
+        fp64 = {"bound": "fp64", "kernel": "k_links", "achieved": ach_l / 1e9, "peak": peak64 / 1e9,
+                "unit": "G FP64 thread-instructions/s", "frac": ach_l / peak64,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FMA/s)",
+                "instr_per_link": counts["per_link"], "k_voxels_achieved": ach_v / 1e9, "k_voxels_frac": ach_v / peak64,
+                "instr_per_voxel": counts["per_voxel"], "counts_source": counts["source"]}
+    traffic = counts["traffic_per_link"] * n_links if (counts and dom == "k_links" and counts.get("traffic_per_link")) else None
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "algorithmic_bytes_per_launch": dom_b, "kernel_ms": dom_ms, "link_kernel_ms": link_ms, "voxel_kernel_ms": vox_ms,
+            "contact_kernel_ms": con_ms, "traffic": traffic,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per k_links launch, per link "
+                               f"({counts['source']}), times this run's links") if traffic else None,
+            "fp64": fp64,
+            "note": "the step kernels are bound by GB300's FP64 pipe, not by HBM: see roofline.fp64"}, n_links, n_vox
+
+
+def measure_resident(ctx, ids, steps, warmup, dist=None, sample_clocks=True, device=0):
+    """K batched steps of device-resident simulations, after W warm-up steps, timed with CUDA
+    events on the context's stream; returns (device seconds, voxel-steps, launches, clocks, wall)."""
+    import gpuvoxels_gb300 as g
+    ctx.step(ids, warmup, g.BATCHED)
+    if dist:
+        dist.barrier()
+    with ClockSampler(device) as clk:
+        t0 = time.perf_counter()
+        ctx.step(ids, steps, g.BATCHED)
+        wall = time.perf_counter() - t0
+    tm = ctx.timing()
+    return tm["device_ms"] / 1e3, tm["voxel_steps"], tm["launches"], clk.summary(), wall
+
+
+def workload_block(args, name, steps, full_steps, device, budget, peak64):
+    """One more configuration measured in the same run: its own context, the autotuner's shape,
+    W warm-up steps, then `steps` batched steps (a stated share of the configuration's
+    `full_steps` when smaller), with its HBM and FP64 rooflines."""
+    import gpuvoxels_gb300 as g
+    t0 = time.perf_counter()
+    cs, desc = make_workload(name, 0, args.batch)
+    gen_s = time.perf_counter() - t0
+    with g.Context(device, budget) as ctx:
+        t0 = time.perf_counter()
+        ids = ctx.load_many([c.vxa for c in cs], names=[f"{name}{i}" for i in range(len(cs))])
+        ctx.step(ids, 1, g.BATCHED)
+        load_s = time.perf_counter() - t0
+        if not args.no_autotune:
+            ctx.autotune(ids)
+        dev_s, vsteps, launches, clocks, wall = measure_resident(ctx, ids, steps, args.warmup, device=device)
+        link_ms, con_ms, vox_ms = kernel_times(ctx, ids)
+        roof, n_links, n_vox = rooflines(ctx, ids, name, link_ms, con_ms, vox_ms, peak64)
+        status = {}
+        for i in ids:
+            st = ctx.info(i).status
+            status[st] = status.get(st, 0) + 1
+        out = dict(workload=desc["workload"], simulations=len(cs), voxels=n_vox, links=n_links, value=vsteps / dev_s,
+                   unit="voxel-steps/s", steps=steps, of_steps=full_steps,
+                   share_note=(None if steps >= full_steps else
+                               f"{steps} of the configuration's {full_steps} steps, timed as a bounded share of the run "
+                               "(the per-step cost of a running simulation is steady)"),
+                   ms_per_step=dev_s * 1e3 / steps, gpu_launches=launches, tuning=ctx.tuning(), roofline=roof,
+                   clocks=clocks, status_counts={str(k): v for k, v in status.items()},
+                   host_s=dict(generate=round(gen_s, 2), load_upload_first_step=round(load_s, 2)))
+    return out
+
+
+def serve_stream(args, device, budget, n_requests, rates):
+    """The serving stream (seeded Poisson arrivals per offered rate) through the continuous-
+    batching loop, and the plain per-simulation path on the same requests.
+
+    Served: each request is parsed and loaded on arrival (vx3_load_vxa), queued with its horizon
+    (vx3_submit) and advanced by vx3_poll, which admits queued requests as the context's HBM
+    budget allows, advances every admitted one by --chunk-steps steps in one captured batch and
+    retires finished ones.  Latency = completion (the poll that returned it) - arrival.
+    Plain: one request at a time, in arrival order, each alone in PLAIN mode (one simulation
+    per launch); every request is loaded and run for a bounded sample of its steps, and its
+    service time is the measured load plus the measured per-step time times its horizon; the
+    queue of the stream is then replayed first-come-first-served with those service times."""
+    import itertools
+    import gpuvoxels_gb300 as g
+    from gpuvoxels_gb300 import synth
+    t0 = time.perf_counter()
+    reqs = synth.serving_requests(n_requests, seed=4)
+    gen_s = time.perf_counter() - t0
+    work = [c.num_voxel * h for c, h in reqs]
+    # ---- plain arm: measured per-request service times
+    service = []
+    with g.Context(device, budget) as ctx:
+        w = ctx.load_vxa(reqs[0][0].vxa, name="warm")
+        ctx.step(w, 1, g.PLAIN)
+        ctx.step(w, 32, g.PLAIN)
+        ctx.free(w)
+        for k, (c, h) in enumerate(reqs):
+            a = time.perf_counter()
+            sid = ctx.load_vxa(c.vxa, name=f"p{k}")
+            ctx.step(sid, 1, g.PLAIN)
+            b = time.perf_counter()
+            n_s = max(1, min(h - 1, args.plain_sample_steps))
+            ctx.step(sid, n_s, g.PLAIN)
+            e = time.perf_counter()
+            service.append((b - a) + (e - b) * (h - 1) / n_s)
+            ctx.free(sid)
+    pct = lambda xs, p: sorted(xs)[min(len(xs) - 1, int(round(p / 100.0 * (len(xs) - 1))))]
+    out = []
+    for ri, rate in enumerate(rates):
+        rng = np.random.default_rng(5 + ri)
+        arrivals = list(itertools.accumulate(rng.exponential(1.0 / rate, size=len(reqs))))
+        # ---- served arm
+        with g.Context(device, budget) as ctx:
+            w = ctx.load_vxa(reqs[0][0].vxa, name="warm")
+            ctx.submit(w, 256)
+            while ctx.pending():
+                for r in ctx.poll(args.chunk_steps):
+                    ctx.free(r.id)
+            lat, vsteps, k, arrival_of = [], 0, 0, {}
+            t0 = time.perf_counter()
+            last = t0
+            while k < len(reqs) or ctx.pending():
+                now = time.perf_counter() - t0
+                while k < len(reqs) and arrivals[k] <= now:
+                    c, horizon = reqs[k]
+                    sid = ctx.load_vxa(c.vxa, name=f"r{k}")
+                    ctx.submit(sid, horizon)
+                    arrival_of[sid] = arrivals[k]
+                    k += 1
+                if ctx.pending():
+                    done = ctx.poll(args.chunk_steps)
+                    tnow = time.perf_counter() - t0
+                    for r in done:
+                        lat.append(tnow - arrival_of[r.id])
+                        vsteps += r.num_voxel * r.steps
+                        ctx.free(r.id)
+                        last = time.perf_counter()
+                elif k < len(reqs):
+                    time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t0))))
+            span = (last - t0) - arrivals[0]
+        # ---- plain arm: the same arrivals, first come first served
+        free_at, plat = 0.0, []
+        for a, sv in zip(arrivals, service):
+            start = max(a, free_at)
+            free_at = start + sv
+            plat.append(free_at - a)
+        pspan = free_at - arrivals[0]
+        served = vsteps / span
+        plain = sum(work) / pspan
+        out.append(dict(offered_req_per_s=rate, completed=len(lat), p50_latency_s=pct(lat, 50), p99_latency_s=pct(lat, 99),
+                        served_voxel_steps_per_s=served, makespan_s=span,
+                        plain_p50_latency_s=pct(plat, 50), plain_p99_latency_s=pct(plat, 99),
+                        plain_voxel_steps_per_s=plain, plain_makespan_s=pspan, served_vs_plain=served / plain))
+    vs = [c.num_voxel for c, _ in reqs]
+    return dict(
+        requests=len(reqs), voxels_min=min(vs), voxels_max=max(vs), voxel_steps_total=int(sum(work)),
+        collide=int(sum(1 for c, _ in reqs if c.meta.get("collide"))), chunk_steps=args.chunk_steps,
+        stream=("Poisson arrivals at each offered rate (seeded); creatures with V log-uniform in [100, 1e5] (fill "
+                "U(0.5, 0.9), 4 materials E log-uniform [1e5, 1e7] Pa), horizons U[1e3, 5e4] steps, 20% with "
+                "self-collision; the same requests at every rate"),
+        plain_arm=(f"each request alone in PLAIN mode (one simulation per launch): load + first step measured, then "
+                   f"min(horizon, {args.plain_sample_steps}) steps measured and scaled to its horizon; the stream's "
+                   "queue replayed first come first served with those service times"),
+        plain_service_s_total=sum(service), generate_s=round(gen_s, 2), target_served_vs_plain=10.0, rates=out)
+
+
 def run_ours(args):
     rank, ws, dist = dist_init()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -240,59 +448,26 @@ def run_ours(args):
     ctx.set_precision(prec)
     ids = [ctx.load_vxa(c.vxa, name=f"c{i}") for i, c in enumerate(cs)]
     ctx.step(ids, 1, g.BATCHED)                       # upload + first step
-    if args.autotune:
-        ctx.autotune(ids)
     if args.tuning:
         bl, bv, il, iv = (int(x) for x in args.tuning.split(","))
         ctx.set_tuning(bl, bv, il, iv, args.graph_steps)
     else:
         ctx.set_tuning(graph_steps=args.graph_steps)
-    ctx.step(ids, args.warmup, g.BATCHED)
-    if dist:
-        dist.barrier()
-    with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        ctx.step(ids, args.steps, g.BATCHED)
-        wall = time.perf_counter() - t0
-    tm = ctx.timing()
-    dev_s = tm["device_ms"] / 1e3
-    vsteps = tm["voxel_steps"]
-    launches = tm["launches"]
+        if not args.no_autotune:
+            ctx.autotune(ids)                         # launch shape picked on the live batch
+    tuning = ctx.tuning()
+    dev_s, vsteps, launches, clocks, wall = measure_resident(ctx, ids, args.steps, args.warmup, dist, device=local)
     dev_s, vsteps = reduce_timing(dist, dev_s, vsteps)
     value = vsteps / dev_s
-    # ---- per-kernel times (profiled steps: one launch per kernel, events on the context stream)
-    ctx.set_profiling(True)
-    lk, ck, vk = [], [], []
-    for _ in range(5):
-        ctx.step(ids, 1, g.BATCHED)
-        t = ctx.timing()
-        lk.append(t["link_ms"]); ck.append(t["contact_ms"]); vk.append(t["voxel_ms"])
-    ctx.set_profiling(False)
-    link_ms, vox_ms, con_ms = statistics.median(lk), statistics.median(vk), statistics.median(ck)
-    link_b, vox_b = algorithmic_bytes(ctx, ids)
-    dom = "k_links" if link_ms >= vox_ms else "k_voxels"
-    dom_ms, dom_b = (link_ms, link_b) if dom == "k_links" else (vox_ms, vox_b)
-    peak, peak_kind = measured_peaks()
-    achieved = dom_b / (dom_ms / 1e3) / 1e9
-    n_links = sum(ctx.info(i).num_link for i in ids)
-    n_vox = sum(ctx.info(i).num_voxel for i in ids)
-    # ---- the FP64 roofline that actually bounds both step kernels
-    fp64 = None
-    if args.workload == "batch" and args.precision != "exact":
-        fp64 = {"unavailable": "FP64 instructions per link were counted (ncu) for the exact build, the one measured by default"}
-    elif args.workload == "batch":
+    link_ms, con_ms, vox_ms = kernel_times(ctx, ids)
+    peak64 = None
+    if args.precision == "exact":
         try:
             peak64 = fp64_peak_fma_per_s(local)
-            ach_l = FP64_INSTR_PER_LINK * n_links / (link_ms / 1e3)
-            ach_v = FP64_INSTR_PER_VOXEL * n_vox / (vox_ms / 1e3)
-            fp64 = {"bound": "fp64", "kernel": "k_links", "achieved": ach_l / 1e9, "peak": peak64 / 1e9,
-                    "unit": "G FP64 thread-instructions/s", "frac": ach_l / peak64,
-                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FMA/s)",
-                    "instr_per_link": FP64_INSTR_PER_LINK, "k_voxels_achieved": ach_v / 1e9, "k_voxels_frac": ach_v / peak64,
-                    "instr_per_voxel": FP64_INSTR_PER_VOXEL}
-        except Exception as e:   # the FP64 roofline is reported beside the HBM one; its absence is not fatal
-            fp64 = {"unavailable": str(e)[:200]}
-    # ---- plain one-simulation-per-launch form of the same kernels, on a sample of the batch
+        except Exception:   # the FP64 roofline is reported beside the HBM one; its absence is not fatal
+            peak64 = None
+    roof, n_links, n_vox = rooflines(ctx, ids, args.workload, link_ms, con_ms, vox_ms, peak64)
+    # ---- plain one-simulation-per-launch form against the batched form, on the same sample
     plain = None
     if args.workload == "batch" and rank == 0:
         sub = ids[:args.plain_sims]
@@ -300,9 +475,10 @@ def run_ours(args):
         tp = ctx.timing()
         ctx.step(sub, 32, g.BATCHED)
         tb = ctx.timing()
-        plain = dict(sample=f"first {len(sub)} creatures x 32 steps", plain_value=tp["voxel_steps"] / (tp["device_ms"] / 1e3),
-                     batched_value_same_sample=tb["voxel_steps"] / (tb["device_ms"] / 1e3),
-                     full_batch_vs_plain=value / (tp["voxel_steps"] / (tp["device_ms"] / 1e3)))
+        pv = tp["voxel_steps"] / (tp["device_ms"] / 1e3)
+        bv = tb["voxel_steps"] / (tb["device_ms"] / 1e3)
+        plain = dict(sample=f"first {len(sub)} creatures x 32 steps, both forms", plain_value=pv, batched_value=bv,
+                     batched_vs_plain=bv / pv)
     ctx.close()
     # ---- end to end through the C ABI with host buffers: parse+load, upload, K steps, read back
     e2e = None
@@ -311,6 +487,9 @@ def run_ours(args):
         for _ in range(args.e2e_reps):           # each a fresh context: parse, upload, steps, read-back
             c2 = g.Context(local, budget)
             c2.set_precision(prec)
+            c2.set_tuning(tuning["block_links"], tuning["block_voxels"], tuning["items_links"], tuning["items_voxels"],
+                          tuning["graph_steps"])
+            c2.set_claim_sizes(tuning["claim_links"], tuning["claim_voxels"])
             h0, d0 = c2.transfer_bytes()
             t0 = time.perf_counter()
             ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
@@ -335,96 +514,55 @@ def run_ours(args):
     if not args.no_cpu:
         v, cores, kind, sample = cpu_sample(cs, args.cpu_seconds)
         cpu = dict(value=v, unit="voxel-steps/s", cores=cores, kind=kind, sample=sample)
+    modes = {}
+    if plain:
+        modes["plain_vs_batched"] = plain
+    if args.workload == "batch" and ws == 1 and not args.no_modes:
+        rates = [float(x) for x in args.serve_rates.split(",")]
+        modes["serve"] = serve_stream(args, local, budget, args.serve_requests, rates)
+        modes["collide"] = workload_block(args, "collide", args.collide_steps, 20000, local, budget, peak64)
+        modes["slab"] = workload_block(args, "slab", args.slab_steps, 2000, local, budget, peak64)
     line = {
         "metric": "voxel-steps/sec (batched step of all simulations)",
         "value": value, "unit": "voxel-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded creatures, no dataset)",
         "config": dict(desc, simulations=len(cs) * ws, voxels=n_vox * ws, links=n_links * ws, mode="batched",
-                       kernel_build=args.precision,
+                       kernel_build=args.precision, tuning=tuning,
+                       tuning_source="vx3_autotune on the live batch" if not (args.tuning or args.no_autotune) else "set",
                        l2="device state larger than L2; no flush needed", parallelism=f"replicas x{ws} (no collective)"),
         "e2e": e2e,
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                     "algorithmic_bytes_per_launch": dom_b, "kernel_ms": dom_ms,
-                     "link_kernel_ms": link_ms, "voxel_kernel_ms": vox_ms, "contact_kernel_ms": con_ms,
-                     "traffic": LINK_TRAFFIC_PER_LINK * n_links if dom == "k_links" else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per k_links launch at step 205, "
-                                       "per link, times this run's links",
-                     "fp64": fp64,
-                     "note": "the step kernels are bound by GB300's FP64 pipe, not by HBM: see roofline.fp64"},
+        "roofline": roof,
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "wall_s_timed": wall,
     }
-    if plain:
-        line["modes"] = plain
+    if modes:
+        line["modes"] = modes
     print(json.dumps(line))
 
 
 def run_serve(args):
-    """Serving: requests arrive as a Poisson stream; each is parsed and loaded on arrival
-    (vx3_load_vxa), queued (vx3_submit) and advanced by vx3_poll in chunks of --chunk-steps
-    alongside every other admitted request, within the context's HBM budget.  Per offered
-    rate: completion latency p50/p99 (submit to finish) and served voxel-steps/s."""
-    import itertools
-    import numpy as np
-    import gpuvoxels_gb300 as g
-    from gpuvoxels_gb300 import synth
-    reqs = synth.serving_requests(args.serve_requests, seed=4)
-    ctx = g.Context(0, int(args.budget_gb * (1 << 30)))
-    ctx.set_precision(g.FMA if args.precision == "fma" else g.EXACT)
-    # warm the kernels and graphs with one small request
-    w = ctx.load_vxa(reqs[0][0].vxa, name="warm")
-    ctx.submit(w, 256)
-    while ctx.pending():
-        for r in ctx.poll(args.chunk_steps):
-            ctx.free(r.id)
+    """The serving block alone (see serve_stream), as its own JSON line."""
     rates = [float(x) for x in args.serve_rates.split(",")]
-    rng = np.random.default_rng(5)
-    out = []
-    for rate in rates:
-        arrivals = list(itertools.accumulate(rng.exponential(1.0 / rate, size=len(reqs))))
-        lat, vsteps, k = [], 0, 0
-        t0 = time.perf_counter()
-        while k < len(reqs) or ctx.pending():
-            now = time.perf_counter() - t0
-            while k < len(reqs) and arrivals[k] <= now:
-                c, horizon = reqs[k]
-                sid = ctx.load_vxa(c.vxa, name=f"r{k}")
-                ctx.submit(sid, horizon)
-                k += 1
-            if ctx.pending():
-                for r in ctx.poll(args.chunk_steps):
-                    lat.append(r.finish_time_s - r.submit_time_s)
-                    vsteps += r.num_voxel * r.steps
-                    ctx.free(r.id)
-            elif k < len(reqs):
-                time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t0))))
-        span = time.perf_counter() - t0
-        lat.sort()
-        pct = lambda p: lat[min(len(lat) - 1, int(round(p / 100.0 * (len(lat) - 1))))]
-        out.append(dict(offered_req_per_s=rate, completed=len(lat), p50_latency_s=pct(50), p99_latency_s=pct(99),
-                        served_voxel_steps_per_s=vsteps / span, makespan_s=span))
-    ctx.close()
-    line = {"metric": "served voxel-steps/s and completion latency (Poisson arrivals)", "unit": "voxel-steps/s",
-            "value": max(o["served_voxel_steps_per_s"] for o in out), "n_gpus": 1, "higher_is_better": True,
+    out = serve_stream(args, 0, int(args.budget_gb * (1 << 30)), args.serve_requests, rates)
+    best = max(out["rates"], key=lambda r: r["served_voxel_steps_per_s"])
+    line = {"metric": "served voxel-steps/s and completion latency (Poisson arrivals) vs the plain per-simulation path",
+            "unit": "voxel-steps/s", "value": best["served_voxel_steps_per_s"], "n_gpus": 1, "higher_is_better": True,
             "dtype": "f64", "data": "synthetic (seeded creatures, no dataset)",
-            "config": {"workload": f"serving: {len(reqs)} requests per rate, V log-uniform [100, 1e4], horizon U[1e3, 5e3] "
-                                   f"steps, 20% with self-collision, chunk {args.chunk_steps} steps per poll",
-                       "kernel_build": args.precision},
-            "rates": out}
+            "config": {"workload": f"serving stream: {out['requests']} requests per rate", "kernel_build": args.precision},
+            "serve": out}
     print(json.dumps(line))
 
 
 def profile_case(args):
     """A short, self-terminating run for ncu: the workload's kernels, one launch each per step."""
     import gpuvoxels_gb300 as g
-    cs, desc = make_workload(args.workload, 0, args.batch)
+    cs, desc = make_workload(args.workload, 0, args.batch, args.collide_sims)
     ctx = g.Context(0, int(args.budget_gb * (1 << 30)))
     ctx.set_precision(g.FMA if args.precision == "fma" else g.EXACT)
-    ids = [ctx.load_vxa(c.vxa, name=f"c{i}") for i, c in enumerate(cs)]
+    ids = ctx.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
     ctx.set_profiling(True)
     ctx.step(ids, args.profile_steps, g.BATCHED)
     t = ctx.timing()
@@ -467,14 +605,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch", choices=["batch", "slab", "collide", "plain", "serve"])
-    ap.add_argument("--serve-requests", type=int, default=64)
-    ap.add_argument("--serve-rates", default="5,10,20,40", help="offered request rates (req/s) for --workload serve")
+    ap.add_argument("--serve-requests", type=int, default=16, help="requests of the serving stream (per offered rate)")
+    ap.add_argument("--serve-rates", default="50,200,2000", help="offered request rates (req/s) of the serving stream")
     ap.add_argument("--chunk-steps", type=int, default=64)
+    ap.add_argument("--plain-sample-steps", type=int, default=256,
+                    help="steps of each request measured in PLAIN mode for the plain arm of the serving stream")
+    ap.add_argument("--collide-steps", type=int, default=2000, help="steps of the collision-heavy block (of 20,000)")
+    ap.add_argument("--collide-sims", type=int, default=64, help="creatures of the collision workload for --profile-steps")
+    ap.add_argument("--slab-steps", type=int, default=2000, help="steps of the single-body block (of 2,000)")
+    ap.add_argument("--no-modes", action="store_true", help="skip the serving, collision and single-body blocks")
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--graph-steps", type=int, default=64)
-    ap.add_argument("--tuning", default="", help="block_links,block_voxels,items_links,items_voxels (0 = keep)")
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--tuning", default="", help="block_links,block_voxels,items_links,items_voxels (0 = keep); skips the autotuner")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--plain-sims", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -36,7 +36,8 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_set_tuning", "vx3_autotune", "vx3_set_profiling", "vx3_set_precision", "vx3_sim_bytes", "vx3_bytes_in_use",
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
            "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states",
-           "vx3_get_extras", "vx3_get_links", "vx3_transfer_bytes"]
+           "vx3_get_extras", "vx3_get_links", "vx3_transfer_bytes", "vx3_set_claim_sizes", "vx3_get_tuning",
+           "vx3_set_contact_slots", "vx3_eval_formula"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -86,7 +87,8 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_get_state": (I, [P, I64, P, P, P]), "vx3_get_voxel_state": (I, [P, I64, P, P, P]),
         "vx3_get_link_state": (I, [P, I64, P, P, P]), "vx3_write_report": (I, [P, P, I, S, S]),
         "vx3_free_sim": (I, [P, I64]), "vx3_last_timing": (I, [P, P]), "vx3_set_tuning": (I, [P, I, I, I, I, I]),
-        "vx3_autotune": (I, [P, P, I]), "vx3_set_profiling": (I, [P, I]), "vx3_set_precision": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
+        "vx3_autotune": (I, [P, P, I]), "vx3_set_claim_sizes": (I, [P, I, I]), "vx3_get_tuning": (I, [P, P]),
+        "vx3_set_contact_slots": (I, [P, I]), "vx3_eval_formula": (I, [P, S, S, I, P, I, P]), "vx3_set_profiling": (I, [P, I]), "vx3_set_precision": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
         "vx3_bytes_in_use": (ctypes.c_size_t, [P]),
         "vx3_inspect_vxa": (I, [S, S, P, P, ctypes.c_char_p, I]),
         "vx3_inspect_topology": (I, [S, S, P, P, P, P, P, P, P]),
@@ -336,6 +338,30 @@ class Context:
 
     def set_tuning(self, block_links=0, block_voxels=0, items_links=0, items_voxels=0, graph_steps=0):
         self.L.vx3_set_tuning(self.h, block_links, block_voxels, items_links, items_voxels, graph_steps)
+
+    def set_claim_sizes(self, claim_links=0, claim_voxels=0):
+        self._check(self.L.vx3_set_claim_sizes(self.h, claim_links, claim_voxels))
+
+    def set_contact_slots(self, slots):
+        """Contacts kept in each voxel's own slots for simulations uploaded afterwards (1..16)."""
+        self._check(self.L.vx3_set_contact_slots(self.h, slots))
+
+    def tuning(self):
+        """The launch shape in use (vx3_get_tuning)."""
+        out = np.zeros(8, np.int32)
+        self._check(self.L.vx3_get_tuning(self.h, _p(out)))
+        keys = ("block_links", "block_voxels", "items_links", "items_voxels", "graph_steps", "claim_links", "claim_voxels",
+                "contact_slots")
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    def eval_formula(self, base_xml: str, which: str, vars9, vxd_xml: Optional[str] = None) -> np.ndarray:
+        """A formula of the VXA evaluated on the device for each row of vars9 (n x 9):
+        which = 'stop', 'fitness', 'force_x', 'force_y' or 'force_z'."""
+        w = {"stop": 0, "fitness": 1, "force_x": 2, "force_y": 3, "force_z": 4}[which]
+        v = np.ascontiguousarray(vars9, np.float64).reshape(-1, 9)
+        out = np.zeros(len(v))
+        self._check(self.L.vx3_eval_formula(self.h, _b(base_xml), _b(vxd_xml), w, _p(v), len(v), _p(out)))
+        return out
 
     def autotune(self, ids):
         a = self._ids(ids)

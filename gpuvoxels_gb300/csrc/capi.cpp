@@ -545,6 +545,22 @@ int vx3_autotune(vx3_ctx* c, const vx3_sim_id* ids, int n) {
     return e ? fail(c, e, err) : VX3_OK;
 }
 
+int vx3_set_claim_sizes(vx3_ctx* c, int claim_links, int claim_voxels) {
+    if (!c || claim_links < 0 || claim_voxels < 0) return VX3_E_ARG;
+    return c->eng->set_claims(claim_links, claim_voxels);
+}
+
+int vx3_set_contact_slots(vx3_ctx* c, int slots) {
+    if (!c) return VX3_E_ARG;
+    return c->eng->set_contact_slots(slots) ? fail(c, VX3_E_ARG, "contact slots must be 1..16") : VX3_OK;
+}
+
+int vx3_get_tuning(vx3_ctx* c, int32_t* out8) {
+    if (!c || !out8) return VX3_E_ARG;
+    c->eng->get_tuning(out8);
+    return VX3_OK;
+}
+
 int vx3_set_profiling(vx3_ctx* c, int on) {
     if (!c) return VX3_E_ARG;
     c->eng->set_profiling(on);
@@ -640,6 +656,16 @@ int vx3_inspect_externals(const char* base, const char* vxd, int32_t* dof, float
         }
     }
     return VX3_OK;
+}
+
+int vx3_eval_formula(vx3_ctx* c, const char* base, const char* vxd, int which, const double* vars9, int n, double* out) {
+    if (!c || !base || (n > 0 && (!vars9 || !out)) || n < 0 || which < 0 || which > 4) return VX3_E_ARG;
+    gvx::SimDesc d;
+    std::string err;
+    if (!gvx::parse_vxa(base, vxd, &d, &err)) return fail(c, VX3_E_PARSE, err);
+    const gvx::MathTree& m = which == 0 ? d.stop_formula : which == 1 ? d.fitness : d.force_field[which - 2];
+    int e = c->eng->eval_formula(m, vars9, n, out, &err);
+    return e ? fail(c, e, err) : VX3_OK;
 }
 
 int vx3_inspect_formula(const char* base, const char* vxd, int which, const double* vars, double* out) {

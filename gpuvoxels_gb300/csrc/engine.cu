@@ -49,6 +49,18 @@ __global__ void k_ctl_end_steps(dev::Ctl* ctl, const int* __restrict__ slots, in
     if (c.status == SIM_DONE) c.status = SIM_IDLE;
 }
 
+// One formula evaluated on the device for n variable sets (x, y, z, hit, t, angle,
+// closeness, numClosePairs, num_voxel): the evaluator the step kernels use.
+__global__ void k_eval_formula(const MathTree* m, const double* __restrict__ vars9, int n, double* out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double* v = vars9 + 9 * (size_t)k;
+    MathVars mv;
+    mv.x = v[0]; mv.y = v[1]; mv.z = v[2]; mv.hit = v[3]; mv.t = v[4]; mv.angle = v[5]; mv.closeness = v[6];
+    mv.num_close_pairs = (int)v[7]; mv.num_voxel = (int)v[8];
+    out[k] = mathtree_eval(*m, mv);
+}
+
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // First-fit allocator over one device allocation (the HBM budget).
@@ -127,12 +139,21 @@ public:
     dev::Sim* d_sims_ = nullptr;
     dev::Ctl* d_ctl_ = nullptr;
     std::vector<SimRec*> slot_owner_;
+    // queue tickets of the step kernels (0 links, 1 contacts, 2 voxels, 3 signals) and the
+    // contact spill pool's record count of the step
+    static constexpr int kTickets = 8, kSpillTicket = 4;
     int* d_tickets_ = nullptr;
+    int32_t* d_spill_p_ = nullptr;
+    float* d_spill_f_ = nullptr;
+    int spill_cap_ = 0;
+    static constexpr int kAttachCandPerVoxel = 16;   // attachment candidate pairs kept per voxel and step
+    int contact_inline_ = dev::kContactInline;        // contacts in each voxel's own slots (simulations uploaded later)
     dev::Item* d_items_ = nullptr;
     int cap_items_ = 0;
     double* d_com4_ = nullptr;
     // tuning
     int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 1024, graph_steps_ = 64;
+    int claim_links_ = 32, claim_voxels_ = 32;   // elements a warp claims from the step queues at a time
     // link binning: regrouped every bin_every_ steps (the first step after a batch change always)
     int bin_every_ = 1, bin_phase_ = 0;
     bool bins_dirty_ = true;
@@ -202,6 +223,7 @@ public:
         }
         cudaFree(d_gather_);
         cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_com4_);
+        cudaFree(d_spill_p_); cudaFree(d_spill_f_);
         cudaFree(d_attach_slots_);
         cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
         cudaFree(d_vox_hist_); cudaFree(d_vox_base_); cudaFree(d_vox_total_); cudaFree(d_vox_perm_); cudaFree(d_batch_slots_);
@@ -229,8 +251,12 @@ public:
         }
         CK(cudaMalloc(&arena_base_, budget));
         arena_.init(arena_base_, budget);
-        CK(cudaMalloc(&d_tickets_, 4 * sizeof(int)));
-        CK(cudaMemset(d_tickets_, 0, 4 * sizeof(int)));
+        CK(cudaMalloc(&d_tickets_, kTickets * sizeof(int)));
+        CK(cudaMemset(d_tickets_, 0, kTickets * sizeof(int)));
+        // contact spill pool: 1/64 of the budget in 16-byte records (partner + force), 1M to 64M records
+        spill_cap_ = (int)std::min<size_t>(64u << 20, std::max<size_t>(1u << 20, budget / 64 / 16));
+        CK(cudaMalloc(&d_spill_p_, sizeof(int32_t) * (size_t)spill_cap_));
+        CK(cudaMalloc(&d_spill_f_, 3 * sizeof(float) * (size_t)spill_cap_));
         CK(cudaMalloc(&d_com4_, 4 * sizeof(double)));
         for (Pinned* b : {&up_[0], &up_[1], &rb_, &gen_}) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
         return grow_slots(64, err);
@@ -337,7 +363,7 @@ public:
 
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
-        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, hhead, hnext, cpos, cilia, ffield;
+        size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, cspill, hhead, hnext, cpos, cilia, ffield;
         size_t shift, sig, vlink, targets, init_pos, lnew, cand, cpart, acond;
         size_t zero_from;   // everything from here on starts as zeros
         int hash_size;
@@ -393,15 +419,16 @@ public:
         t.lsf = L->add(4 * 3 * std::max<size_t>(1, nl));
         if (col) {
             t.ccount = L->add(4 * nv);
-            t.cforce = L->add(4 * 3 * dev::kContactCap * nv);
+            t.cforce = L->add(4 * 3 * dev::kContactInline * nv);
+            t.cspill = L->add(4 * nv);
             t.hnext = L->add(4 * nv);
             t.cpos = L->add(16 * nv);
         }
         if (d.enable_signals) t.sig = L->add(8 * dev::SG_FIELDS * nv);
         if (attaches(d)) {
             t.lnew = L->add(4 * nl);
-            t.cand = L->add(8 * (size_t)dev::kContactCap / 2 * nv + 8);
-            t.cpart = L->add(4 * (size_t)dev::kContactCap * nv);
+            t.cand = L->add(8 * (size_t)kAttachCandPerVoxel * nv + 8);
+            t.cpart = L->add(4 * (size_t)dev::kContactInline * nv);
         }
         if (o) *o = t;
     }
@@ -706,7 +733,9 @@ public:
         S.ijk = (const int16_t*)D(o.ijk);
         if (w.desc.collisions) {
             S.surf = (const int32_t*)D(o.surf); S.reach = (const uint32_t*)D(o.reach);
-            S.ccount = (int32_t*)D(o.ccount); S.cforce = (float*)D(o.cforce);
+            S.ccount = (int32_t*)D(o.ccount); S.cforce = (float*)D(o.cforce); S.cspill = (int32_t*)D(o.cspill);
+            S.spill_p = d_spill_p_; S.spill_f = d_spill_f_; S.spill_used = d_tickets_ + kSpillTicket; S.spill_cap = spill_cap_;
+            S.contact_inline = contact_inline_;
             S.hash_head = (int32_t*)D(o.hhead); S.hash_next = (int32_t*)D(o.hnext);
             S.cpos = (float4*)D(o.cpos);
             S.inv_cell = (float)(1.0 / S.cell_size);
@@ -720,7 +749,7 @@ public:
         if (dd.enable_signals || removes_materials(dd) || attaches(dd)) S.vlink = (int32_t*)D(o.vlink);
         if (attaches(dd)) {
             S.nl_cap = (int)nl_cap;
-            S.cand_cap = dev::kContactCap / 2 * (int)nv + 1;
+            S.cand_cap = kAttachCandPerVoxel * (int)nv + 1;
             S.safety_guard = dd.safety_guard;
             S.attach_mask = dd.attach_cond_mask;
             S.lnew = (int32_t*)D(o.lnew);
@@ -1087,7 +1116,7 @@ public:
             if (slot_owner_[slots[i]]->w.desc.enable_signals)
                 CK(copy_async(&d_ctl_[slots[i]].sig_done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
         }
-        CK(cudaMemsetAsync(d_tickets_, 0, 4 * sizeof(int), stream_));
+        CK(cudaMemsetAsync(d_tickets_, 0, kTickets * sizeof(int), stream_));
         return 0;
     }
 
@@ -1126,14 +1155,14 @@ public:
             return (int)std::max<size_t>(1, std::min(full, (elems + block - 1) / block));
         };
         ks_.links(grid_chunks(batch_links_, bl, 0), bl, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
-                  (int)cap_perm_, cap_slots_, d_tickets_);
+                  (int)cap_perm_, cap_slots_, d_tickets_, claim_links_);
         if (prof) cudaEventRecord(evk_[1], st);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
         if (prof) cudaEventRecord(evk_[3], st);
         ks_.voxels(grid_chunks(batch_voxels_, bv, 1), bv, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
-                   (int)cap_vperm_, cap_slots_, d_tickets_);
+                   (int)cap_vperm_, cap_slots_, d_tickets_, claim_voxels_);
         if (prof) cudaEventRecord(evk_[4], st);
         ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_);
         if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
@@ -1847,45 +1876,115 @@ public:
         batch_dirty_ = true;
         return 0;
     }
-    // Project autotuner: time a few graph replays of the batch for each candidate
-    // (block size, elements per work item) and keep the fastest.
+    int set_claims(int cl, int cv) override {
+        if (cl > 0) claim_links_ = std::min(1024, std::max(32, cl & ~31));   // whole warps' worth
+        if (cv > 0) claim_voxels_ = std::min(1024, std::max(32, cv & ~31));
+        batch_dirty_ = true;
+        return 0;
+    }
+    int set_contact_slots(int n) override {
+        if (n < 1 || n > dev::kContactInline) return -6;
+        contact_inline_ = n;
+        return 0;
+    }
+    void get_tuning(int32_t* out8) const override {
+        out8[0] = block_links_; out8[1] = block_voxels_; out8[2] = items_links_; out8[3] = items_voxels_;
+        out8[4] = graph_steps_; out8[5] = claim_links_; out8[6] = claim_voxels_; out8[7] = contact_inline_;
+    }
+    // Project autotuner: times a few steps of the live batch for each candidate launch shape
+    // (threads per block, elements per work item = the grouping window, elements a warp
+    // claims from the queue at a time) and keeps the fastest.  The simulations' device
+    // regions and control blocks are copied aside first and put back afterwards, so tuning
+    // leaves their state as it found it.
+    struct TuneCand { int bl, bv, il, iv, cl, cv; };
+    std::vector<TuneCand> tune_candidates() const {
+        std::vector<TuneCand> c;
+        for (int b : {128, 256})
+            for (int il : {256, 1024})
+                for (int cl : {32, 64, 128}) c.push_back({b, b, il, il / 2, cl, cl});
+        return c;
+    }
     int autotune(const int64_t* ids, int n, std::string* err) override {
         std::vector<SimRec*> rs;
         if (int e = prepare(ids, n, &rs, err)) return e;
         std::vector<int> slots;
         for (auto* r : rs) slots.push_back(r->slot);
-        struct Cand { int bl, bv, il, iv; };
-        const Cand cands[] = {{128, 128, 256, 128}, {128, 256, 512, 256}, {256, 256, 256, 256}, {256, 256, 512, 256}, {256, 256, 1024, 512}};
+        if (slots.empty()) return 0;
+        const std::vector<TuneCand> cands = tune_candidates();
         double best = 1e30;
-        Cand bc = cands[2];
-        // snapshot the simulations' device regions so tuning does not advance them
-        std::vector<std::vector<char>> snap(rs.size());
+        TuneCand bc{block_links_, block_voxels_, items_links_, items_voxels_, claim_links_, claim_voxels_};
+        // copy the simulations' device regions aside (on the device when there is room)
+        size_t total = 0;
+        for (auto* r : rs) total += r->bytes;
+        char* d_snap = nullptr;
+        std::vector<std::vector<char>> snap;
+        if (cudaMalloc(&d_snap, total) != cudaSuccess) {
+            cudaGetLastError();   // the failed allocation is not an error of the engine
+            d_snap = nullptr;
+            snap.resize(rs.size());
+        }
         std::vector<dev::Ctl> csnap(rs.size());
+        size_t at = 0;
         for (size_t i = 0; i < rs.size(); i++) {
-            snap[i].resize(rs[i]->bytes);
-            CK(copy_sync(snap[i].data(), arena_base_ + rs[i]->off, rs[i]->bytes, cudaMemcpyDeviceToHost));
-            CK(copy_sync(&csnap[i], d_ctl_ + rs[i]->slot, sizeof(dev::Ctl), cudaMemcpyDeviceToHost));
+            if (d_snap) CK(copy_async(d_snap + at, arena_base_ + rs[i]->off, rs[i]->bytes, cudaMemcpyDeviceToDevice, stream_));
+            else {
+                snap[i].resize(rs[i]->bytes);
+                CK(copy_async(snap[i].data(), arena_base_ + rs[i]->off, rs[i]->bytes, cudaMemcpyDeviceToHost, stream_));
+            }
+            at += rs[i]->bytes;
+            CK(copy_async(&csnap[i], d_ctl_ + rs[i]->slot, sizeof(dev::Ctl), cudaMemcpyDeviceToHost, stream_));
         }
+        CK(cudaStreamSynchronize(stream_));
         std::vector<int64_t> tg(slots.size(), (int64_t)1 << 40);
-        for (const Cand& c : cands) {
-            block_links_ = c.bl; block_voxels_ = c.bv; items_links_ = c.il; items_voxels_ = c.iv;
-            if (int e = build_items(slots, err)) return e;
-            if (int e = set_running(slots, tg, err)) return e;
-            for (int w = 0; w < 2; w++) launch_step(stream_, false);
-            CK(cudaEventRecord(ev0_, stream_));
-            for (int k = 0; k < 8; k++) launch_step(stream_, false);
-            CK(cudaEventRecord(ev1_, stream_));
-            CK(cudaEventSynchronize(ev1_));
-            float ms;
-            cudaEventElapsedTime(&ms, ev0_, ev1_);
-            if (ms < best) { best = ms; bc = c; }
-        }
+        const int reps = 2;
+        for (int rep = 0; rep < reps; rep++)
+            for (const TuneCand& c : cands) {
+                block_links_ = c.bl; block_voxels_ = c.bv; items_links_ = c.il; items_voxels_ = c.iv;
+                claim_links_ = c.cl; claim_voxels_ = c.cv;
+                if (int e = build_items(slots, err)) { cudaFree(d_snap); return e; }
+                if (int e = set_running(slots, tg, err)) { cudaFree(d_snap); return e; }
+                for (int w = 0; w < 2; w++) launch_step(stream_, false);
+                CK(cudaEventRecord(ev0_, stream_));
+                for (int k = 0; k < 6; k++) launch_step(stream_, false);
+                CK(cudaEventRecord(ev1_, stream_));
+                CK(cudaEventSynchronize(ev1_));
+                float ms;
+                cudaEventElapsedTime(&ms, ev0_, ev1_);
+                if (ms < best) { best = ms; bc = c; }
+            }
+        at = 0;
         for (size_t i = 0; i < rs.size(); i++) {
-            CK(copy_sync(arena_base_ + rs[i]->off, snap[i].data(), rs[i]->bytes, cudaMemcpyHostToDevice));
-            CK(copy_sync(d_ctl_ + rs[i]->slot, &csnap[i], sizeof(dev::Ctl), cudaMemcpyHostToDevice));
+            if (d_snap) CK(copy_async(arena_base_ + rs[i]->off, d_snap + at, rs[i]->bytes, cudaMemcpyDeviceToDevice, stream_));
+            else CK(copy_async(arena_base_ + rs[i]->off, snap[i].data(), rs[i]->bytes, cudaMemcpyHostToDevice, stream_));
+            at += rs[i]->bytes;
+            CK(copy_async(d_ctl_ + rs[i]->slot, &csnap[i], sizeof(dev::Ctl), cudaMemcpyHostToDevice, stream_));
         }
+        CK(cudaStreamSynchronize(stream_));
+        cudaFree(d_snap);
         block_links_ = bc.bl; block_voxels_ = bc.bv; items_links_ = bc.il; items_voxels_ = bc.iv;
+        claim_links_ = bc.cl; claim_voxels_ = bc.cv;
+        tuned_ms_ = best;
         batch_dirty_ = true;
+        if (graph_) { cudaGraphExecDestroy(graph_); graph_ = nullptr; }
+        return 0;
+    }
+    double tuned_ms_ = 0;
+
+    int eval_formula(const MathTree& m, const double* vars9, int n, double* out, std::string* err) override {
+        if (n <= 0) return 0;
+        char* d = nullptr;
+        const size_t o_vars = align256(sizeof(MathTree)), o_out = o_vars + align256(72 * (size_t)n);
+        CK(cudaMalloc(&d, o_out + 8 * (size_t)n));
+        auto fail = [&](cudaError_t e) { cudaFree(d); if (err) *err = cudaGetErrorString(e); return -5; };
+        cudaError_t e;
+        if ((e = copy_async(d, &m, sizeof(MathTree), cudaMemcpyHostToDevice, stream_)) != cudaSuccess) return fail(e);
+        if ((e = copy_async(d + o_vars, vars9, 72 * (size_t)n, cudaMemcpyHostToDevice, stream_)) != cudaSuccess) return fail(e);
+        k_eval_formula<<<(unsigned)((n + 127) / 128), 128, 0, stream_>>>((const MathTree*)d, (const double*)(d + o_vars), n,
+                                                                         (double*)(d + o_out));
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+        if ((e = copy_async(out, d + o_out, 8 * (size_t)n, cudaMemcpyDeviceToHost, stream_)) != cudaSuccess) return fail(e);
+        if ((e = cudaStreamSynchronize(stream_)) != cudaSuccess) return fail(e);
+        cudaFree(d);
         return 0;
     }
 };

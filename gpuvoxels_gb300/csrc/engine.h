@@ -100,6 +100,16 @@ public:
     virtual int device_check(std::string* err) = 0;
     virtual int set_tuning(int block_links, int block_voxels, int items_links, int items_voxels, int graph_steps) = 0;
     virtual int autotune(const int64_t* ids, int n, std::string* err) = 0;
+    // Elements a warp claims from the link / voxel queues at a time (multiples of 32; 0 keeps).
+    virtual int set_claims(int claim_links, int claim_voxels) = 0;
+    // Contacts kept in each voxel's own slots (1..kContactInline) for simulations uploaded later.
+    virtual int set_contact_slots(int n) = 0;
+    // block_links, block_voxels, items_links, items_voxels, graph_steps, claim_links,
+    // claim_voxels, contact slots
+    virtual void get_tuning(int32_t* out8) const = 0;
+    // A formula evaluated on the device for n variable sets of 9 (x, y, z, hit, t, angle,
+    // closeness, numClosePairs, num_voxel): the step kernels' evaluator.
+    virtual int eval_formula(const MathTree& m, const double* vars9, int n, double* out, std::string* err) = 0;
     virtual int64_t sim_bytes(const SimDesc& d) const = 0;
     virtual int64_t sim_bytes_id(int64_t id) = 0;
     // 0: exact build (no contraction, the reference's rounding); 1: FMA build

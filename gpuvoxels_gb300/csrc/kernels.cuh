@@ -463,20 +463,24 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sim
     }
 }
 
-// Warps take 32-link chunks of the binned list (one atomic per chunk); each lane
-// updates one link of whatever simulation it belongs to.
+// Warps take chunks of `claim` consecutive links of the binned list (one atomic per
+// chunk; claim is a multiple of 32, so each lane updates claim/32 links of whatever
+// simulations they belong to).
 __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
-                                                                     const int* __restrict__ total, int cap, int n_slots, int* tickets) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; }
+                                                                     const int* __restrict__ total, int cap, int n_slots, int* tickets,
+                                                                     int claim) {
+    // this step's queues of the kernels that follow, and the contact spill pool's records
+    if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; tickets[4] = 0; }
     const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
     for (;;) {
         int chunk = 0;
         if (lane == 0) chunk = atomicAdd(&tickets[0], 1);
         chunk = __shfl_sync(0xffffffffu, chunk, 0);
-        const int k = chunk * 32 + lane;
-        if (chunk * 32 >= n) break;
-        if (k < n) {
+        const int k0 = chunk * claim;
+        if (k0 >= n) break;
+        const int k1 = min(n, k0 + claim);
+        for (int k = k0 + lane; k < k1; k += 32) {
             const int2 e = __ldg(perm + k);
             if ((unsigned)e.x >= (unsigned)n_slots) continue;   // never: the grouping lists running slots
             Ctl& c = ctl[e.x];
@@ -540,28 +544,17 @@ __device__ __forceinline__ bool maybe_touching(float4 a, float4 b, float env_rad
     return dx * dx + dy * dy + dz * dz <= lim * lim;
 }
 
-// Spatial-hash broadphase + exact contact forces for one surface voxel.  The
-// reference keeps a conservative pair list of surface voxels that are not
-// within 5 lattice links of each other (Voxelyze3/src/old/Voxelyze.cpp:671-751,
-// VX_Voxel.cpp:394-417) and sums the pair forces in increasing partner order;
-// pairs that do not overlap contribute exactly zero, so summing the
-// overlapping pairs in partner order reproduces it.
-__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
-    if (S.flags & SF_DYNSURF) {
-        // the surface set changes during the run: every voxel is listed, interior and
-        // removed ones have no contacts
-        const uint32_t f = S.vfl[v];
-        if (f & (VF_INTERIOR | VF_REMOVED)) { S.ccount[v] = 0; return; }
-    }
+// Calls fn(q) for every partner q of surface voxel v in this step's contact list, in no
+// particular order: hashed voxels in the 27 cells around v that are not within 5 lattice
+// links of v (nor linked to it by a link made at run time) and overlap it by the exact test.
+template <typename Fn>
+__device__ __forceinline__ void for_each_contact(const Sim& S, int v, int parity, Fn fn) {
     const float4 pv = S.cpos[v];
     const float ic = S.inv_cell;
     const int cx = cell_of(pv.x, ic), cy = cell_of(pv.y, ic), cz = cell_of(pv.z, ic);
     const int nv = S.nv;
     const int vx = S.ijk[v], vy = S.ijk[nv + v], vz = S.ijk[2 * nv + v];
     const int* head = S.hash_head + (size_t)parity * S.hash_size;
-    int partners[kContactCap];
-    int np = 0;
-    bool overflow = false;
     for (int dz = -1; dz <= 1; dz++)
         for (int dy = -1; dy <= 1; dy++)
             for (int dx = -1; dx <= 1; dx++) {
@@ -598,27 +591,73 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
                                 }
                         }
                         if (!near) {
-                            const int a = v < q ? v : q, b = v < q ? q : v;
                             float f3[3];
-                            // cheap reject before the exact test
-                            if (pair_force(S, a, b, f3)) {
-                                if (np < kContactCap) {
-                                    int k = np++;
-                                    while (k > 0 && partners[k - 1] > q) { partners[k] = partners[k - 1]; k--; }
-                                    partners[k] = q;
-                                } else overflow = true;
-                            }
+                            if (pair_force(S, v < q ? v : q, v < q ? q : v, f3)) fn(q);
                         }
                     }
                     q = nq;
                 }
             }
-    if (overflow) atomicOr(&c.error, 1);
-    float* out = S.cforce + (size_t)v * 3 * kContactCap;
-    if (S.cpart)   // partner ids, kept where attachment may drop a pair's force
-        for (int k = 0; k < np; k++) S.cpart[(size_t)v * kContactCap + k] = partners[k];
+}
+
+// Spatial-hash broadphase + exact contact forces for one surface voxel.  The
+// reference keeps a conservative pair list of surface voxels that are not
+// within 5 lattice links of each other (Voxelyze3/src/old/Voxelyze.cpp:671-751,
+// VX_Voxel.cpp:394-417) and sums the pair forces in increasing partner order;
+// pairs that do not overlap contribute exactly zero, so summing the
+// overlapping pairs in partner order reproduces it.  The list has no length
+// limit: up to S.contact_inline (at most kContactInline) contacts go to the
+// voxel's own slots; a voxel with more takes a run of records of the spill pool, fills it with its
+// partners in a second pass over the hash and sorts them there.
+__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
+    if (S.flags & SF_DYNSURF) {
+        // the surface set changes during the run: every voxel is listed, interior and
+        // removed ones have no contacts
+        const uint32_t f = S.vfl[v];
+        if (f & (VF_INTERIOR | VF_REMOVED)) { S.ccount[v] = 0; return; }
+    }
+    // the `cap` smallest partners in increasing order, and the number of partners
+    const int cap = min(max(S.contact_inline, 1), kContactInline);
+    int partners[kContactInline] = {};
+    int np = 0, ntot = 0;
+    for_each_contact(S, v, parity, [&](int q) {
+        ntot++;
+        if (np == cap) {
+            if (q > partners[cap - 1]) return;
+            np--;   // the largest kept partner gives way
+        }
+        int k = np++;
+        while (k > 0 && partners[k - 1] > q) { partners[k] = partners[k - 1]; k--; }
+        partners[k] = q;
+    });
+    int32_t* sp = nullptr;   // the spill run of a voxel with more than kContactInline partners
+    float* out = S.cforce + (size_t)v * 3 * kContactInline;
+    if (ntot > cap) {
+        const int off = atomicAdd(S.spill_used, ntot);
+        if (off < 0 || (unsigned)off > (unsigned)(S.spill_cap - ntot)) {
+            // the pool's records for this step are used up: the simulation stops with an error
+            atomicOr(&c.error, 2);
+            S.ccount[v] = 0;
+            return;
+        }
+        sp = S.spill_p + off;
+        int k = 0;
+        for_each_contact(S, v, parity, [&](int q) { if (k < ntot) sp[k++] = q; });
+        for (int i = 1; i < k; i++) {   // insertion sort by partner index (runs are short)
+            const int q = sp[i];
+            int j = i;
+            while (j > 0 && sp[j - 1] > q) { sp[j] = sp[j - 1]; j--; }
+            sp[j] = q;
+        }
+        np = k;
+        out = S.spill_f + 3 * (size_t)off;
+        S.cspill[v] = off;
+    } else if (S.cpart) {   // partner ids, kept where attachment may drop a pair's force
+        for (int k = 0; k < np; k++) S.cpart[(size_t)v * kContactInline + k] = partners[k];
+    }
+    auto partner = [&](int k) { return sp ? sp[k] : partners[k]; };
     for (int k = 0; k < np; k++) {
-        const int q = partners[k];
+        const int q = partner(k);
         float f3[3];
         pair_force(S, v < q ? v : q, v < q ? q : v, f3);
         const float sgn = v < q ? 1.0f : -1.0f;   // contactForce(): +force on voxel1, -force on voxel2
@@ -634,7 +673,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
         const VMat& mm = S.vm[mv];
         if ((fv & VF_ATTACH) && (mm.vx3 & VM_STICKY) && !(mm.vx3 & VM_FIXED)) {
             for (int k = 0; k < np; k++) {
-                const int q = partners[k];
+                const int q = partner(k);
                 if (q < v || __ldg(S.vmat + q) != mv || !(S.vfl[q] & VF_ATTACH)) continue;
                 const int slot = atomicAdd(&c.n_cand, 1);
                 if (slot < S.cand_cap) { S.cand[2 * slot] = v; S.cand[2 * slot + 1] = q; }
@@ -649,7 +688,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
         int pairs = 0;
         bool hit = false;
         for (int k = 0; k < np; k++) {
-            const int q = partners[k];
+            const int q = partner(k);
             const bool tq = S.vm[__ldg(S.vmat + q)].vx3 & VM_TARGET;
             if (tv != tq) { hit = true; if (q > v) pairs++; }
         }
@@ -802,7 +841,7 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         F.z += m.gravForceD;
         if (flags & SF_COLLIDE) {
             const int nc = S.ccount[v];
-            const float* cf = S.cforce + (size_t)v * 3 * kContactCap;
+            const float* cf = nc <= S.contact_inline ? S.cforce + (size_t)v * 3 * kContactInline : S.spill_f + 3 * (size_t)S.cspill[v];
             for (int k = 0; k < nc; k++) { F.x -= cf[3 * k]; F.y -= cf[3 * k + 1]; F.z -= cf[3 * k + 2]; }
         }
         // VX3 cilia (gpu_update_cilia_force, VX3_VoxelyzeKernel.cu:846-859; VX3_Voxel::force,
@@ -1076,9 +1115,11 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
 }
 
 __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxels(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
-                                                                       const int* __restrict__ total, int cap, int n_slots, int* tickets) {
+                                                                       const int* __restrict__ total, int cap, int n_slots, int* tickets,
+                                                                       int claim) {
     // the voxels of the running simulations, grouped by key like the links (k_bin_*); warps
-    // take 32-voxel chunks, so no warp waits at a block barrier for a costlier one
+    // take chunks of `claim` voxels (a multiple of 32), so no warp waits at a block barrier
+    // for a costlier one
     if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
     const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
@@ -1086,9 +1127,10 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxel
         int chunk = 0;
         if (lane == 0) chunk = atomicAdd(&tickets[2], 1);
         chunk = __shfl_sync(0xffffffffu, chunk, 0);
-        if (chunk * 32 >= n) break;
-        const int k = chunk * 32 + lane;
-        if (k < n) {
+        const int k0 = chunk * claim;
+        if (k0 >= n) break;
+        const int k1 = min(n, k0 + claim);
+        for (int k = k0 + lane; k < k1; k += 32) {
             const int2 e = __ldg(perm + k);
             if ((unsigned)e.x >= (unsigned)n_slots) continue;   // never: the grouping lists running slots
             const Ctl& c = ctl[e.x];
@@ -1170,8 +1212,9 @@ __device__ bool linked_within(const Sim& S, int from, int target, int depth) {
 // Drops voxel v's contact force from partner q for this step (a zero force adds nothing).
 __device__ void drop_pair_contact(const Sim& S, int v, int q) {
     const int n = S.ccount[v];
-    const int32_t* part = S.cpart + (size_t)v * kContactCap;
-    float* f = S.cforce + (size_t)v * 3 * kContactCap;
+    const bool spilled = n > S.contact_inline;
+    const int32_t* part = spilled ? S.spill_p + S.cspill[v] : S.cpart + (size_t)v * kContactInline;
+    float* f = spilled ? S.spill_f + 3 * (size_t)S.cspill[v] : S.cforce + (size_t)v * 3 * kContactInline;
     for (int k = 0; k < n; k++)
         if (part[k] == q) { f[3 * k] = 0.0f; f[3 * k + 1] = 0.0f; f[3 * k + 2] = 0.0f; }
 }
@@ -1386,13 +1429,13 @@ inline void l_bins(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, BinList la,
     k_bin_scatter<<<g, 256, 0, s>>>(sims, ctl, la, lb);
 }
 inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
-                    int* tk) {
-    k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk);
+                    int* tk, int claim) {
+    k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk, claim);
 }
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
-                     int* tk) {
-    k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk);
+                     int* tk, int claim) {
+    k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk, claim);
 }
 inline void l_sim_end(cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
     if (n > 0) k_sim_end<<<n, 256, 0, s>>>(sims, ctl, slots, n);

@@ -12,12 +12,13 @@ struct KernelSet {
     // groups the elements of the running simulations by key for two lists at once (links and
     // voxels), in windows of work items
     void (*bins)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, dev::BinList links, dev::BinList voxels);
-    // perm holds at most `cap` entries; entries name slots below n_slots
+    // perm holds at most `cap` entries; entries name slots below n_slots; warps claim `claim`
+    // entries at a time (a multiple of 32)
     void (*links)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int cap,
-                  int n_slots, int* tickets);
+                  int n_slots, int* tickets, int claim);
     void (*contacts)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
     void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int cap,
-                   int n_slots, int* tickets);
+                   int n_slots, int* tickets, int claim);
     // the end of the step for n simulations (slot list): centre-of-mass sample, time, stop
     void (*sim_end)(cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
     // VX3 signals relayed between neighbours (after voxels, over the voxel items)

@@ -10,7 +10,11 @@ namespace gvx {
 namespace dev {
 
 // ---------------------------------------------------------------- layouts
-constexpr int kContactCap = 32;       // contacts kept per voxel per step
+// Contact list of one voxel in one step: up to kContactInline contacts sit in the voxel's
+// own slots; a voxel with more takes a run of records from the context's spill pool, so the
+// list is unbounded like the reference's (only the pool's size, a fraction of the HBM
+// budget, limits the contacts of a whole step).
+constexpr int kContactInline = 16;
 constexpr int kReachWords = 8;        // 231 offsets of the L1 ball of radius 5 -> 8 x 32 bits
 constexpr int kOrderKeysBins = 10;    // link ordering keys (the step kernels' kOrderKeys)
 
@@ -132,7 +136,15 @@ struct Sim {
     const int16_t* ijk;         // lattice indices, 3 blocks of nv
     const uint32_t* reach;      // kReachWords per voxel
     int32_t* ccount;            // per voxel
-    float* cforce;              // 3*kContactCap per voxel
+    float* cforce;              // 3*kContactInline per voxel
+    int32_t* cspill;            // per voxel: first spill record when ccount > kContactInline
+    // the context's spill pool (shared by every simulation of a step): partner and force
+    // records, the records taken this step (reset by k_links) and the pool's capacity
+    int32_t* spill_p;
+    float* spill_f;
+    int32_t* spill_used;
+    int32_t spill_cap;
+    int32_t contact_inline;     // contacts kept in the voxel's own slots (1..kContactInline); more spill
     int32_t* hash_head;         // 2 tables of hash_size
     int32_t* hash_next;         // per voxel
     float4* cpos;               // per hashed voxel: position rounded to float, float base size (broadphase only)
@@ -157,7 +169,7 @@ struct Sim {
     int32_t attach_mask;        // bit k: AttachCondition k given (a missing one holds)
     int32_t* lnew;              // per link: steps left with forces scaled by 0.01
     int32_t* cand;              // 2 per candidate pair
-    int32_t* cpart;             // contact partners, kContactCap per voxel
+    int32_t* cpart;             // contact partners, kContactInline per voxel
     const MathTree* attach_cond;   // 5 formulas
 };
 

@@ -1,11 +1,14 @@
 // Centre of mass without any device allocation.
 //
-// Who needs this: callers that cannot call cudaMalloc — code that records into
-// a CUDA graph (stream capture forbids synchronous allocation), host processes
-// whose device memory is owned by another framework's allocator or pool, and
-// real-time loops that must not allocate.  They pass device inputs and a
-// device output; the two-pass reduction's per-block partial sums live in a
-// fixed scratch array compiled into this library.
+// Who needs this: callers that cannot call cudaMalloc.  A plugin that runs
+// inside another framework's process often finds all device memory reserved by
+// that framework's caching allocator or pool, so a cudaMalloc of its own fails
+// or fragments the pool; a real-time control loop cannot take cudaMalloc's
+// implicit device synchronisation and unbounded latency; a service that admits
+// work against an HBM budget cannot have allocations it does not account for.
+// They pass device inputs and a device output; the two-pass reduction's
+// per-block partial sums live in a fixed scratch array compiled into this
+// library.
 //
 // The scratch array holds kNoAllocBlocks x 4 doubles (64 KiB).  Every GPU
 // that loads the library keeps it until the process exits.  All calls share
@@ -74,7 +77,8 @@ __global__ void k_com_finish(const double* __restrict__ partials, int nblocks, d
     }
 }
 
-// Device address of the scratch array, resolved once per device with that device current.
+// Device address of the scratch array, resolved once per device with that device current and
+// kept for the life of the process (a cudaDeviceReset of that device invalidates it).
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch[kMaxDevices] = {};
@@ -85,10 +89,15 @@ extern "C" int vx3_center_of_mass_noalloc(const double* x, const double* y, cons
                                           double* out4, void* stream) {
     if (!x || !y || !z || !mass || !out4 || n < 0) return VX3_E_ARG;
     if (n > kNoAllocMaxPoints) return VX3_E_LIMIT;   // beyond the fixed scratch: 4,194,304 points at most
+    // an error already pending on this thread belongs to the caller: leave it for them to
+    // read, launch nothing, so that the status below speaks only of this call's launches
+    if (cudaPeekAtLastError() != cudaSuccess) return VX3_E_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return VX3_E_CUDA;
     double* scratch = nullptr;
     {
+        // set-up, once per device, with that device current: the device address of the
+        // scratch array (the array's name in host code is not a device address)
         std::lock_guard<std::mutex> lock(g_mu);
         if (!g_scratch[dev]) {
             void* p = nullptr;
@@ -100,6 +109,7 @@ extern "C" int vx3_center_of_mass_noalloc(const double* x, const double* y, cons
     cudaStream_t s = (cudaStream_t)stream;
     const int nblocks = n == 0 ? 1 : (int)((n + (int64_t)kNoAllocThreads * kNoAllocPerThread - 1) / ((int64_t)kNoAllocThreads * kNoAllocPerThread));
     k_com_partials<<<nblocks, kNoAllocThreads, 0, s>>>(x, y, z, mass, n, scratch);
+    if (cudaGetLastError() != cudaSuccess) return VX3_E_CUDA;
     k_com_finish<<<1, kNoAllocThreads, 0, s>>>(scratch, nblocks, out4);
     return cudaGetLastError() == cudaSuccess ? VX3_OK : VX3_E_CUDA;
 }

@@ -21,7 +21,20 @@ ACTIVE = dict(E=1e6, rho=1000.0, nu=0.35, cte=0.01, mus=1.0, muk=0.5)
 
 
 def largest_component(cells: np.ndarray) -> np.ndarray:
-    """Keeps the largest 6-connected component of a boolean (Z, Y, X) array."""
+    """Keeps the largest 6-connected component of a boolean (Z, Y, X) array (the first one in
+    raster order among equals): scipy.ndimage.label with its default structure where scipy is
+    installed, else a breadth-first search with the same result."""
+    try:
+        from scipy import ndimage
+    except ImportError:
+        ndimage = None
+    if ndimage is not None:
+        lab, n = ndimage.label(cells)
+        if n == 0:
+            return cells.copy()
+        cnt = np.bincount(lab.ravel())
+        cnt[0] = 0
+        return lab == int(cnt.argmax())
     filled = np.argwhere(cells)
     if len(filled) == 0:
         return cells.copy()
@@ -143,9 +156,7 @@ def config1_batch(n: int = 512, seed: int = 1, sim_time: float = 0.5, **kw) -> L
     for i in range(n):
         s = int(rng.integers(6, 21))
         fill = float(rng.uniform(0.3, 0.9))
-        Es = 10 ** rng.uniform(5, 7, size=4)
-        n_act = int(rng.integers(1, 3))
-        mats = [dict(E=float(E), rho=1000.0, nu=0.35, cte=(0.01 if k < n_act else 0.0), mus=1.0, muk=0.5) for k, E in enumerate(Es)]
+        mats = config1_materials(rng)
         out.append(random_creature(int(rng.integers(1 << 31)), (s, s, s), fill, mats, stop_time=sim_time, **kw))
     return out
 
@@ -160,21 +171,33 @@ def config2_batch(n: int = 64, seed: int = 2, **kw) -> List[Creature]:
     return [random_creature(int(rng.integers(1 << 31)), (40, 40, 40), 0.5, mats, collision=True, **kw) for _ in range(n)]
 
 
-def serving_requests(n: int = 64, seed: int = 4, v_range=(100, 10000), horizon_range=(1000, 5000),
-                     collide_frac: float = 0.2) -> List[tuple]:
-    """Serving requests: (creature, horizon_steps) with the voxel count log-uniform in v_range,
-    the horizon uniform in horizon_range and a fraction with self-collision on (contraction-only
-    actuation for those).  Cubic lattices at fill U(0.5, 0.9), largest component kept."""
+def config1_materials(rng) -> List[dict]:
+    """Four materials with E log-uniform in [1e5, 1e7] Pa, rho=1000, nu=0.35; the first one or
+    two actuated (CTE 0.01), as in the batched configuration."""
+    Es = 10 ** rng.uniform(5, 7, size=4)
+    n_act = int(rng.integers(1, 3))
+    return [dict(E=float(E), rho=1000.0, nu=0.35, cte=(0.01 if k < n_act else 0.0), mus=1.0, muk=0.5) for k, E in enumerate(Es)]
+
+
+def serving_requests(n: int = 64, seed: int = 4, v_range=(100, 100000), horizon_range=(1000, 50000),
+                     collide_frac: float = 0.2, fill_range=(0.5, 0.9)) -> List[tuple]:
+    """Serving requests: (creature, horizon_steps).  The target voxel count is log-uniform in
+    v_range and sets a cubic lattice's side from the fill; materials as in the batched
+    configuration; the horizon is uniform in horizon_range; a fraction has self-collision on
+    (with contraction-only actuation).  The fill is drawn from U(0.5, 0.9) rather than the batch's
+    U(0.3, 0.9): below the cubic lattice's percolation threshold (about 0.31) the largest
+    component holds a vanishing share of the cells and the voxel count could not follow its draw."""
     rng = np.random.default_rng(seed)
-    mats = [PASSIVE, ACTIVE]
     out = []
     for _ in range(n):
         v = math.exp(rng.uniform(math.log(v_range[0]), math.log(v_range[1])))
-        fill = float(rng.uniform(0.5, 0.9))
+        fill = float(rng.uniform(*fill_range))
         s = max(2, int(round((v / fill) ** (1.0 / 3.0))))
         collide = bool(rng.random() < collide_frac)
         kw = dict(collision=True, expansion=False) if collide else {}
+        mats = config1_materials(rng)
         c = random_creature(int(rng.integers(1 << 31)), (s, s, s), fill, mats, **kw)
+        c.meta["collide"] = collide
         out.append((c, int(rng.integers(horizon_range[0], horizon_range[1] + 1))))
     return out
 

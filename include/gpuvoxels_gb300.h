@@ -119,7 +119,9 @@ int vx3_get_result(vx3_ctx* ctx, vx3_sim_id id, vx3_result* out);
 int vx3_sim_info_get(vx3_ctx* ctx, vx3_sim_id id, vx3_sim_info* out);
 /* Voxel and link counts of many simulations, from the host-side description only (no
  * device read): what VX3_VoxelyzeKernel keeps as num_d_voxels / num_d_links
- * (Voxelyze3/src/VX3/VX3_VoxelyzeKernel.cuh:72,79).  Either output may be NULL. */
+ * (Voxelyze3/src/VX3/VX3_VoxelyzeKernel.cuh:72,79).  Either output may be NULL.
+ * num_link is the number of links loaded from the VXA: links that VX3 attachment (EnableAttach)
+ * creates during the run are not in it; vx3_get_links reports the live count. */
 int vx3_sim_sizes(vx3_ctx* ctx, const vx3_sim_id* ids, int n, int32_t* num_voxel, int32_t* num_link);
 
 /* Voxel state in the reference's CVX_Voxel member layout (Voxelyze3/src/old/VX_Voxel.h:166-182):
@@ -177,8 +179,23 @@ int vx3_transfer_bytes(vx3_ctx* ctx, int64_t* h2d, int64_t* d2h);
 /* Tuning: threads per block and elements per work item for the link and voxel
  * launches, and steps per captured graph; 0 keeps the current value. */
 int vx3_set_tuning(vx3_ctx* ctx, int block_links, int block_voxels, int items_links, int items_voxels, int graph_steps);
-/* Times candidate launch shapes on the given simulations (state restored afterwards) and keeps the fastest. */
+/* Elements (links, voxels) a warp claims from the step kernels' work queues at a time: multiples of 32
+ * (0 keeps the current value).  No reference counterpart: the reference launches one thread per element. */
+int vx3_set_claim_sizes(vx3_ctx* ctx, int claim_links, int claim_voxels);
+/* Times candidate launch shapes on the given simulations and keeps the fastest: threads per block,
+ * elements per work item (the grouping window) and elements a warp claims at a time.  The simulations'
+ * device state is copied aside before and put back after, so their results are those of an untuned run.
+ * No reference counterpart (the reference's launch shapes are fixed, VX3_VoxelyzeKernel.cu:237-359). */
 int vx3_autotune(vx3_ctx* ctx, const vx3_sim_id* ids, int n);
+/* The launch shape in use: out8 = threads per block (links, voxels), elements per work item (links,
+ * voxels), steps per captured graph, elements per claim (links, voxels), contact slots per voxel. */
+int vx3_get_tuning(vx3_ctx* ctx, int32_t* out8);
+/* Contacts kept in each voxel's own slots (1..16, default 16) for simulations uploaded afterwards; a voxel
+ * with more contacts in a step takes records of the context's spill pool (1/64 of the HBM budget), so the
+ * contact list has no per-voxel limit, like the reference's CVX_Voxel::colWatch vector
+ * (Voxelyze3/src/old/Voxelyze.cpp:726-751).  A memory/speed knob only: results do not depend on it.
+ * A step whose contacts overflow the whole pool stops the simulations concerned with VX3_SIM_ERROR. */
+int vx3_set_contact_slots(vx3_ctx* ctx, int slots);
 int vx3_set_profiling(vx3_ctx* ctx, int on);
 /* Kernel build used by the context (no reference counterpart: the reference has one GPU build).
  * VX3_EXACT (default): every FP64/FP32 multiply and add rounded separately, as the reference's CPU path.
@@ -189,19 +206,24 @@ int vx3_set_profiling(vx3_ctx* ctx, int on);
 int vx3_set_precision(vx3_ctx* ctx, int mode);
 
 /* Mass-weighted centre of mass of n points already on the device, for callers that cannot
- * allocate device memory: code recording a CUDA graph (stream capture forbids cudaMalloc),
- * processes whose device memory belongs to another framework's allocator, real-time loops.
+ * allocate device memory: a plugin inside another framework whose caching allocator or pool owns
+ * the device memory, a real-time loop that cannot take cudaMalloc's implicit synchronisation and
+ * latency, a service whose HBM budget must account for every allocation.
  * This entry point has no counterpart in the reference.  It is the engine's centre-of-mass
  * reduction (per-block partial sums, then one fixed-order fold) with its scratch in a fixed
  * array compiled into the library, so it calls no cudaMalloc, cudaFree or allocating routine.
- *   x, y, z[n] (double), mass[n] (float): device inputs; out4: device output (cx, cy, cz, total mass);
+ *   x, y, z[n] (double), mass[n] (float): device inputs; out4: device output (cx, cy, cz, total mass;
+ *   zeros for n = 0 or a total mass of 0);
  *   stream: a cudaStream_t, or NULL for the legacy default stream; the work is only enqueued.
  * Limit: n <= VX3_NOALLOC_MAX_POINTS; larger n returns VX3_E_LIMIT without launching anything.
+ * A CUDA error already pending on the calling thread makes it return VX3_E_CUDA without launching
+ * and leaves that error pending for the caller.
  * The scratch (64 KiB) stays resident on every GPU that loads the library until the process exits.
- * The first call on a device resolves the scratch array's device address with that device current;
- * make that first call before any stream capture.  All calls share the scratch and it keeps the last
- * call's contents (each call overwrites everything it reads); calls that overlap on the GPU race,
- * so serialise them (one stream, or events between streams). */
+ * The first call on a device resolves the scratch array's device address with that device current
+ * (kept for the life of the process; a cudaDeviceReset of the device invalidates it); make that first
+ * call before any stream capture.  All calls share the scratch and it keeps the last call's contents
+ * (each call overwrites everything it reads); calls that overlap on the GPU race, so serialise them
+ * (one stream, or events between streams). */
 #define VX3_NOALLOC_MAX_POINTS 4194304
 int vx3_center_of_mass_noalloc(const double* x, const double* y, const double* z, const float* mass, int64_t n, double* out4,
                                void* stream);
@@ -234,6 +256,13 @@ int vx3_inspect_topology(const char* base_vxa_xml, const char* vxd_xml_or_null, 
 /* Stop/fitness formula evaluation as the engine performs it (Utils/VX3_MathTree.h:50-192);
  * which: 0 stop condition, 1 fitness.  vars = x, y, z, hit, t, angle, closeness, numClosePairs, num_voxel. */
 int vx3_inspect_formula(const char* base_vxa_xml, const char* vxd_xml_or_null, int which, const double* vars9, double* out);
+/* The same formulas evaluated on the context's device by the evaluator the step kernels use
+ * (VX3_MathTree::eval run on the GPU, Utils/VX3_MathTree.h:50-192; stop condition in the step loop,
+ * VX3_VoxelyzeKernel.cu:162-182; force field in the voxel update, VX3_Voxel.cu:178-184), for n
+ * variable sets of 9 doubles (vars9[9*n]); which: 0 stop condition, 1 fitness, 2/3/4 force field
+ * x/y/z.  out[n]; absent formulas give NaN (0 for an absent force-field component). */
+int vx3_eval_formula(vx3_ctx* ctx, const char* base_vxa_xml, const char* vxd_xml_or_null, int which, const double* vars9, int n,
+                     double* out);
 
 #ifdef __cplusplus
 }

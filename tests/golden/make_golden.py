@@ -87,7 +87,7 @@ def worlds():
 
 
 # The reference's own sample worlds (read from its source tree; the merged VXA text is stored in the fixture).
-REF = os.environ.get("VX_REFERENCE", "/root/reference")
+REF = os.environ.get("VX_REFERENCE", "")   # the reference's project root (required to regenerate the fixtures)
 SAMPLES = {
     "ref_zoo_basic": ("zoo/basic/base.vxa", "zoo/basic/robot.vxd", [1, 300, 1000]),
     "ref_example": ("doc/misc/example.vxa", None, [1, 300, 1000]),
