@@ -153,15 +153,17 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------- workloads
-def make_workload(name, rank=0, n_batch=512, n_collide=64):
+def make_workload(name, rank=0, n_batch=512, n_collide=64, slab_dims=(200, 200, 100)):
     from gpuvoxels_gb300 import synth
     if name == "batch":
         cs = synth.config1_batch(n_batch, seed=1 + 1000 * rank, sim_time=0.5)
         desc = dict(workload="batched plain physics: %d creatures, side U{6..20}, fill U(0.3,0.9), 4 materials E log-uniform "
                     "[1e5,1e7] Pa, nu=0.35, 5 Hz actuation, 0.01 m voxels, gravity+floor, no self-collision" % len(cs))
     elif name == "slab":
-        cs = [synth.slab(200, 200, 100, seed=3 + rank)]
-        desc = dict(workload="single large body: solid 200x200x100 slab (4M voxels), E=1e6, nu=0.35, per-voxel CTE actuation")
+        X, Y, Z = slab_dims
+        cs = [synth.slab(X, Y, Z, seed=3 + rank)]
+        desc = dict(workload=f"single large body: solid {X}x{Y}x{Z} slab ({X * Y * Z} voxels), E=1e6, nu=0.35, "
+                             "per-voxel CTE actuation")
     elif name == "collide":
         cs = synth.config2_batch(n_collide, seed=2 + rank)
         desc = dict(workload="collision-heavy: %d creatures 40^3 fill 0.5, 3 materials incl. E=1e5, self-collision on "
@@ -559,7 +561,7 @@ def run_serve(args):
 def profile_case(args):
     """A short, self-terminating run for ncu: the workload's kernels, one launch each per step."""
     import gpuvoxels_gb300 as g
-    cs, desc = make_workload(args.workload, 0, args.batch, args.collide_sims)
+    cs, desc = make_workload(args.workload, 0, args.batch, args.collide_sims, tuple(int(x) for x in args.slab_dims.split(",")))
     ctx = g.Context(0, int(args.budget_gb * (1 << 30)))
     ctx.set_precision(g.FMA if args.precision == "fma" else g.EXACT)
     ids = ctx.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
@@ -613,6 +615,7 @@ def main():
     ap.add_argument("--collide-steps", type=int, default=2000, help="steps of the collision-heavy block (of 20,000)")
     ap.add_argument("--collide-sims", type=int, default=64, help="creatures of the collision workload for --profile-steps")
     ap.add_argument("--slab-steps", type=int, default=2000, help="steps of the single-body block (of 2,000)")
+    ap.add_argument("--slab-dims", default="200,200,100", help="slab size X,Y,Z for --profile-steps (a smaller case for ncu)")
     ap.add_argument("--no-modes", action="store_true", help="skip the serving, collision and single-body blocks")
     ap.add_argument("--batch", type=int, default=512)
     ap.add_argument("--budget-gb", type=float, default=64.0)

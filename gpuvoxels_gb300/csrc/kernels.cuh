@@ -977,7 +977,7 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
         if (!(ten[0] && ten[1] && ten[2])) {
             float add = 0;
             for (int i = 0; i < 3; i++) if (ten[i]) add += s[i];
-            const float value = poisson_pow(1.0f + add, -m.nu) - 1.0f;
+            const float value = poisson_power(m, 1.0f + add) - 1.0f;
             for (int i = 0; i < 3; i++) if (!ten[i]) s[i] = value;
         }
         S.ps[v] = s[0]; S.ps[nv + v] = s[1]; S.ps[2 * nv + v] = s[2];

@@ -73,7 +73,12 @@ struct VMat {
     double pmPeriod, sigDecay, sigDelay, sigInactive, removeAfter;
     int32_t attachLmat;   // link material of a new link between two voxels of this material (-1: not sticky)
     int32_t pad_vm;
+    // powf(x, -nu) of the host's C library for every float x in [0.5, 2) (index: bits(x) - kPowTabFirst),
+    // the Poisson power of the reference's CPU path; null when nu is 0
+    const float* powtab;
 };
+constexpr uint32_t kPowTabFirst = 0x3F000000u;   // bits of 0.5f
+constexpr uint32_t kPowTabSize = 0x01000000u;    // floats in [0.5, 2)
 
 // VX3 per-voxel signal state (SF_SIGNALS), one block of nv doubles each
 enum SigField {

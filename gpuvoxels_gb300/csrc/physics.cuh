@@ -243,6 +243,17 @@ __device__ __forceinline__ float poisson_pow(float x, float y) {
     return d2f(e);
 }
 
+// The Poisson power of CVX_Voxel::strain (VX_Voxel.cpp:327): pow(float, float), i.e. the C
+// library's powf, which is not correctly rounded (about 6e-4 of its results are the other
+// neighbour of the exact power).  The engine tabulates the host C library's powf(x, -nu)
+// for every float x in [0.5, 2) per Poisson ratio, so the step reads the reference's value
+// itself; other x (strains beyond -50% / +100%) take the series above.
+__device__ __forceinline__ float poisson_power(const VMat& m, float x) {
+    const uint32_t k = fp64i::fbits(x) - kPowTabFirst;
+    if (m.powtab && k < kPowTabSize) return __ldg(m.powtab + k);
+    return poisson_pow(x, -m.nu);
+}
+
 // CVX_Voxel::baseSize(axis) and baseSizeAverage  Voxelyze3/src/old/VX_Voxel.h:91-92
 __device__ __forceinline__ double base_size(const VMat& m, float temp) { return m.nom * f2d(1 + temp * m.cte); }
 __device__ __forceinline__ double base_size_avg(const VMat& m, float temp) {

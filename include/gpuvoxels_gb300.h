@@ -182,9 +182,11 @@ int vx3_set_tuning(vx3_ctx* ctx, int block_links, int block_voxels, int items_li
 /* Elements (links, voxels) a warp claims from the step kernels' work queues at a time: multiples of 32
  * (0 keeps the current value).  No reference counterpart: the reference launches one thread per element. */
 int vx3_set_claim_sizes(vx3_ctx* ctx, int claim_links, int claim_voxels);
-/* Times candidate launch shapes on the given simulations and keeps the fastest: threads per block,
- * elements per work item (the grouping window) and elements a warp claims at a time.  The simulations'
- * device state is copied aside before and put back after, so their results are those of an untuned run.
+/* Searches the launch shape on the given simulations and keeps the fastest found: threads per block
+ * (128, 256), elements per link and per voxel work item (256, 512, 1024: the grouping window) and elements
+ * a warp claims from the link and voxel queues at a time (32, 64, 128), one axis at a time from the
+ * current shape, each candidate timed as the median of three runs.  The simulations' device state is
+ * copied aside before and put back after, so their results are those of an untuned run.
  * No reference counterpart (the reference's launch shapes are fixed, VX3_VoxelyzeKernel.cu:237-359). */
 int vx3_autotune(vx3_ctx* ctx, const vx3_sim_id* ids, int n);
 /* The launch shape in use: out8 = threads per block (links, voxels), elements per work item (links,

@@ -1,8 +1,8 @@
 """The project autotuner (vx3_autotune) and the launch-shape knobs it searches.
 
-* It picks a shape from its candidate set: threads per block 128 or 256,
-  elements per link work item 256 or 1024 (voxel items half that), elements a
-  warp claims from the queues 32, 64 or 128.
+* It picks a shape from its search space: threads per block 128 or 256 (links
+  and voxels alike), elements per link and per voxel work item 256, 512 or
+  1024, elements a warp claims from the link and voxel queues 32, 64 or 128.
 * It leaves the simulations' state as it found it: tuned and untuned runs of
   the same steps are bit-identical, and so are the steps after tuning.
 * Claim sizes and block sizes never change results (the step kernels' work is
@@ -17,7 +17,7 @@ from gpuvoxels_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 BLOCKS = {128, 256}
-ITEMS = {256, 1024}
+ITEMS = {256, 512, 1024}
 CLAIMS = {32, 64, 128}
 
 
@@ -49,8 +49,8 @@ def test_autotune_shape_and_state():
     cs = synth.config1_batch(24, seed=31, sim_time=0.5)
     shape, pos, q, fl = _run(cs, 150, tune=True)
     assert shape["block_links"] in BLOCKS and shape["block_voxels"] == shape["block_links"]
-    assert shape["items_links"] in ITEMS and shape["items_voxels"] == shape["items_links"] // 2
-    assert shape["claim_links"] in CLAIMS and shape["claim_voxels"] == shape["claim_links"]
+    assert shape["items_links"] in ITEMS and shape["items_voxels"] in ITEMS
+    assert shape["claim_links"] in CLAIMS and shape["claim_voxels"] in CLAIMS
     _, pos0, q0, fl0 = _run(cs, 150)
     assert np.array_equal(_bits(pos), _bits(pos0))
     assert np.array_equal(_bits(q), _bits(q0))
