@@ -69,6 +69,11 @@ def measured_peaks():
 FP64_COUNTS = {
     "batch": dict(per_link=684878336 / 1627115, per_voxel=236663360 / 844972,
                   traffic_per_link=(410284544 + 358874112) / 1627115, source="ncu, 512-creature batch, step 205"),
+    # profiles/fp64_counts_collide_slab.md: 8 of the 64 collision creatures and a 100x100x50 slab, step 201
+    "collide": dict(per_link=156123968 / 373621, per_voxel=60842368 / 249183,
+                    traffic_per_link=(111591680 + 71004928) / 373621, source="ncu, 8 collision creatures 40^3, step 201"),
+    "slab": dict(per_link=732160544 / 1480000, per_voxel=117621120 / 500000,
+                 traffic_per_link=(193994496 + 228061696) / 1480000, source="ncu, 100x100x50 slab, step 201"),
 }
 FP64_INSTR_PER_LINK = FP64_COUNTS["batch"]["per_link"]
 FP64_INSTR_PER_VOXEL = FP64_COUNTS["batch"]["per_voxel"]
@@ -177,7 +182,8 @@ def make_workload(name, rank=0, n_batch=512, n_collide=64, slab_dims=(200, 200, 
 
 
 def algorithmic_bytes(ctx, ids):
-    """Compulsory DRAM bytes of one step (the kernels' data model)."""
+    """Compulsory DRAM bytes of one step: k_links reads and writes 284 B per link plus 73 B per
+    endpoint voxel; k_voxels 249 B per voxel plus 52 B per link end (its force and moment slot)."""
     import gpuvoxels_gb300 as g
     link_b = vox_b = 0
     for i in ids:
