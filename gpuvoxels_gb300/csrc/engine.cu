@@ -106,6 +106,33 @@ const float* host_pow_table(float nu) {
     return t;
 }
 
+// The device copy of a powf table on `device` (current), shared by every context of the
+// process on that device: made on first use, read-only afterwards, held until the process
+// exits (64 MiB per Poisson ratio and device, outside the contexts' HBM budgets).
+const float* device_pow_table(int device, float nu, int64_t* h2d_bytes, std::string* err) {
+    static std::mutex mu;
+    static std::map<std::pair<int, uint32_t>, float*> tabs;
+    uint32_t key;
+    memcpy(&key, &nu, 4);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = tabs.find({device, key});
+    if (it != tabs.end()) return it->second;
+    const float* h = host_pow_table(nu);
+    if (!h) { if (err) *err = "host memory for the powf table"; return nullptr; }
+    float* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(float) * dev::kPowTabSize);
+    if (e == cudaSuccess) e = cudaMemcpy(d, h, sizeof(float) * dev::kPowTabSize, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);   // complete before any context's stream reads it
+    if (e != cudaSuccess) {
+        if (d) cudaFree(d);
+        if (err) *err = std::string("powf table: ") + cudaGetErrorString(e);
+        return nullptr;
+    }
+    *h2d_bytes += (int64_t)sizeof(float) * dev::kPowTabSize;
+    tabs[{device, key}] = d;
+    return d;
+}
+
 // First-fit allocator over one device allocation (the HBM budget).
 struct Arena {
     char* base = nullptr;
@@ -191,8 +218,9 @@ public:
     int spill_cap_ = 0;
     static constexpr int kAttachCandPerVoxel = 16;   // attachment candidate pairs kept per voxel and step
     int contact_inline_ = dev::kContactInline;        // contacts in each voxel's own slots (simulations uploaded later)
-    // device copies of the powf tables of the Poisson ratios in use (key: the ratio's bits)
-    std::map<uint32_t, float*> dev_pow_;
+    // the powf tables of the Poisson ratios in use (key: the ratio's bits; the process's
+    // device copies, shared with the other contexts on this device)
+    std::map<uint32_t, const float*> dev_pow_;
     dev::Item* d_items_ = nullptr;
     int cap_items_ = 0;
     double* d_com4_ = nullptr;
@@ -273,7 +301,6 @@ public:
         cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
         cudaFree(d_vox_hist_); cudaFree(d_vox_base_); cudaFree(d_vox_total_); cudaFree(d_vox_perm_); cudaFree(d_batch_slots_);
         cudaFree(arena_base_);
-        for (auto& kv : dev_pow_) cudaFree(kv.second);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
         for (auto& e : evk_) if (e) cudaEventDestroy(e);
@@ -583,12 +610,9 @@ public:
             uint32_t key;
             memcpy(&key, &m.nu, 4);
             if (dev_pow_.count(key)) continue;
-            const float* h = host_pow_table(m.nu);
-            if (!h) { if (err) *err = "host memory for the powf table"; return -5; }
-            float* d = nullptr;
-            CK(cudaMalloc(&d, sizeof(float) * dev::kPowTabSize));
+            const float* d = device_pow_table(device_, m.nu, &h2d_bytes_, err);
+            if (!d) return -5;
             dev_pow_[key] = d;
-            CK(copy_async(d, h, sizeof(float) * dev::kPowTabSize, cudaMemcpyHostToDevice, stream_));
         }
         return 0;
     }

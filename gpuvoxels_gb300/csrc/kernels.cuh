@@ -131,9 +131,11 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         pos2.x -= restLen;
         a1v = D3(0, 0, 0);                  // ToRotationVector of the identity
     } else {
-        angle1 = q_from_angle_to_posx(angle1, pos2, &wide1);
+        // pos2.Length(), used by FromAngleToPosX's general branch and for the axial position
+        const double len = sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z);
+        angle1 = q_from_angle_to_posx(angle1, pos2, len, &wide1);
         angle2 = qmul_x0(angle1, angle2);
-        pos2 = D3(sqrt(pos2.x * pos2.x + pos2.y * pos2.y + pos2.z * pos2.z) - restLen, 0, 0);
+        pos2 = D3(len - restLen, 0, 0);
         a1v = q_to_rotvec<true>(angle1, &acos1);
     }
     const d3 a2v = q_to_rotvec(angle2, &wide2);

@@ -154,8 +154,9 @@ __device__ __forceinline__ q4 q_from_rotvec(const d3& v, bool* wide = nullptr) {
     return Q4(w, tx * s, ty * s, tz * s);
 }
 // Quat3D::FromAngleToPosX  Quat3D.h:145-170; `cur` is returned for a zero vector;
-// *wide = the general (acos, sincos) branch was taken
-__device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r, bool* wide = nullptr) {
+// *wide = the general (acos, sincos) branch was taken.  len = r.Length() (sqrt(x*x + y*y + z*z)),
+// which the caller needs too: the general branch's normalisation takes it from there.
+__device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r, double len, bool* wide = nullptr) {
     if (fp64i::eq0(r.x) && fp64i::eq0(r.y) && fp64i::eq0(r.z)) return cur;
     double yox = r.y / r.x, zox = r.z / r.x;
     if (fp64i::lt(fabs(yox), 1.732e-2) && fp64i::lt(fabs(zox), 1.732e-2)) {   // |yox|, |zox| < 1.732e-2
@@ -163,7 +164,7 @@ __device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r, b
         return Q4(1 + half(-y * y - z * z), 0, y, z);
     }
     if (wide) *wide = true;
-    double l = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+    const double l = len;
     double nx = r.x, ny = r.y, nz = r.z;
     if (fp64i::gt0(l)) { double li = 1.0 / l; nx *= li; ny *= li; nz *= li; }
     double theta = acos(nx);
