@@ -391,6 +391,7 @@ def serve_stream(args, device, budget, n_requests, rates):
         arrivals = list(itertools.accumulate(rng.exponential(1.0 / rate, size=len(reqs))))
         # ---- served arm
         with g.Context(device, budget) as ctx:
+            ctx.set_serving(args.serve_order, args.serve_cap_voxels)
             w = ctx.load_vxa(reqs[0][0].vxa, name="warm")
             ctx.submit(w, 256)
             while ctx.pending():
@@ -418,12 +419,18 @@ def serve_stream(args, device, budget, n_requests, rates):
                 elif k < len(reqs):
                     time.sleep(max(0.0, min(0.01, arrivals[k] - (time.perf_counter() - t0))))
             span = (last - t0) - arrivals[0]
-        # ---- plain arm: the same arrivals, first come first served
-        free_at, plat = 0.0, []
-        for a, sv in zip(arrivals, service):
-            start = max(a, free_at)
-            free_at = start + sv
-            plat.append(free_at - a)
+        # ---- plain arm: the same arrivals, one request at a time in the same order policy
+        free_at, plat, waiting, nxt = 0.0, [], [], 0
+        while nxt < len(reqs) or waiting:
+            if not waiting:
+                free_at = max(free_at, arrivals[nxt])
+            while nxt < len(reqs) and arrivals[nxt] <= free_at:
+                waiting.append(nxt)
+                nxt += 1
+            pick = min(waiting, key=lambda i: (work[i], i)) if args.serve_order == 1 else waiting[0]
+            waiting.remove(pick)
+            free_at += service[pick]
+            plat.append(free_at - arrivals[pick])
         pspan = free_at - arrivals[0]
         served = vsteps / span
         plain = sum(work) / pspan
@@ -435,6 +442,8 @@ def serve_stream(args, device, budget, n_requests, rates):
     return dict(
         requests=len(reqs), voxels_min=min(vs), voxels_max=max(vs), voxel_steps_total=int(sum(work)),
         collide=int(sum(1 for c, _ in reqs if c.meta.get("collide"))), chunk_steps=args.chunk_steps,
+        policy=dict(order="least voxels x horizon first" if args.serve_order == 1 else "first come first served",
+                    max_active_voxels=args.serve_cap_voxels, both_arms=True),
         stream=("Poisson arrivals at each offered rate (seeded); creatures with V log-uniform in [100, 1e5] (fill "
                 "U(0.5, 0.9), 4 materials E log-uniform [1e5, 1e7] Pa), horizons U[1e3, 5e4] steps, 20% with "
                 "self-collision; the same requests at every rate"),
@@ -616,6 +625,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16, help="requests of the serving stream (per offered rate)")
     ap.add_argument("--serve-rates", default="50,200,2000", help="offered request rates (req/s) of the serving stream")
     ap.add_argument("--chunk-steps", type=int, default=64)
+    ap.add_argument("--serve-order", type=int, default=0, help="admission order: 0 first come first served, 1 least work first")
+    ap.add_argument("--serve-cap-voxels", type=int, default=0, help="most voxels in the running batch (0: the HBM budget decides)")
     ap.add_argument("--plain-sample-steps", type=int, default=256,
                     help="steps of each request measured in PLAIN mode for the plain arm of the serving stream")
     ap.add_argument("--collide-steps", type=int, default=2000, help="steps of the collision-heavy block (of 20,000)")

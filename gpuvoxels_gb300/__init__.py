@@ -24,6 +24,7 @@ import numpy as np
 from . import build as _build
 
 PLAIN, BATCHED = 0, 1
+SERVE_FCFS, SERVE_LEAST_WORK = 0, 1
 EXACT, FMA = 0, 1
 SIM_IDLE, SIM_RUNNING, SIM_DONE, SIM_DIVERGED, SIM_ERROR = range(5)
 ERRORS = {-1: "VX3_E_PARSE", -2: "VX3_E_OOM_BUDGET", -3: "VX3_E_DIVERGED", -4: "VX3_E_TIMEOUT", -5: "VX3_E_CUDA",
@@ -37,7 +38,7 @@ EXPORTS = ["vx3_create", "vx3_destroy", "vx3_last_error", "vx3_load_vxa", "vx3_s
            "vx3_inspect_vxa", "vx3_inspect_topology", "vx3_inspect_formula", "vx3_center_of_mass_noalloc",
            "vx3_write_report_multi", "vx3_load_vxa_many", "vx3_record_history", "vx3_inspect_externals", "vx3_get_states",
            "vx3_get_extras", "vx3_get_links", "vx3_transfer_bytes", "vx3_set_claim_sizes", "vx3_get_tuning",
-           "vx3_set_contact_slots", "vx3_eval_formula"]
+           "vx3_set_contact_slots", "vx3_eval_formula", "vx3_set_serving"]
 NOALLOC_MAX_POINTS = 4194304
 E_LIMIT = -8
 
@@ -88,7 +89,7 @@ def library(build_if_missing: bool = True) -> ctypes.CDLL:
         "vx3_get_link_state": (I, [P, I64, P, P, P]), "vx3_write_report": (I, [P, P, I, S, S]),
         "vx3_free_sim": (I, [P, I64]), "vx3_last_timing": (I, [P, P]), "vx3_set_tuning": (I, [P, I, I, I, I, I]),
         "vx3_autotune": (I, [P, P, I]), "vx3_set_claim_sizes": (I, [P, I, I]), "vx3_get_tuning": (I, [P, P]),
-        "vx3_set_contact_slots": (I, [P, I]), "vx3_eval_formula": (I, [P, S, S, I, P, I, P]), "vx3_set_profiling": (I, [P, I]), "vx3_set_precision": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
+        "vx3_set_contact_slots": (I, [P, I]), "vx3_set_serving": (I, [P, I, I64]), "vx3_eval_formula": (I, [P, S, S, I, P, I, P]), "vx3_set_profiling": (I, [P, I]), "vx3_set_precision": (I, [P, I]), "vx3_sim_bytes": (I64, [P, I64]),
         "vx3_bytes_in_use": (ctypes.c_size_t, [P]),
         "vx3_inspect_vxa": (I, [S, S, P, P, ctypes.c_char_p, I]),
         "vx3_inspect_topology": (I, [S, S, P, P, P, P, P, P, P]),
@@ -338,6 +339,11 @@ class Context:
 
     def set_tuning(self, block_links=0, block_voxels=0, items_links=0, items_voxels=0, graph_steps=0):
         self.L.vx3_set_tuning(self.h, block_links, block_voxels, items_links, items_voxels, graph_steps)
+
+    def set_serving(self, order: int = 0, max_active_voxels: int = 0):
+        """Admission policy of poll(): order 0 first come first served, 1 least voxels x horizon first;
+        max_active_voxels caps the running batch (0 = the HBM budget decides)."""
+        self._check(self.L.vx3_set_serving(self.h, order, max_active_voxels))
 
     def set_claim_sizes(self, claim_links=0, claim_voxels=0):
         self._check(self.L.vx3_set_claim_sizes(self.h, claim_links, claim_voxels))

@@ -545,6 +545,11 @@ int vx3_autotune(vx3_ctx* c, const vx3_sim_id* ids, int n) {
     return e ? fail(c, e, err) : VX3_OK;
 }
 
+int vx3_set_serving(vx3_ctx* c, int order, int64_t max_active_voxels) {
+    if (!c) return VX3_E_ARG;
+    return c->eng->set_serving(order, max_active_voxels) ? fail(c, VX3_E_ARG, "order must be 0 or 1, the voxel cap >= 0") : VX3_OK;
+}
+
 int vx3_set_claim_sizes(vx3_ctx* c, int claim_links, int claim_voxels) {
     if (!c || claim_links < 0 || claim_voxels < 0) return VX3_E_ARG;
     return c->eng->set_claims(claim_links, claim_voxels);

@@ -1624,13 +1624,40 @@ public:
     }
     int pending() const override { return (int)(queue_.size() + active_.size()); }
 
+    // Serving policy: the order queued requests are admitted in (first come first served, or
+    // the least work — voxels x horizon steps — first) and the voxels the running batch may
+    // hold (0: as many as the HBM budget allows; the first request is always admitted).
+    int serve_order_ = 0;
+    int64_t serve_max_voxels_ = 0;
+    int set_serving(int order, int64_t max_active_voxels) override {
+        if (order < 0 || order > 1 || max_active_voxels < 0) return -6;
+        serve_order_ = order;
+        serve_max_voxels_ = max_active_voxels;
+        return 0;
+    }
+
     int poll(SimResult* out, int max, int chunk, std::string* err) override {
-        // admit while the HBM budget allows (first come, first served); the uploads of
-        // everything admitted now are finished together
+        // admit while the HBM budget (and the voxel cap) allows, in the policy's order; the
+        // uploads of everything admitted now are finished together
         std::vector<SimRec*> begun, admitted;
+        int64_t active_voxels = 0;
+        for (int64_t id : active_) if (SimRec* a = find(id)) active_voxels += a->w.nv;
+        if (serve_order_ == 1 && queue_.size() > 1) {
+            // least work first; ties keep their arrival order
+            std::stable_sort(queue_.begin(), queue_.end(), [&](int64_t x, int64_t y) {
+                SimRec* a = find(x);
+                SimRec* b = find(y);
+                const double wa = a ? (double)a->w.nv * (double)(a->horizon > 0 ? a->horizon : 1000000) : 0;
+                const double wb = b ? (double)b->w.nv * (double)(b->horizon > 0 ? b->horizon : 1000000) : 0;
+                return wa < wb;
+            });
+        }
         while (!queue_.empty()) {
             SimRec* r = find(queue_.front());
             if (!r) { queue_.pop_front(); continue; }
+            if (serve_max_voxels_ > 0 && !(active_.empty() && admitted.empty()) &&
+                active_voxels + r->w.nv > serve_max_voxels_)
+                break;
             std::string e2;
             const bool fresh = !r->resident;
             int e = fresh ? upload_begin(r, &e2) : 0;
@@ -1641,6 +1668,7 @@ public:
             if (e) { upload_finish(begun, err); *err = e2; return e; }
             if (fresh) begun.push_back(r);
             admitted.push_back(r);
+            active_voxels += r->w.nv;
             queue_.pop_front();
             r->start_s = now_s() - t0_;
             active_.push_back(r->id);

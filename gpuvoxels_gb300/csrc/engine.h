@@ -69,6 +69,9 @@ public:
     // Serving: advance everything admitted by one chunk, admit/retire; returns finished results.
     virtual int poll(SimResult* out, int max, int chunk_steps, std::string* err) = 0;
     virtual int pending() const = 0;
+    // Serving policy: admission order (0 first come first served, 1 least voxels x horizon first)
+    // and the most voxels the running batch may hold (0 = as the HBM budget allows).
+    virtual int set_serving(int order, int64_t max_active_voxels) = 0;
     virtual int result(int64_t id, SimResult* out, std::string* err) = 0;
     virtual int info(int64_t id, int* nv, int* nl, double* dt, double* t, int64_t* steps, int* status) = 0;
     virtual int voxel_state(int64_t id, double* d13, float* f4, int32_t* flags, std::string* err) = 0;

@@ -546,9 +546,61 @@ __device__ __forceinline__ bool maybe_touching(float4 a, float4 b, float env_rad
     return dx * dx + dy * dy + dz * dz <= lim * lim;
 }
 
+// First index of each (oz, oy) row of the radius-5 L1 ball enumerated z-major, then y, then
+// x (the order of the reach masks, world.cpp l1_ball_offsets); rows outside the ball unused.
+struct BallRows {
+    int r[11][11];
+    constexpr BallRows() : r() {
+        int k = 0;
+        for (int z = -5; z <= 5; z++) {
+            const int rz = 5 - (z < 0 ? -z : z);
+            for (int y = -5; y <= 5; y++) {
+                const int ay = y < 0 ? -y : y;
+                r[z + 5][y + 5] = k;
+                if (ay <= rz) k += 2 * (rz - ay) + 1;
+            }
+        }
+    }
+};
+__constant__ const BallRows kBallRowTable{};
+#define kBallRow kBallRowTable.r
+
+// Whether hashed voxel q, found in cell (tx, ty, tz) of the table, is a partner of surface
+// voxel v (float position pv, lattice indices vx, vy, vz) in this step's contact list: q
+// lies in that cell, is not within 5 lattice links of v (nor linked to it by a link made
+// at run time) and overlaps v by the exact test.
+__device__ __forceinline__ bool is_contact(const Sim& S, int v, int q, float4 pv, int vx, int vy, int vz, int tx, int ty, int tz) {
+    const float ic = S.inv_cell;
+    const float4 pq = S.cpos[q];
+    if (q == v || cell_of(pq.x, ic) != tx || cell_of(pq.y, ic) != ty || cell_of(pq.z, ic) != tz || !maybe_touching(pv, pq, S.env_radius))
+        return false;
+    const int nv = S.nv;
+    // lattice exclusion: within 5 links of each other
+    const int ox = S.ijk[q] - vx, oy = S.ijk[nv + q] - vy, oz = S.ijk[2 * nv + q] - vz;
+    const int l1 = abs(ox) + abs(oy) + abs(oz);
+    if (l1 == 1) return false;   // lattice neighbours are always linked to each other
+    if (l1 <= 5) {
+        // index of (ox,oy,oz) in the L1 ball enumerated z-major, then y, then x: the row of
+        // (oz, oy) starts at kBallRow, the row spans ox in [-(5-|oz|-|oy|), 5-|oz|-|oy|]
+        const int k = kBallRow[oz + 5][oy + 5] + ox + (5 - abs(oz) - abs(oy));
+        if ((S.reach[(size_t)v * kReachWords + (k >> 5)] >> (k & 31)) & 1u) return false;
+    }
+    if (S.flags & SF_ATTACH) {
+        // links made at run time join voxels the loaded topology kept apart: voxels linked to
+        // each other do not collide (is_neighbor depth 1, VX3_VoxelyzeKernel.cu:697-700)
+        const uint32_t fv = S.vfl[v];
+        for (int d = 0; d < 6; d++)
+            if ((fv >> d) & 1) {
+                const int l = S.vlink[6 * v + d];
+                if (S.lneg[l] == q || S.lpos[l] == q) return false;
+            }
+    }
+    float f3[3];
+    return pair_force(S, v < q ? v : q, v < q ? q : v, f3);
+}
+
 // Calls fn(q) for every partner q of surface voxel v in this step's contact list, in no
-// particular order: hashed voxels in the 27 cells around v that are not within 5 lattice
-// links of v (nor linked to it by a link made at run time) and overlap it by the exact test.
+// particular order: hashed voxels in the 27 cells around v that pass is_contact.
 template <typename Fn>
 __device__ __forceinline__ void for_each_contact(const Sim& S, int v, int parity, Fn fn) {
     const float4 pv = S.cpos[v];
@@ -565,38 +617,7 @@ __device__ __forceinline__ void for_each_contact(const Sim& S, int v, int parity
                 int guard = 0;
                 while (q >= 0 && guard++ < nv) {
                     const int nq = S.hash_next[q];
-                    const float4 pq = S.cpos[q];
-                    if (q != v && cell_of(pq.x, ic) == tx && cell_of(pq.y, ic) == ty && cell_of(pq.z, ic) == tz &&
-                        maybe_touching(pv, pq, S.env_radius)) {
-                        // lattice exclusion: within 5 links of each other
-                        const int ox = S.ijk[q] - vx, oy = S.ijk[nv + q] - vy, oz = S.ijk[2 * nv + q] - vz;
-                        const int l1 = abs(ox) + abs(oy) + abs(oz);
-                        bool near = false;
-                        if (l1 <= 5) {
-                            // index of (ox,oy,oz) in the L1 ball enumerated z-major, then y, then x
-                            int k = 0;
-                            for (int zz = -5; zz < oz; zz++) { int r = 5 - abs(zz); k += (2 * r * r + 2 * r + 1); }
-                            const int r = 5 - abs(oz);
-                            for (int yy = -r; yy < oy; yy++) k += 2 * (r - abs(yy)) + 1;
-                            k += ox + (r - abs(oy));
-                            near = (S.reach[(size_t)v * kReachWords + (k >> 5)] >> (k & 31)) & 1u;
-                        }
-                        if (!near && (S.flags & SF_ATTACH)) {
-                            // links made at run time join voxels the loaded topology kept apart:
-                            // voxels linked to each other do not collide (is_neighbor depth 1,
-                            // VX3_VoxelyzeKernel.cu:697-700)
-                            const uint32_t fv = S.vfl[v];
-                            for (int d = 0; d < 6; d++)
-                                if ((fv >> d) & 1) {
-                                    const int l = S.vlink[6 * v + d];
-                                    if (S.lneg[l] == q || S.lpos[l] == q) near = true;
-                                }
-                        }
-                        if (!near) {
-                            float f3[3];
-                            if (pair_force(S, v < q ? v : q, v < q ? q : v, f3)) fn(q);
-                        }
-                    }
+                    if (is_contact(S, v, q, pv, vx, vy, vz, tx, ty, tz)) fn(q);
                     q = nq;
                 }
             }

@@ -156,10 +156,33 @@ __device__ __forceinline__ q4 q_from_rotvec(const d3& v, bool* wide = nullptr) {
 // Quat3D::FromAngleToPosX  Quat3D.h:145-170; `cur` is returned for a zero vector;
 // *wide = the general (acos, sincos) branch was taken.  len = r.Length() (sqrt(x*x + y*y + z*z)),
 // which the caller needs too: the general branch's normalisation takes it from there.
+// Whether |RN(n/d)| < T for T = SMALL_ANGLE_RAD (1.732e-2), decided with one multiply
+// where n/d lies outside [T(1 - 2^-20), T(1 + 2^-20)]: 1 (yes), 0 (no), -1 (undecided:
+// near the threshold, or d zero, tiny, huge or not finite; the quotient decides).
+__device__ __forceinline__ int quot_small_band(double n, double d) {
+    const uint64_t ua = fp64i::bits(n) & fp64i::kAbs, ub = fp64i::bits(d) & fp64i::kAbs;
+    const uint32_t eb = (uint32_t)(ub >> 52);
+    if (eb - 64u >= 1918u || ua >= fp64i::kInf) return -1;
+    const double a = fp64i::from_bits(ua), b = fp64i::from_bits(ub);
+    if (fp64i::lt(a, (1.732e-2 * (1.0 - 0x1p-20)) * b)) return 1;
+    if (fp64i::gt(a, (1.732e-2 * (1.0 + 0x1p-20)) * b)) return 0;
+    return -1;
+}
 __device__ __forceinline__ q4 q_from_angle_to_posx(const q4& cur, const d3& r, double len, bool* wide = nullptr) {
     if (fp64i::eq0(r.x) && fp64i::eq0(r.y) && fp64i::eq0(r.z)) return cur;
-    double yox = r.y / r.x, zox = r.z / r.x;
-    if (fp64i::lt(fabs(yox), 1.732e-2) && fp64i::lt(fabs(zox), 1.732e-2)) {   // |yox|, |zox| < 1.732e-2
+    // YoverX, ZoverX within +-SMALL_ANGLE_RAD: the general branch below does not use the
+    // quotients, so they are formed only when the small-angle branch needs them or the
+    // band test cannot decide
+    const int by = quot_small_band(r.y, r.x);
+    const int bz = by == 0 ? 0 : quot_small_band(r.z, r.x);
+    bool small_turn = by == 1 && bz == 1;
+    double yox = 0, zox = 0;
+    if (by != 0 && bz != 0) {
+        yox = r.y / r.x;
+        zox = r.z / r.x;
+        small_turn = fp64i::lt(fabs(yox), 1.732e-2) && fp64i::lt(fabs(zox), 1.732e-2);   // |yox|, |zox| < 1.732e-2
+    }
+    if (small_turn) {
         double y = half(zox), z = -half(yox);
         return Q4(1 + half(-y * y - z * z), 0, y, z);
     }
