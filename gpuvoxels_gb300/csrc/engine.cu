@@ -64,6 +64,22 @@ __global__ void k_eval_formula(const MathTree* m, const double* __restrict__ var
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// One region of a generation's upload: its image at stage + src (img bytes), copied to
+// arena + dst, and the rest of the region (up to total bytes) cleared.  All offsets and
+// sizes are multiples of 256 bytes.
+struct RegionCopy {
+    uint64_t src, dst, img, total;
+};
+// blockIdx.y picks the region, the blocks along x stride over it in 16-byte words.
+__global__ void k_scatter_regions(const char* __restrict__ stage, const RegionCopy* __restrict__ list, char* arena) {
+    const RegionCopy c = list[blockIdx.y];
+    const uint4* src = (const uint4*)(stage + c.src);
+    uint4* dst = (uint4*)(arena + c.dst);
+    const size_t ni = c.img / 16, nt = c.total / 16;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = i < ni ? src[i] : make_uint4(0u, 0u, 0u, 0u);
+}
+
 // Host tables of the C library's powf(x, -nu) for every float x in [0.5, 2), one per Poisson
 // ratio: the reference's CPU path takes the Poisson strain's power from that function
 // (CVX_Voxel::strain, Voxelyze3/src/old/VX_Voxel.cpp:327), whose results are not always the
@@ -284,6 +300,16 @@ public:
     Pinned rb_;
     char* d_gather_ = nullptr;
     size_t cap_gather_ = 0;
+    char* d_stage_ = nullptr;   // a generation's region images on the device (upload_many), when
+    size_t cap_stage_ = 0;      // the arena has no room for them
+    static constexpr size_t kNoStage = ~(size_t)0;
+    size_t stage_off_ = kNoStage, stage_len_ = 0;   // the arena's temporary staging region in use
+    void release_stage() {
+        if (stage_off_ == kNoStage) return;
+        arena_.release(stage_off_, stage_len_);
+        stage_off_ = kNoStage;
+        stage_len_ = 0;
+    }
     static constexpr size_t kPinnedUploadMax = 256u << 20;   // larger regions are copied from pageable memory
 
     ~EngineImpl() override {
@@ -295,6 +321,7 @@ public:
             if (b->done) cudaEventDestroy(b->done);
         }
         cudaFree(d_gather_);
+        cudaFree(d_stage_);
         cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_com4_);
         cudaFree(d_spill_p_); cudaFree(d_spill_f_);
         cudaFree(d_attach_slots_);
@@ -960,7 +987,30 @@ public:
         }
         TraceClock tc;
         tc.mark("upload_many: reserve");
-        if (int e = pinned(&gen_, total, err)) { unreserve_from(0); return e; }
+        // the images, then the list of region copies, in one pinned buffer and one copy to a
+        // device staging buffer; one kernel then places every image and clears the rest of
+        // every region (per-region copies and clears were a thousand small operations)
+        const size_t o_list = align256(total), stage_bytes = o_list + sizeof(RegionCopy) * n;
+        if (int e = pinned(&gen_, stage_bytes, err)) { unreserve_from(0); return e; }
+        // the staging area: a temporary region of the arena (given back once upload_finish has
+        // waited for the copies), else a buffer of the context's own
+        char* stage = nullptr;
+        size_t stage_off = 0;
+        if (stage_off_ == kNoStage && arena_.alloc(stage_bytes, &stage_off)) {
+            stage = arena_base_ + stage_off;
+            stage_off_ = stage_off;
+            stage_len_ = stage_bytes;
+        } else {
+            if (stage_bytes > cap_stage_) {
+                CK(cudaStreamSynchronize(stream_));
+                cudaFree(d_stage_);
+                d_stage_ = nullptr;
+                cap_stage_ = 0;
+                if (cudaMalloc(&d_stage_, stage_bytes) != cudaSuccess) { unreserve_from(0); if (err) *err = "device staging buffer"; return -5; }
+                cap_stage_ = stage_bytes;
+            }
+            stage = d_stage_;
+        }
         tc.mark("upload_many: pinned buffer");
         std::atomic<size_t> next{0};
         auto work = [&]() {
@@ -972,10 +1022,32 @@ public:
         work();
         for (auto& t : pool) t.join();
         tc.mark("upload_many: fill (threads)");
+        RegionCopy* list = (RegionCopy*)(gen_.p + o_list);
+        size_t largest = 0;
         for (size_t i = 0; i < n; i++) {
-            if (int e = upload_copy(rs[i], plans[i], gen_.p + at[i], err)) { unreserve_from(i); return e; }
-            begun->push_back(rs[i]);
+            list[i] = RegionCopy{at[i], plans[i].off, plans[i].o.zero_from, plans[i].L.total};
+            largest = std::max(largest, plans[i].L.total);
         }
+        if (cudaError_t e = copy_async(stage, gen_.p, stage_bytes, cudaMemcpyHostToDevice, stream_)) {
+            unreserve_from(0);
+            cudaStreamSynchronize(stream_);
+            release_stage();
+            if (err) *err = cudaGetErrorString(e);
+            return -5;
+        }
+        const unsigned bx = (unsigned)std::max<size_t>(1, std::min<size_t>(64, largest >> 20));
+        for (size_t k0 = 0; k0 < n; k0 += 65535) {
+            const unsigned ny = (unsigned)std::min<size_t>(65535, n - k0);
+            k_scatter_regions<<<dim3(bx, ny), 256, 0, stream_>>>(stage, (const RegionCopy*)(stage + o_list) + k0, arena_base_);
+        }
+        if (cudaError_t e = cudaGetLastError()) {
+            unreserve_from(0);
+            cudaStreamSynchronize(stream_);
+            release_stage();
+            if (err) *err = cudaGetErrorString(e);
+            return -5;
+        }
+        for (size_t i = 0; i < n; i++) begun->push_back(rs[i]);
         CK(cudaEventRecord(gen_.done, stream_));
         tc.mark("upload_many: copies issued");
         return rc;
@@ -999,7 +1071,10 @@ public:
     // copy, derives the time steps on the host (the reference's float arithmetic) and
     // writes the control blocks, with one synchronisation in all.
     int upload_finish(const std::vector<SimRec*>& rs, std::string* err) {
-        if (rs.empty()) return 0;
+        if (rs.empty()) {
+            if (stage_off_ != kNoStage) { cudaStreamSynchronize(stream_); release_stage(); }
+            return 0;
+        }
         const size_t n = rs.size();
         // pinned image: descriptors, first control blocks, slot list, initial temperatures,
         // every slot's frequency word, the final control blocks
@@ -1052,6 +1127,7 @@ public:
         TraceClock tc;
         CK(cudaStreamSynchronize(stream_));
         tc.mark("upload_finish: wait for copies");
+        release_stage();   // the scatter of the region images has run
         for (size_t k = 0; k < rs.size(); k++) {
             SimRec* r = rs[k];
             const SimWorld& w = r->w;

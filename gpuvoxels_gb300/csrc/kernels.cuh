@@ -1026,15 +1026,19 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
 }
 
 __device__ __forceinline__ double block_sum(double x, double* red) {
-    // fixed-order tree reduction (deterministic)
-    const int tid = threadIdx.x;
-    red[tid] = x;
+    // fixed-order reduction (deterministic): a shuffle tree inside each warp, then the warps'
+    // sums folded in warp order by the first warp (blockDim.x a multiple of 32, at most 1024)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) x = x + __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[wid] = x;
     __syncthreads();
-    for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
-        if (tid < s) red[tid] = red[tid] + red[tid + s];
-        __syncthreads();
+    if (wid == 0) {
+        double y = lane < nw ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) y = y + __shfl_down_sync(0xffffffffu, y, o);
+        if (lane == 0) red[32] = y;
     }
-    const double r = red[0];
+    __syncthreads();
+    const double r = red[32];
     __syncthreads();
     return r;
 }
