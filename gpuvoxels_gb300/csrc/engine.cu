@@ -478,8 +478,6 @@ public:
         t.vm = L->add(sizeof(dev::VMat) * w.vmats.size());
         t.lm = L->add(sizeof(dev::LMat) * std::max<size_t>(1, w.lmats.size()));
         t.ext = L->add(sizeof(dev::Ext) * std::max<size_t>(1, w.desc.externals.size()));
-        for (int k = 0; k < 3; k++) t.pos[k] = L->add(8 * nv);
-        t.q[0] = L->add(8 * nv);
         t.vfl = L->add(4 * nv);
         t.vmat = L->add(nv);
         t.vext = L->add(4 * nv);
@@ -507,6 +505,10 @@ public:
         if (int nt = target_count(w)) t.targets = L->add(4 * (size_t)nt);
         if (d.secondary_experiment) t.init_pos = L->add(8 * 3 * nv);
         t.zero_from = L->total;
+        // the initial positions (lattice index x voxel size) and orientations (identity) are
+        // written on the device at upload (k_init_temp), so they are not copied
+        for (int k = 0; k < 3; k++) t.pos[k] = L->add(8 * nv);
+        t.q[0] = L->add(8 * nv);
         for (int k = 0; k < 3; k++) t.mom[k] = L->add(8 * nv);
         for (int k = 1; k < 4; k++) t.q[k] = L->add(8 * nv);
         for (int k = 0; k < 3; k++) t.am[k] = L->add(8 * nv);
@@ -747,8 +749,6 @@ public:
                 x.rq[0] = qw; x.rq[1] = tx * s; x.rq[2] = ty * s; x.rq[3] = tz * s;
             } else { x.rq[0] = 1; x.rq[1] = x.rq[2] = x.rq[3] = 0; }
         }
-        double* px = (double*)P(o.pos[0]); double* py = (double*)P(o.pos[1]); double* pz = (double*)P(o.pos[2]);
-        double* qw = (double*)P(o.q[0]);
         uint32_t* vfl = (uint32_t*)P(o.vfl);
         uint8_t* vmat = (uint8_t*)P(o.vmat);
         int32_t* vext = (int32_t*)P(o.vext);
@@ -757,8 +757,6 @@ public:
         for (size_t i = 0; i < nv; i++) {
             int mi = w.desc.voxels[4 * i + 3];
             double nom = w.vmats[mi].nom;
-            px[i] = w.desc.voxels[4 * i] * nom; py[i] = w.desc.voxels[4 * i + 1] * nom; pz[i] = w.desc.voxels[4 * i + 2] * nom;
-            qw[i] = 1.0;
             uint32_t f = dev::VF_STATIC;
             for (int d = 0; d < 6; d++) if (w.vox_links[i * 6 + d] >= 0) f |= 1u << d;
             if (w.vox_interior[i]) f |= dev::VF_INTERIOR;
@@ -818,7 +816,10 @@ public:
         if (dd.secondary_experiment) {
             flags |= dev::SF_REMOVE;
             double* ip = (double*)P(o.init_pos);
-            for (size_t i = 0; i < nv; i++) { ip[i] = px[i]; ip[nv + i] = py[i]; ip[2 * nv + i] = pz[i]; }
+            for (size_t i = 0; i < nv; i++) {
+                const double nom = w.vmats[w.desc.voxels[4 * i + 3]].nom;
+                ip[i] = w.desc.voxels[4 * i] * nom; ip[nv + i] = w.desc.voxels[4 * i + 1] * nom; ip[2 * nv + i] = w.desc.voxels[4 * i + 2] * nom;
+            }
         }
         for (auto& pm : dd.mats) if (pm.fixed) flags |= dev::SF_FIXEDMAT;
         double max_bsa = 0;
@@ -1082,14 +1083,18 @@ public:
         const size_t o_sim = 0, o_ctl0 = al(o_sim + sizeof(dev::Sim) * n), o_slot = al(o_ctl0 + sizeof(dev::Ctl) * n);
         const size_t o_init = al(o_slot + 4 * n), o_bits = al(o_init + 4 * n), o_ctl = al(o_bits + 4 * (size_t)cap_slots_);
         const size_t total = al(o_ctl + sizeof(dev::Ctl) * n);
+        TraceClock tf;
         if (int e = pinned(&rb_, total, err)) return e;
+        tf.mark("upload_finish: pinned buffer");
         if (total > cap_gather_) {
             CK(cudaStreamSynchronize(stream_));
+            tf.mark("upload_finish: sync (gather)");
             cudaFree(d_gather_);
             d_gather_ = nullptr;
             cap_gather_ = 0;
             CK(cudaMalloc(&d_gather_, total));
             cap_gather_ = total;
+            tf.mark("upload_finish: gather buffer");
         }
         char* h = rb_.p;
         dev::Sim* sim_img = (dev::Sim*)(h + o_sim);
@@ -1114,6 +1119,7 @@ public:
         const float* d_init = (const float*)(d_gather_ + o_init);
         // first actuation temperature (t = 0), then the stable step from it, then the collision hash
         auto blocks = [&](int elems) { return std::max(1, std::min(4 * sm_count_, (elems + 255) / 256) / (int)std::min<size_t>(n, 64)); };
+        tf.mark("upload_finish: descriptors");
         ks_.init_temp(blocks(max_nv), stream_, d_sims_, d_slots, d_init, (int)n);
         CK(cudaGetLastError());
         ks_.dt(blocks(max_nl), stream_, d_sims_, d_ctl_, d_slots, (int)n);
@@ -1124,6 +1130,7 @@ public:
         dev::Ctl* ctl_img = (dev::Ctl*)(h + o_ctl);
         CK(copy2d_async(bits_all, sizeof(uint32_t), &d_ctl_[0].maxf2_bits, sizeof(dev::Ctl), sizeof(uint32_t), cap_slots_,
                              cudaMemcpyDeviceToHost, stream_));
+        tf.mark("upload_finish: set-up launches");
         TraceClock tc;
         CK(cudaStreamSynchronize(stream_));
         tc.mark("upload_finish: wait for copies");

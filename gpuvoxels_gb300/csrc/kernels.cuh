@@ -1380,13 +1380,22 @@ __global__ void k_dt(const Sim* __restrict__ sims, Ctl* ctl, const int* __restri
     if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(&ctl[sim].maxf2_bits, __float_as_uint(best));
 }
 
+// Set-up of newly uploaded simulations: initial positions and orientations, and the first
+// actuation temperature.
 __global__ void k_init_temp(const Sim* __restrict__ sims, const int* __restrict__ slots, const float* __restrict__ initials, int n) {
     if ((int)blockIdx.y >= n) return;
     const Sim& S = sims[slots[blockIdx.y]];
     const float initial = initials[blockIdx.y];
     const float two_pi = 2 * 3.1415926f;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < S.nv; v += gridDim.x * blockDim.x) {
+    const int nv = S.nv;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
         const VMat& m = S.vm[S.vmat[v]];
+        // the lattice position and the identity orientation (CVoxelyze::addVoxel places a voxel
+        // at its index times the voxel size, Voxelyze3/src/old/Voxelyze.cpp:439-470)
+        S.px[v] = (double)S.ijk[v] * m.nom;
+        S.py[v] = (double)S.ijk[nv + v] * m.nom;
+        S.pz[v] = (double)S.ijk[2 * nv + v] * m.nom;
+        S.qw[v] = 1.0;
         if ((S.flags & SF_VARY) && !fp64i::gt(m.thermalOn, 0.0) && !(m.vx3 & VM_FIXED)) {
             double T = S.temp_amp * sin((double)two_pi * (0.0 / S.temp_period + S.phase[v]));
             if (!(S.flags & SF_EXPAND) && T > 0) T = 0;

@@ -163,3 +163,37 @@ def test_report_matches_worker_format(ctx, tmp_path):
     finally:
         for i in ids:
             ctx.free(i)
+
+
+def _serve_all(order, cap, creatures, horizons, chunk=32):
+    with g.Context(0, 2 << 30) as c:
+        c.set_serving(order, cap)
+        ids = [c.load_vxa(cr.vxa, name=f"s{i}") for i, cr in enumerate(creatures)]
+        for i, h in zip(ids, horizons):
+            c.submit(i, h)
+        finished = []
+        while c.pending():
+            finished += c.poll(chunk_steps=chunk)
+        by_sim = {ids.index(r.id): r for r in finished}
+        order_done = [ids.index(r.id) for r in finished]
+        return by_sim, order_done
+
+
+def test_serving_policies_change_order_not_results():
+    """Least-work-first admission under a voxel cap finishes the small jobs first; every
+    simulation's result is bit-identical to first-come-first-served admission."""
+    cs = sorted(synth.config1_batch(6, seed=41, sim_time=10.0), key=lambda c: c.num_voxel)[::-1]
+    horizons = [600, 500, 400, 300, 200, 100]    # the larger creatures run longer: work order = arrival order reversed
+    cap = max(c.num_voxel for c in cs) + min(c.num_voxel for c in cs)   # about two at a time
+    fcfs, _ = _serve_all(g.SERVE_FCFS, 0, cs, horizons)
+    lw, done = _serve_all(g.SERVE_LEAST_WORK, cap, cs, horizons)
+    work = [c.num_voxel * h for c, h in zip(cs, horizons)]
+    assert done[0] == int(np.argmin(work))
+    for k in range(len(cs)):
+        a, b = fcfs[k], lw[k]
+        assert a.steps == b.steps == horizons[k]
+        assert list(a.current_center_of_mass) == list(b.current_center_of_mass)
+        assert a.total_distance_of_all_voxels == b.total_distance_of_all_voxels
+    with g.Context(0, 1 << 30) as c:
+        with pytest.raises(g.VX3Error):
+            c.set_serving(2, 0)
