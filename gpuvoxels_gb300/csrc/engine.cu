@@ -64,6 +64,39 @@ __global__ void k_eval_formula(const MathTree* m, const double* __restrict__ var
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Pinned host buffers outlive the contexts that used them: a destroyed context hands its
+// staging buffers to this cache and the next context takes them from it, so a process that
+// creates contexts again and again pins host memory once (up to kPinnedCacheMax bytes kept).
+struct PinnedCache {
+    std::mutex mu;
+    std::multimap<size_t, char*> free_;   // capacity -> buffer
+    size_t bytes = 0;
+    static constexpr size_t kPinnedCacheMax = 2ull << 30;
+    // the smallest cached buffer of at least `need` bytes, or null
+    char* take(size_t need, size_t* cap) {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = free_.lower_bound(need);
+        if (it == free_.end()) return nullptr;
+        char* p = it->second;
+        *cap = it->first;
+        bytes -= it->first;
+        free_.erase(it);
+        return p;
+    }
+    void give(char* p, size_t cap) {
+        if (!p) return;
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            if (bytes + cap <= kPinnedCacheMax) { free_.emplace(cap, p); bytes += cap; return; }
+        }
+        cudaFreeHost(p);
+    }
+};
+PinnedCache& pinned_cache() {
+    static PinnedCache* c = new PinnedCache();   // never destroyed: buffers stay pinned until exit
+    return *c;
+}
+
 // One region of a generation's upload: its image at stage + src (img bytes), copied to
 // arena + dst, and the rest of the region (up to total bytes) cleared.  All offsets and
 // sizes are multiples of 256 bytes.
@@ -264,6 +297,7 @@ public:
     std::vector<int> batch_slots_;
     int n_link_items_ = 0, n_contact_items_ = 0, n_vox_items_ = 0;
     bool any_collide_ = false;
+    bool any_watch_ = false;   // some simulation of the batch takes its contacts from watch lists
     bool any_signals_ = false;
     // batch-wide grouping of links by key (k_bin_hist / k_bin_scan / k_bin_scatter)
     int* d_link_hist_ = nullptr;
@@ -300,6 +334,7 @@ public:
     Pinned rb_;
     char* d_gather_ = nullptr;
     size_t cap_gather_ = 0;
+    static constexpr size_t kGatherInitial = 16u << 20;
     char* d_stage_ = nullptr;   // a generation's region images on the device (upload_many), when
     size_t cap_stage_ = 0;      // the arena has no room for them
     static constexpr size_t kNoStage = ~(size_t)0;
@@ -317,7 +352,7 @@ public:
         cudaSetDevice(device_);
         if (stream_) cudaStreamSynchronize(stream_);
         for (Pinned* b : {&up_[0], &up_[1], &rb_, &gen_}) {
-            if (b->p) cudaFreeHost(b->p);
+            pinned_cache().give(b->p, b->cap);
             if (b->done) cudaEventDestroy(b->done);
         }
         cudaFree(d_gather_);
@@ -358,8 +393,39 @@ public:
         CK(cudaMalloc(&d_spill_p_, sizeof(int32_t) * (size_t)spill_cap_));
         CK(cudaMalloc(&d_spill_f_, 3 * sizeof(float) * (size_t)spill_cap_));
         CK(cudaMalloc(&d_com4_, 4 * sizeof(double)));
+        // device scratch for the per-call tables (slot lists, descriptors, read-back packing):
+        // sized for a few thousand simulations up front, so that calls rarely allocate
+        CK(cudaMalloc(&d_gather_, kGatherInitial));
+        cap_gather_ = kGatherInitial;
         for (Pinned* b : {&up_[0], &up_[1], &rb_, &gen_}) CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+        if (int e = reserve_tables(err)) return e;
         return grow_slots(64, err);
+    }
+
+    // The step's work tables sized up front for batches of up to 4M links, 2M voxels and
+    // 32k work items (about 60 MB), so that running a batch allocates nothing: an allocation
+    // right after a context's first pinned host buffer measured several ms on this machine.
+    int reserve_tables(std::string* err) {
+        cap_bins_ = cap_vbins_ = (size_t)32768 * dev::kOrderKeysBins;
+        cap_perm_ = 4u << 20;
+        cap_vperm_ = 2u << 20;
+        cap_items_ = 65536;
+        cap_batch_ = 16384;
+        cap_attach_ = 1024;
+        CK(cudaMalloc(&d_link_hist_, sizeof(int) * cap_bins_));
+        CK(cudaMalloc(&d_link_base_, sizeof(int) * cap_bins_));
+        CK(cudaMalloc(&d_link_total_, sizeof(int)));
+        CK(cudaMemset(d_link_total_, 0, sizeof(int)));
+        CK(cudaMalloc(&d_link_perm_, sizeof(int2) * cap_perm_));
+        CK(cudaMalloc(&d_vox_hist_, sizeof(int) * cap_vbins_));
+        CK(cudaMalloc(&d_vox_base_, sizeof(int) * cap_vbins_));
+        CK(cudaMalloc(&d_vox_total_, sizeof(int)));
+        CK(cudaMemset(d_vox_total_, 0, sizeof(int)));
+        CK(cudaMalloc(&d_vox_perm_, sizeof(int2) * cap_vperm_));
+        CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
+        CK(cudaMalloc(&d_batch_slots_, sizeof(int) * cap_batch_));
+        CK(cudaMalloc(&d_attach_slots_, sizeof(int) * cap_attach_));
+        return 0;
     }
 
     // A pinned buffer of at least `bytes`, once its previous copy has finished.
@@ -387,11 +453,13 @@ public:
     int pinned(Pinned* b, size_t bytes, std::string* err) {
         CK(cudaEventSynchronize(b->done));
         if (b->cap >= bytes) return 0;
-        if (b->p) CK(cudaFreeHost(b->p));
+        pinned_cache().give(b->p, b->cap);
         b->p = nullptr;
         b->cap = 0;
-        const size_t cap = std::max<size_t>(bytes, 16u << 20);
-        CK(cudaHostAlloc((void**)&b->p, cap, cudaHostAllocDefault));
+        size_t cap = 0;
+        if (char* p = pinned_cache().take(bytes, &cap)) { b->p = p; b->cap = cap; return 0; }
+        cap = std::max<size_t>(bytes, 16u << 20);
+        CK(cudaHostAlloc((void**)&b->p, cap, cudaHostAllocPortable));
         b->cap = cap;
         return 0;
     }
@@ -451,6 +519,12 @@ public:
     }
     static bool dynamic_surface(const SimDesc& d) { return d.enable_detach || removes_materials(d) || attaches(d); }
     static int contact_list_size(const SimWorld& w) { return dynamic_surface(w.desc) ? w.nv : w.surface_count; }
+    // Contacts from watch lists regenerated as the reference does (collisions on, a surface that
+    // does not change during the run); kWatchPerVoxel partners per surface voxel on average fit
+    // (the reference's lists hold about 7 on a 40^3 creature at fill 0.5), more fall back to the
+    // per-step hash search until the next regeneration
+    static bool watches(const SimDesc& d) { return d.collisions && !dynamic_surface(d); }
+    static constexpr int kWatchPerVoxel = 32;
     // VX3 attachment needs the contact pass to find touching pairs; links made at run time
     // take slots nl .. 3*nv-1 (every voxel has six link directions)
     static bool attaches(const SimDesc& d) { return d.enable_attach && d.collisions; }
@@ -464,6 +538,7 @@ public:
     struct Offs {
         size_t vm, lm, ext, pos[3], mom[3], q[4], am[3], temp, ps, vfl, vmat, vext, phase, sf, sm, ss;
         size_t lneg, lpos, lax, lmt, lst, lsf, lfl, surf, ijk, reach, ccount, cforce, cspill, hhead, hnext, cpos, cilia, ffield;
+        size_t watch, woff, wlist;
         size_t shift, sig, vlink, targets, init_pos, lnew, cand, cpart, acond;
         size_t zero_from;   // everything from here on starts as zeros
         int hash_size;
@@ -525,6 +600,12 @@ public:
             t.cspill = L->add(4 * nv);
             t.hnext = L->add(4 * nv);
             t.cpos = L->add(16 * nv);
+            if (watches(d)) {
+                const size_t ns = std::max(1, contact_list_size(w));
+                t.watch = L->add(16 * nv);
+                t.woff = L->add(4 * (ns + 1));
+                t.wlist = L->add(4 * (size_t)kWatchPerVoxel * ns);
+            }
         }
         if (d.enable_signals) t.sig = L->add(8 * dev::SG_FIELDS * nv);
         if (attaches(d)) {
@@ -779,6 +860,7 @@ public:
         int flags = 0;
         if (w.desc.floor) flags |= dev::SF_FLOOR;
         if (w.desc.collisions) flags |= dev::SF_COLLIDE;
+        if (watches(w.desc)) flags |= dev::SF_WATCH;
         if (w.desc.vary_temp && w.desc.temp_period > 0) flags |= dev::SF_VARY;
         if (w.desc.enable_expansion) flags |= dev::SF_EXPAND;
         if (w.desc.enable_cilia) {
@@ -860,6 +942,19 @@ public:
             S.ccount = (int32_t*)D(o.ccount); S.cforce = (float*)D(o.cforce); S.cspill = (int32_t*)D(o.cspill);
             S.spill_p = d_spill_p_; S.spill_f = d_spill_f_; S.spill_used = d_tickets_ + kSpillTicket; S.spill_cap = spill_cap_;
             S.contact_inline = contact_inline_;
+            if (watches(dd)) {
+                // the reference's radii (CVoxelyze::updateCollisions, Voxelyze.cpp:673-675), in float
+                const float watchVx = 2 * dd.bounding_radius + dd.watch_distance;
+                const float watchMm = (float)(dd.vox_size * watchVx);
+                const float recalc = (float)(dd.vox_size * dd.watch_distance / 2);
+                S.watch = (float4*)D(o.watch);
+                S.woff = (int32_t*)D(o.woff);
+                S.wlist = (int32_t*)D(o.wlist);
+                S.wcap = kWatchPerVoxel * std::max(1, contact_list_size(w));
+                S.watch_r2 = watchMm * watchMm;
+                S.recalc2 = recalc * recalc;
+                S.wcells = (int)std::floor(1.03 * watchMm / S.cell_size) + 1;
+            }
             S.hash_head = (int32_t*)D(o.hhead); S.hash_next = (int32_t*)D(o.hnext);
             S.cpos = (float4*)D(o.cpos);
             S.inv_cell = (float)(1.0 / S.cell_size);
@@ -895,6 +990,7 @@ public:
         // currentCenterOfMass starts as the initial one (VX3_SimulationManager.cu:54-55)
         for (int k = 0; k < 3; k++) c.com[k] = c.init_com[k] = r->init_com[k];
         c.n_links = w.nl;
+        c.col_stale = 1;   // the first step regenerates the watch lists (the reference's nearbyStale)
         r->pending_ctl = c;
     }
 
@@ -1189,7 +1285,7 @@ public:
         std::vector<dev::Item> items;
         std::vector<int> attach_slots;
         n_link_items_ = n_contact_items_ = n_vox_items_ = 0;
-        any_collide_ = any_signals_ = false;
+        any_collide_ = any_signals_ = any_watch_ = false;
         for (int s : slots) {
             SimRec* r = slot_owner_[s];
             const int nl = link_capacity(r->w);
@@ -1225,6 +1321,7 @@ public:
             const int ns = contact_list_size(r->w);
             if (!r->w.desc.collisions || ns == 0) continue;
             any_collide_ = true;
+            if (watches(r->w.desc)) any_watch_ = true;
             const int chunk = 128;
             for (int b = 0; b < ns; b += chunk) items.push_back({s, b, std::min(ns, b + chunk), 0});
         }
@@ -1306,7 +1403,7 @@ public:
 
     // One step of the batch; returns the number of kernels it launched.
     int launch_step(cudaStream_t st, bool prof) {
-        int launched = 3 + (any_collide_ ? 1 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
+        int launched = 3 + (any_collide_ ? 1 : 0) + (any_watch_ ? 3 : 0) + (any_signals_ ? 1 : 0) + (n_attach_ ? 1 : 0);
         const dev::Item* li = d_items_;
         const dev::Item* ci = d_items_ + n_link_items_;
         const dev::Item* vi = d_items_ + n_link_items_ + n_contact_items_;
@@ -1336,6 +1433,7 @@ public:
         ks_.links(grid_chunks(batch_links_, bl, 0), bl, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
                   (int)cap_perm_, cap_slots_, d_tickets_, claim_links_);
         if (prof) cudaEventRecord(evk_[1], st);
+        if (any_watch_) ks_.watch(grid_for(n_contact_items_, 128), st, d_sims_, d_ctl_, ci, n_contact_items_, d_batch_slots_, n_batch_);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
@@ -1943,26 +2041,41 @@ public:
         const size_t b_pos = 24 * (size_t)total, b_q = 32 * (size_t)total, b_fl = (size_t)total;
         const size_t b_idx = 4 * (size_t)n + 8 * (size_t)n;
         const size_t need = b_pos + b_q + b_fl + 16 + b_idx + 16;
+        // the packing area: the context's scratch, or for large read-backs a temporary region
+        // of the arena (given back below, after the copy has finished), else a larger scratch
+        char* dg = d_gather_;
+        size_t tmp_off = 0;
+        bool tmp = false;
         if (need > cap_gather_) {
-            CK(cudaStreamSynchronize(stream_));
-            cudaFree(d_gather_);
-            d_gather_ = nullptr;
-            cap_gather_ = 0;
-            CK(cudaMalloc(&d_gather_, need));
-            cap_gather_ = need;
+            if (arena_.alloc(need, &tmp_off)) {
+                tmp = true;
+                dg = arena_base_ + tmp_off;
+            } else {
+                CK(cudaStreamSynchronize(stream_));
+                cudaFree(d_gather_);
+                d_gather_ = nullptr;
+                cap_gather_ = 0;
+                CK(cudaMalloc(&d_gather_, need));
+                cap_gather_ = need;
+                dg = d_gather_;
+            }
         }
+        struct ArenaTemp {   // gives the temporary region back on every way out
+            EngineImpl* e; bool on; size_t off, n;
+            ~ArenaTemp() { if (on) { cudaStreamSynchronize(e->stream_); e->arena_.release(off, n); } }
+        } arena_temp{this, tmp, tmp_off, need};
         if (int e = pinned(&rb_, b_idx, err)) return e;
         // the index tables go through the pinned buffer
         const size_t o_idx = (b_pos + b_q + b_fl + 15) & ~(size_t)15;
         char* h = rb_.p;
         memcpy(h, offs.data(), 8 * (size_t)n);
         memcpy(h + 8 * (size_t)n, slots.data(), 4 * (size_t)n);
-        CK(copy_async(d_gather_ + o_idx, h, b_idx, cudaMemcpyHostToDevice, stream_));
-        double* dpos = (double*)d_gather_;
-        double* dq = (double*)(d_gather_ + b_pos);
-        uint8_t* dfl = (uint8_t*)(d_gather_ + b_pos + b_q);
-        const int64_t* doff = (const int64_t*)(d_gather_ + o_idx);
-        const int* dslot = (const int*)(d_gather_ + o_idx + 8 * (size_t)n);
+        CK(copy_async(dg + o_idx, h, b_idx, cudaMemcpyHostToDevice, stream_));
+        double* dpos = (double*)dg;
+        double* dq = (double*)(dg + b_pos);
+        uint8_t* dfl = (uint8_t*)(dg + b_pos + b_q);
+        const int64_t* doff = (const int64_t*)(dg + o_idx);
+        const int* dslot = (const int*)(dg + o_idx + 8 * (size_t)n);
         for (int k0 = 0; k0 < n; k0 += 65535)
             ks_.gather(stream_, d_sims_, dslot + k0, doff + k0, std::min(65535, n - k0), dpos, dq, dfl);
         CK(cudaGetLastError());
@@ -1970,7 +2083,9 @@ public:
         if (gen_.p && gen_.cap >= b_all) {
             // the generation upload buffer is large enough: one copy into pinned memory, then
             // host threads copy into the caller's arrays (and take their first-touch faults)
+            TraceClock tg;
             if (int e = pinned(&gen_, b_all, err)) return e;   // waits for the buffer's last use
+            tg.mark("gather: pinned buffer");
             char* hs = gen_.p;
             if (pos3 && q4 && flags) {
                 CK(copy_async(hs, dpos, b_all, cudaMemcpyDeviceToHost, stream_));
@@ -1981,6 +2096,7 @@ public:
             }
             CK(cudaEventRecord(gen_.done, stream_));
             CK(cudaEventSynchronize(gen_.done));
+            tg.mark("gather: kernel and copy");
             struct Piece { char* dst; const char* src; size_t n; };
             std::vector<Piece> pieces;
             auto cut = [&](void* dst, const char* src, size_t n) {
@@ -2000,6 +2116,7 @@ public:
             for (int t = 1; t < nt; t++) pool.emplace_back(work);
             work();
             for (auto& t : pool) t.join();
+            tg.mark("gather: host copies");
             return 0;
         }
         // straight into the caller's buffers: no pinned buffer grown to the size of a whole

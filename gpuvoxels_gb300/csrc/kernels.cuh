@@ -632,7 +632,27 @@ __device__ __forceinline__ void for_each_contact(const Sim& S, int v, int parity
 // limit: up to S.contact_inline (at most kContactInline) contacts go to the
 // voxel's own slots; a voxel with more takes a run of records of the spill pool, fills it with its
 // partners in a second pass over the hash and sorts them there.
-__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
+// Calls fn(q) for every partner q of voxel v (surface index si) on its watch list that
+// overlaps it this step, in increasing q: the reference's collision list of the last
+// regeneration (sorted), each pair's float envelope test first, then the exact test.
+template <typename Fn>
+__device__ __forceinline__ void for_each_watch_contact(const Sim& S, int v, int si, Fn fn) {
+    const float4 pv = S.cpos[v];
+    const int e = S.woff[si + 1];
+    for (int k = S.woff[si]; k < e; k++) {
+        const int q = S.wlist[k];
+        if (!maybe_touching(pv, S.cpos[q], S.env_radius)) continue;
+        float f3[3];
+        if (pair_force(S, v < q ? v : q, v < q ? q : v, f3)) fn(q);
+    }
+}
+
+__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c, int si = -1) {
+    const bool watch = si >= 0;
+    auto enumerate = [&](auto fn) {
+        if (watch) for_each_watch_contact(S, v, si, fn);
+        else for_each_contact(S, v, parity, fn);
+    };
     if (S.flags & SF_DYNSURF) {
         // the surface set changes during the run: every voxel is listed, interior and
         // removed ones have no contacts
@@ -643,7 +663,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
     const int cap = min(max(S.contact_inline, 1), kContactInline);
     int partners[kContactInline] = {};
     int np = 0, ntot = 0;
-    for_each_contact(S, v, parity, [&](int q) {
+    enumerate([&](int q) {
         ntot++;
         if (np == cap) {
             if (q > partners[cap - 1]) return;
@@ -665,7 +685,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
         }
         sp = S.spill_p + off;
         int k = 0;
-        for_each_contact(S, v, parity, [&](int q) { if (k < ntot) sp[k++] = q; });
+        enumerate([&](int q) { if (k < ntot) sp[k++] = q; });
         for (int i = 1; i < k; i++) {   // insertion sort by partner index (runs are short)
             const int q = sp[i];
             int j = i;
@@ -720,6 +740,142 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
     }
 }
 
+// ---------------------------------------------------------------- watch lists
+// The reference regenerates its collision list (CVoxelyze::regenerateCollisions,
+// Voxelyze3/src/old/Voxelyze.cpp:726-751) when a surface voxel has moved more than half
+// the watch distance since the last regeneration (updateCollisions, :671-711): the list
+// holds every pair of surface voxels not within 5 links of each other whose centres lie
+// within the watch radius, (2 boundingRadius + watchDistance) voxel sizes, and each step
+// sums the forces of the pairs on it.  SF_WATCH simulations keep the same lists: per
+// surface voxel its partners in increasing order, found through the spatial hash (cells on
+// each side enough to cover the radius), in three passes (count, offsets, fill) that run
+// only in the steps that regenerate.
+
+// Calls fn(q) for every partner q of surface voxel v on its regenerated watch list, in no
+// particular order; the exact test is the reference's: squared centre distance (double)
+// not above the squared watch radius (float).
+template <typename Fn>
+__device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int parity, Fn fn) {
+    const float4 pv = S.cpos[v];
+    const float ic = S.inv_cell;
+    const int cx = cell_of(pv.x, ic), cy = cell_of(pv.y, ic), cz = cell_of(pv.z, ic);
+    const int nv = S.nv;
+    const int vx = S.ijk[v], vy = S.ijk[nv + v], vz = S.ijk[2 * nv + v];
+    const int* head = S.hash_head + (size_t)parity * S.hash_size;
+    const double wr2 = (double)S.watch_r2;
+    const float lim = sqrtf(S.watch_r2) * 1.02f + 2.4e-7f * (fabsf(pv.x) + fabsf(pv.y) + fabsf(pv.z)) * 2.0f;
+    const int R = S.wcells;
+    const double ax = S.px[v], ay = S.py[v], az = S.pz[v];
+    for (int dz = -R; dz <= R; dz++)
+        for (int dy = -R; dy <= R; dy++)
+            for (int dx = -R; dx <= R; dx++) {
+                const int tx = cx + dx, ty = cy + dy, tz = cz + dz;
+                int q = head[cell_hash(tx, ty, tz, S.hash_size - 1)];
+                int guard = 0;
+                while (q >= 0 && guard++ < nv) {
+                    const int nq = S.hash_next[q];
+                    const float4 pq = S.cpos[q];
+                    const float fx = pq.x - pv.x, fy = pq.y - pv.y, fz = pq.z - pv.z;
+                    if (q != v && cell_of(pq.x, ic) == tx && cell_of(pq.y, ic) == ty && cell_of(pq.z, ic) == tz &&
+                        fx * fx + fy * fy + fz * fz <= lim * lim) {
+                        const int ox = S.ijk[q] - vx, oy = S.ijk[nv + q] - vy, oz = S.ijk[2 * nv + q] - vz;
+                        const int l1 = abs(ox) + abs(oy) + abs(oz);
+                        bool near = l1 == 1;   // lattice neighbours are always linked to each other
+                        if (!near && l1 <= 5) {
+                            const int k = kBallRow[oz + 5][oy + 5] + ox + (5 - abs(oz) - abs(oy));
+                            near = (S.reach[(size_t)v * kReachWords + (k >> 5)] >> (k & 31)) & 1u;
+                        }
+                        if (!near) {
+                            const double ex = ax - S.px[q], ey = ay - S.py[q], ez = az - S.pz[q];
+                            if (!(ex * ex + ey * ey + ez * ez > wr2)) fn(q);
+                        }
+                    }
+                    q = nq;
+                }
+            }
+}
+
+// Pass 1: every surface voxel of a regenerating simulation counts its partners (into
+// woff[si + 1]) and records its position as the regeneration's (lastColWatchPosition).
+__global__ void __launch_bounds__(128) k_watch_count(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                     int n_items) {
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const Item w = items[it];
+        const Ctl& c = ctl[w.sim];
+        const Sim& S = sims[w.sim];
+        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale) continue;
+        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) {
+            const int v = S.surf[i];
+            S.watch[v] = make_float4(d2f(S.px[v]), d2f(S.py[v]), d2f(S.pz[v]), 0.0f);
+            int n = 0;
+            for_each_watch_partner(S, v, c.hash_parity, [&](int) { n++; });
+            S.woff[i + 1] = n;
+        }
+    }
+}
+
+// Pass 2, one block per simulation of the batch: the counts become offsets (an exclusive
+// scan over the surface voxels); a regeneration that exceeds the lists' capacity leaves the
+// simulation on the hash search until the next one.
+__global__ void __launch_bounds__(1024) k_watch_scan(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
+    __shared__ int s_sum[1024];
+    if ((int)blockIdx.x >= n) return;
+    const int sim = slots[blockIdx.x];
+    Ctl& c = ctl[sim];
+    const Sim& S = sims[sim];
+    if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale) return;
+    const int ns = S.nsurf;
+    const int per = (ns + blockDim.x - 1) / blockDim.x;
+    const int b0 = min(ns, (int)threadIdx.x * per), b1 = min(ns, b0 + per);
+    int sum = 0;
+    for (int i = b0; i < b1; i++) sum += S.woff[i + 1];
+    s_sum[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        const int x = (int)threadIdx.x >= off ? s_sum[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_sum[threadIdx.x] += x;
+        __syncthreads();
+    }
+    int run = threadIdx.x ? s_sum[threadIdx.x - 1] : 0;
+    for (int i = b0; i < b1; i++) {
+        const int cnt = S.woff[i + 1];
+        S.woff[i + 1] = run + cnt;   // the end of voxel i's run = the start of voxel i + 1's
+        run += cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        S.woff[0] = 0;
+        const int total = s_sum[blockDim.x - 1];
+        c.watch_ok = total <= S.wcap ? 1 : 0;
+        c.watch_regens += 1;
+    }
+}
+
+// Pass 3: every surface voxel writes its partners into its run and sorts them.
+__global__ void __launch_bounds__(128) k_watch_fill(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                    int n_items) {
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const Item w = items[it];
+        const Ctl& c = ctl[w.sim];
+        const Sim& S = sims[w.sim];
+        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale || !c.watch_ok) continue;
+        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) {
+            const int v = S.surf[i];
+            int* out = S.wlist + S.woff[i];
+            const int n = S.woff[i + 1] - S.woff[i];
+            int k = 0;
+            for_each_watch_partner(S, v, c.hash_parity, [&](int q) { if (k < n) out[k++] = q; });
+            for (int a = 1; a < k; a++) {   // insertion sort: the reference's increasing partner order
+                const int q = out[a];
+                int j = a;
+                while (j > 0 && out[j - 1] > q) { out[j] = out[j - 1]; j--; }
+                out[j] = q;
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
     __shared__ int s_item;
     for (;;) {
@@ -735,7 +891,8 @@ __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, 
         const int per = (S.hash_size + S.nsurf - 1) / (S.nsurf > 0 ? S.nsurf : 1);
         const int cb = w.begin * per, ce = min(S.hash_size, (w.end == S.nsurf) ? S.hash_size : w.end * per);
         for (int h = cb + threadIdx.x; h < ce; h += blockDim.x) other[h] = -1;
-        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, c);
+        const bool watch = (S.flags & SF_WATCH) && c.watch_ok;
+        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, c, watch ? i : -1);
     }
 }
 
@@ -823,7 +980,8 @@ __device__ void frozen_voxel(const Sim& S, int v, uint32_t fl, const VMat& m, co
     if ((flags & SF_COLLIDE) && !(fl & (VF_INTERIOR | VF_REMOVED))) hash_insert(S, v, pos, S.temp[v], hash_next_table);
 }
 
-__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, const StepTimes& st, int flags, double* com4, int* hash_next_table) {
+__device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, const StepTimes& st, int flags, double* com4, int* hash_next_table,
+                                             int* watch_moved = nullptr) {
     const double t_cycles = st.t_cycles;
     const int nv = S.nv;
     const VMat& m = S.vm[__ldg(S.vmat + v)];
@@ -1023,6 +1181,14 @@ __device__ __forceinline__ void voxel_update(const Sim& S, int v, float dt, cons
     }
     // insert into the table the next step's contact pass reads
     if ((flags & SF_COLLIDE) && !(fl & VF_INTERIOR)) hash_insert(S, v, pos, temp_next, hash_next_table);
+    // watch lists: a surface voxel further than the re-check distance from where the last
+    // regeneration saw it makes the next step regenerate (CVoxelyze::updateCollisions,
+    // Voxelyze.cpp:689-697: (pos - lastColWatchPosition).Length2() > recalcDist*recalcDist)
+    if (watch_moved && !(fl & VF_INTERIOR)) {
+        const float4 wp = S.watch[v];
+        const double dx = pos.x - (double)wp.x, dy = pos.y - (double)wp.y, dz = pos.z - (double)wp.z;
+        if (dx * dx + dy * dy + dz * dz > (double)S.recalc2) *watch_moved = 1;
+    }
 }
 
 __device__ __forceinline__ double block_sum(double x, double* red) {
@@ -1093,6 +1259,7 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
     c.steps = stepno;
     if (flags & SF_VARY) c.t_cycles = (c.t + c.dt) / S.temp_period;   // the next step's actuation phase
     if (flags & SF_COLLIDE) c.hash_parity ^= 1;
+    if (flags & SF_WATCH) { c.col_stale = c.col_moved; c.col_moved = 0; }
     if (com_step) {
         c.angle_samples++;
         for (int j = 0; j < 3; j++) { c.com_hist[0][j] = c.com_hist[1][j]; c.com_hist[1][j] = c.com[j]; }
@@ -1168,7 +1335,7 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxel
                 st.t_now = c.t; st.t_next = c.t + dt; st.t_cycles = c.t_cycles; st.angle = c.recent_angle;
                 st.closeness = c.closeness; st.close_pairs = c.num_close_pairs; st.hits = c.hit_count;
                 int* hnext = (S.flags & SF_COLLIDE) ? S.hash_head + (size_t)(c.hash_parity ^ 1) * S.hash_size : nullptr;
-                voxel_update(S, e.y, dt, st, S.flags, nullptr, hnext);
+                voxel_update(S, e.y, dt, st, S.flags, nullptr, hnext, (S.flags & SF_WATCH) ? &ctl[e.x].col_moved : nullptr);
             }
         }
     }
@@ -1469,6 +1636,11 @@ inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, con
     k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk, claim);
 }
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
+inline void l_watch(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n_items, const int* slots, int n_sims) {
+    k_watch_count<<<g, 128, 0, s>>>(sims, ctl, it, n_items);
+    if (n_sims > 0) k_watch_scan<<<n_sims, 1024, 0, s>>>(sims, ctl, slots, n_sims);
+    k_watch_fill<<<g, 128, 0, s>>>(sims, ctl, it, n_items);
+}
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
                      int* tk, int claim) {
     k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk, claim);
@@ -1512,7 +1684,7 @@ inline int l_resident_blocks(int which, int block) {
 }
 inline KernelSet make_kernelset(const char* name) {
     return KernelSet{name, l_bins, l_links, l_contacts, l_voxels, l_sim_end, l_signals, l_attach, l_dt, l_init_temp, l_hash_build, l_com,
-                     l_gather, l_resident_blocks, GVX_STEP_BLOCK};
+                     l_gather, l_resident_blocks, GVX_STEP_BLOCK, l_watch};
 }
 }  // namespace GVX_KNS
 }  // namespace gvx

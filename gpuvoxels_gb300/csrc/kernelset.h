@@ -37,6 +37,10 @@ struct KernelSet {
     // resident blocks per SM of k_links (0) or k_voxels (1) at a block size
     int (*resident_blocks)(int which, int block);
     int max_block;   // largest block k_links / k_voxels are compiled for
+    // watch-list regeneration (count, offsets, fill) of the simulations that need it, over the
+    // contact items and the batch's slot list
+    void (*watch)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n_items, const int* slots,
+                  int n_sims);
 };
 
 KernelSet kernelset_exact();   // every multiply and add rounded separately (the reference's CPU rounding)

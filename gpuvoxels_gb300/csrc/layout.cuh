@@ -48,6 +48,7 @@ constexpr int SF_REMOVE = 512;                 // secondary experiment: material
 constexpr int SF_FIXEDMAT = 1024;              // materials marked Fixed (their voxels never move)
 constexpr int SF_ATTACH = 2048;                // touching sticky voxels may be joined by new links
 constexpr int SF_DYNSURF = SF_DETACH | SF_REMOVE | SF_ATTACH;   // the surface set can change during the run
+constexpr int SF_WATCH = 4096;                 // contacts from watch lists regenerated as the reference does
 
 // VMat::vx3 bits
 constexpr int VM_TARGET = 1, VM_PACEMAKER = 2, VM_FIXED = 4, VM_STICKY = 8;
@@ -153,6 +154,17 @@ struct Sim {
     int32_t* hash_head;         // 2 tables of hash_size
     int32_t* hash_next;         // per voxel
     float4* cpos;               // per hashed voxel: position rounded to float, float base size (broadphase only)
+    // watch lists (SF_WATCH), the reference's collision list (Voxelyze.cpp:671-751): per voxel the
+    // position at the last regeneration (lastColWatchPosition, float), per surface index the
+    // offset of its partners in wlist (nsurf + 1 entries), the list's capacity, the squared watch
+    // radius and re-check distance (float, as the reference forms them), and the hash cells the
+    // regeneration scans on each side of a voxel's own
+    float4* watch;
+    int32_t* woff;
+    int32_t* wlist;
+    int32_t wcap;
+    int32_t wcells;
+    float watch_r2, recalc2;
     float inv_cell;             // 1 / cell_size, for the float cell index
     // VX3 extras
     const double* cilia;        // BaseCiliaForce, 3 blocks of nv (SF_CILIA)
@@ -200,7 +212,10 @@ struct Ctl {
     int32_t reinit_done;        // initial centre of mass reset (secondary experiment)
     int32_t n_links;            // links in use (VX3 attachment appends)
     int32_t n_cand;             // attachment candidates found this step
-    int32_t pad_ctl3;
+    int32_t col_stale;          // SF_WATCH: regenerate the watch lists at this step's contact pass
+    int32_t col_moved;          // SF_WATCH: a surface voxel moved beyond the re-check distance this step
+    int32_t watch_ok;           // SF_WATCH: the lists hold the current regeneration (else the hash search runs)
+    int32_t watch_regens;       // regenerations so far
     double init_com[3];         // initial centre of mass (host value, reset by the secondary experiment)
     MathTree stop;
 };
