@@ -65,10 +65,10 @@ def measured_peaks():
 # per link (k_links) and per voxel (k_voxels) of one step, read by ncu per workload
 # (sm__thread_inst_executed_pipe_fp64_pred_on.sum / links or voxels), and DRAM bytes per
 # link of one k_links launch (dram__bytes_read.sum + dram__bytes_write.sum / links).
-# Sources: profiles/k_links_k_voxels_batch512_steady.md (batch, step 205).
+# Sources: profiles/k_links_k_voxels_batch512_fp64_mix.md (batch, step 201).
 FP64_COUNTS = {
-    "batch": dict(per_link=684878336 / 1627115, per_voxel=236663360 / 844972,
-                  traffic_per_link=(410284544 + 358874112) / 1627115, source="ncu, 512-creature batch, step 205"),
+    "batch": dict(per_link=672121856 / 1627115, per_voxel=199437824 / 844972,
+                  traffic_per_link=(409993728 + 359042560) / 1627115, source="ncu, 512-creature batch, step 201"),
     # profiles/fp64_counts_collide_slab.md: 8 of the 64 collision creatures and a 100x100x50 slab, step 201
     "collide": dict(per_link=156123968 / 373621, per_voxel=60842368 / 249183,
                     traffic_per_link=(111591680 + 71004928) / 373621, source="ncu, 8 collision creatures 40^3, step 201"),

@@ -2080,9 +2080,10 @@ public:
             ks_.gather(stream_, d_sims_, dslot + k0, doff + k0, std::min(65535, n - k0), dpos, dq, dfl);
         CK(cudaGetLastError());
         const size_t b_all = b_pos + b_q + b_fl;
-        if (gen_.p && gen_.cap >= b_all) {
-            // the generation upload buffer is large enough: one copy into pinned memory, then
-            // host threads copy into the caller's arrays (and take their first-touch faults)
+        if (b_all <= kPinnedUploadMax) {
+            // one copy into the pinned generation buffer (grown if need be; pinned buffers are
+            // cached across contexts), then host threads copy into the caller's arrays (and take
+            // their first-touch faults): a copy straight into pageable memory took up to 38 ms
             TraceClock tg;
             if (int e = pinned(&gen_, b_all, err)) return e;   // waits for the buffer's last use
             tg.mark("gather: pinned buffer");

@@ -632,27 +632,7 @@ __device__ __forceinline__ void for_each_contact(const Sim& S, int v, int parity
 // limit: up to S.contact_inline (at most kContactInline) contacts go to the
 // voxel's own slots; a voxel with more takes a run of records of the spill pool, fills it with its
 // partners in a second pass over the hash and sorts them there.
-// Calls fn(q) for every partner q of voxel v (surface index si) on its watch list that
-// overlaps it this step, in increasing q: the reference's collision list of the last
-// regeneration (sorted), each pair's float envelope test first, then the exact test.
-template <typename Fn>
-__device__ __forceinline__ void for_each_watch_contact(const Sim& S, int v, int si, Fn fn) {
-    const float4 pv = S.cpos[v];
-    const int e = S.woff[si + 1];
-    for (int k = S.woff[si]; k < e; k++) {
-        const int q = S.wlist[k];
-        if (!maybe_touching(pv, S.cpos[q], S.env_radius)) continue;
-        float f3[3];
-        if (pair_force(S, v < q ? v : q, v < q ? q : v, f3)) fn(q);
-    }
-}
-
-__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c, int si = -1) {
-    const bool watch = si >= 0;
-    auto enumerate = [&](auto fn) {
-        if (watch) for_each_watch_contact(S, v, si, fn);
-        else for_each_contact(S, v, parity, fn);
-    };
+__device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
     if (S.flags & SF_DYNSURF) {
         // the surface set changes during the run: every voxel is listed, interior and
         // removed ones have no contacts
@@ -663,7 +643,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c, int si =
     const int cap = min(max(S.contact_inline, 1), kContactInline);
     int partners[kContactInline] = {};
     int np = 0, ntot = 0;
-    enumerate([&](int q) {
+    for_each_contact(S, v, parity, [&](int q) {
         ntot++;
         if (np == cap) {
             if (q > partners[cap - 1]) return;
@@ -685,7 +665,7 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c, int si =
         }
         sp = S.spill_p + off;
         int k = 0;
-        enumerate([&](int q) { if (k < ntot) sp[k++] = q; });
+        for_each_contact(S, v, parity, [&](int q) { if (k < ntot) sp[k++] = q; });
         for (int i = 1; i < k; i++) {   // insertion sort by partner index (runs are short)
             const int q = sp[i];
             int j = i;
@@ -876,6 +856,59 @@ __global__ void __launch_bounds__(128) k_watch_fill(const Sim* __restrict__ sims
     }
 }
 
+// The contact pass of surface voxel v (surface index si) from its watch list: the list is in
+// increasing partner order, so the overlapping pairs (float envelope test, then the exact
+// test) are the reference's colWatch terms in order; their forces go straight to the voxel's
+// slots, and a voxel with more than its slots walks the list again into a spill run.
+__device__ void voxel_contacts_watch(const Sim& S, int v, int si, Ctl& c) {
+    const int cap = min(max(S.contact_inline, 1), kContactInline);
+    float* out = S.cforce + (size_t)v * 3 * kContactInline;
+    const float4 pv = S.cpos[v];
+    const int b = S.woff[si], e = S.woff[si + 1];
+    const bool targets = S.flags & SF_TARGETS;
+    const bool tv = targets && (S.vm[__ldg(S.vmat + v)].vx3 & VM_TARGET);
+    int n = 0, pairs = 0;
+    bool hit = false;
+    for (int k = b; k < e; k++) {
+        const int q = S.wlist[k];
+        if (!maybe_touching(pv, S.cpos[q], S.env_radius)) continue;
+        float f3[3];
+        if (!pair_force(S, v < q ? v : q, v < q ? q : v, f3)) continue;
+        if (n < cap) {
+            const float sgn = v < q ? 1.0f : -1.0f;   // contactForce(): +force on voxel1, -force on voxel2
+            out[3 * n] = sgn * f3[0]; out[3 * n + 1] = sgn * f3[1]; out[3 * n + 2] = sgn * f3[2];
+        }
+        n++;
+        if (targets && (bool)(S.vm[__ldg(S.vmat + q)].vx3 & VM_TARGET) != tv) { hit = true; if (q > v) pairs++; }
+    }
+    if (n > cap) {
+        const int off = atomicAdd(S.spill_used, n);
+        if (off < 0 || (unsigned)off > (unsigned)(S.spill_cap - n)) {
+            atomicOr(&c.error, 2);   // the pool's records for this step are used up
+            S.ccount[v] = 0;
+            return;
+        }
+        int j = 0;
+        for (int k = b; k < e && j < n; k++) {
+            const int q = S.wlist[k];
+            if (!maybe_touching(pv, S.cpos[q], S.env_radius)) continue;
+            float f3[3];
+            if (!pair_force(S, v < q ? v : q, v < q ? q : v, f3)) continue;
+            const float sgn = v < q ? 1.0f : -1.0f;
+            S.spill_p[off + j] = q;
+            float* o = S.spill_f + 3 * (size_t)(off + j);
+            o[0] = sgn * f3[0]; o[1] = sgn * f3[1]; o[2] = sgn * f3[2];
+            j++;
+        }
+        S.cspill[v] = off;
+    }
+    S.ccount[v] = n;
+    if (targets) {   // VX3 target contacts, as in voxel_contacts
+        if (pairs) atomicAdd(&c.hit_count, pairs);
+        if (hit && !tv && (S.flags & SF_SIGNALS)) S.vfl[v] |= VF_TGTHIT;
+    }
+}
+
 __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items, int n_items, int* tickets) {
     __shared__ int s_item;
     for (;;) {
@@ -891,10 +924,14 @@ __global__ void __launch_bounds__(128) k_contacts(const Sim* __restrict__ sims, 
         const int per = (S.hash_size + S.nsurf - 1) / (S.nsurf > 0 ? S.nsurf : 1);
         const int cb = w.begin * per, ce = min(S.hash_size, (w.end == S.nsurf) ? S.hash_size : w.end * per);
         for (int h = cb + threadIdx.x; h < ce; h += blockDim.x) other[h] = -1;
-        const bool watch = (S.flags & SF_WATCH) && c.watch_ok;
-        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, c, watch ? i : -1);
+        if ((S.flags & SF_WATCH) && c.watch_ok) {
+            for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts_watch(S, S.surf[i], i, c);
+        } else {
+            for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) voxel_contacts(S, S.surf[i], parity, c);
+        }
     }
 }
+
 
 // CVX_Voxel::timeStep with force(), moment() and floorForce()
 // (Voxelyze3/src/old/VX_Voxel.cpp:163-297), then the Poisson strain the next

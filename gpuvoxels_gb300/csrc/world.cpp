@@ -552,6 +552,10 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     }
     parse_mathtree(root->path("VXA.Simulator.StopCondition.StopConditionFormula"), &d->stop_formula);
     parse_mathtree(root->path("VXA.Simulator.FitnessFunction"), &d->fitness);
+    // a formula the evaluator cannot take (an unknown token or variable, or more than
+    // kMaxMathTokens - 1 tokens) is refused rather than evaluated to NaN
+    if (!d->stop_formula.valid) { *err = "invalid or too long stop condition formula (at most 63 tokens)"; return false; }
+    if (!d->fitness.valid) { *err = "invalid or too long fitness formula (at most 63 tokens)"; return false; }
     return true;
 }
 

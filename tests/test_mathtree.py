@@ -83,3 +83,15 @@ def test_device_evaluation_matches_reference(ctx, which):
         vxa = _vxa_with(case["xml"], which)
         got = ctx.eval_formula(vxa, which, np.array(case["vars"]))
         assert _close(got, case["ref"], exact=_exact(case)), (which, case["name"], got, case["ref"])
+
+
+def test_long_or_malformed_formula_is_refused():
+    """Formulas the evaluator cannot hold (more than 63 tokens) or parse are refused with
+    VX3_E_PARSE when the world is read, instead of evaluating to NaN."""
+    long_xml = "<mtVAR>t</mtVAR>"
+    for _ in range(40):
+        long_xml = f"<mtADD>{long_xml}<mtCONST>1</mtCONST></mtADD>"
+    for xml in (long_xml, "<mtFOO><mtVAR>t</mtVAR></mtFOO>", "<mtVAR>nowhere</mtVAR>"):
+        with pytest.raises(g.VX3Error):
+            g.inspect_vxa(_vxa_with(xml, "stop"))
+    g.inspect_vxa(_vxa_with("<mtSUB><mtVAR>t</mtVAR><mtCONST>1</mtCONST></mtSUB>", "stop"))
