@@ -626,8 +626,10 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16, help="requests of the serving stream (per offered rate)")
     ap.add_argument("--serve-rates", default="50,200,2000", help="offered request rates (req/s) of the serving stream")
     ap.add_argument("--chunk-steps", type=int, default=64)
-    ap.add_argument("--serve-order", type=int, default=0, help="admission order: 0 first come first served, 1 least work first")
-    ap.add_argument("--serve-cap-voxels", type=int, default=0, help="most voxels in the running batch (0: the HBM budget decides)")
+    ap.add_argument("--serve-order", type=int, default=1, help="admission order: 0 first come first served, 1 least work first")
+    ap.add_argument("--serve-cap-voxels", type=int, default=150000,
+                    help="most voxels in the running batch (0: the HBM budget decides); 150k voxels (~450k links) keep the "
+                         "step kernels' resident warps busy several times over")
     ap.add_argument("--plain-sample-steps", type=int, default=256,
                     help="steps of each request measured in PLAIN mode for the plain arm of the serving stream")
     ap.add_argument("--collide-steps", type=int, default=2000, help="steps of the collision-heavy block (of 20,000)")

@@ -495,6 +495,12 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     if (const XmlNode* bcf = st->child("BaseCiliaForce")) read_triples(bcf, &d->base_cilia);
     if (const XmlNode* scf = st->child("ShiftCiliaForce")) read_triples(scf, &d->shift_cilia);
     int n = 0;
+    {
+        size_t filled = 0;
+        for (uint8_t c : cells) filled += (signed char)c > 0;
+        d->voxels.reserve(4 * filled);
+        d->phase.reserve(filled);
+    }
     for (long i = 0; i < (long)X * Y * Z; i++) {
         int mi = (int)(signed char)cells[i] - 1;
         if (mi < 0) continue;
@@ -787,41 +793,42 @@ bool build_world(const SimDesc& d, SimWorld* w, std::string* err) {
     int mn[3] = {1 << 30, 1 << 30, 1 << 30}, mx[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
     for (int i = 0; i < nv; i++)
         for (int k = 0; k < 3; k++) { mn[k] = std::min(mn[k], d.voxels[4 * i + k]); mx[k] = std::max(mx[k], d.voxels[4 * i + k]); }
-    long dx = mx[0] - mn[0] + 1, dy = mx[1] - mn[1] + 1, dz = mx[2] - mn[2] + 1;
-    std::vector<int32_t> grid((size_t)(dx * dy * dz), -1);
-    auto at = [&](int x, int y, int z) -> int32_t {
-        x -= mn[0]; y -= mn[1]; z -= mn[2];
-        if (x < 0 || y < 0 || z < 0 || x >= dx || y >= dy || z >= dz) return -1;
-        return grid[(size_t)((z * dy + y) * dx + x)];
-    };
-    static const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+    const long dx = mx[0] - mn[0] + 1, dy = mx[1] - mn[1] + 1, dz = mx[2] - mn[2] + 1;
+    // lattice sites with a border of one empty site, so the six neighbour reads need no bounds test
+    const long px = dx + 2, pxy = (dx + 2) * (dy + 2);
+    std::vector<int32_t> grid((size_t)(pxy * (dz + 2)), -1);
+    const long step[6] = {1, -1, px, -px, pxy, -pxy};   // direction order X+,X-,Y+,Y-,Z+,Z-
+    const int nm = (int)w->vmats.size();
+    std::vector<int> pair_lmat((size_t)nm * nm, -1);    // link material of a material pair, either order
     w->vox_links.assign((size_t)nv * 6, -1);
     w->link_neg.clear(); w->link_pos.clear(); w->link_axis.clear(); w->link_mat.clear();
-    std::vector<std::pair<int, int>> lm_pairs;
+    w->link_neg.reserve((size_t)nv * 3); w->link_pos.reserve((size_t)nv * 3);
+    w->link_axis.reserve((size_t)nv * 3); w->link_mat.reserve((size_t)nv * 3);
     for (int i = 0; i < nv; i++) {
-        int x = d.voxels[4 * i], y = d.voxels[4 * i + 1], z = d.voxels[4 * i + 2];
-        if (at(x, y, z) >= 0) { *err = "two voxels at the same lattice site"; return false; }
-        grid[(size_t)(((z - mn[2]) * dy + (y - mn[1])) * dx + (x - mn[0]))] = i;
+        const int* v = &d.voxels[4 * (size_t)i];
+        if (v[3] < 0 || v[3] >= nm) { *err = "voxel references a material missing from the palette"; return false; }
+        const long site = ((v[2] - mn[2] + 1) * (dy + 2) + (v[1] - mn[1] + 1)) * px + (v[0] - mn[0] + 1);
+        if (grid[(size_t)site] >= 0) { *err = "two voxels at the same lattice site"; return false; }
+        grid[(size_t)site] = i;
+        // a link is made when the second of its two voxels (in structure order) is placed
         for (int dir = 0; dir < 6; dir++) {
-            int b = at(x + off[dir][0], y + off[dir][1], z + off[dir][2]);
+            const int b = grid[(size_t)(site + step[dir])];
             if (b < 0 || w->vox_links[(size_t)i * 6 + dir] >= 0) continue;
-            int ma = d.voxels[4 * i + 3], mb = d.voxels[4 * b + 3];
-            int lmi = -1;
-            for (int k = 0; k < (int)lm_pairs.size(); k++)
-                if ((lm_pairs[k].first == ma && lm_pairs[k].second == mb) || (lm_pairs[k].first == mb && lm_pairs[k].second == ma)) { lmi = k; break; }
+            const int ma = v[3], mb = d.voxels[4 * (size_t)b + 3];
+            int lmi = pair_lmat[(size_t)ma * nm + mb];
             if (lmi < 0) {
-                lmi = (int)lm_pairs.size();
-                lm_pairs.emplace_back(ma, mb);
+                lmi = (int)w->lmats.size();
+                pair_lmat[(size_t)ma * nm + mb] = pair_lmat[(size_t)mb * nm + ma] = lmi;
                 w->lmats.push_back(make_link_material(w->vmats[ma], w->vmats[mb], ma, mb));
             }
-            int li = (int)w->link_neg.size();
-            bool rev = dir % 2 == 1;
+            const int li = (int)w->link_neg.size();
+            const bool rev = dir % 2 == 1;
             w->link_neg.push_back(rev ? b : i);
             w->link_pos.push_back(rev ? i : b);
             w->link_axis.push_back((uint8_t)(dir / 2));
             w->link_mat.push_back((uint8_t)lmi);
             w->vox_links[(size_t)i * 6 + dir] = li;
-            w->vox_links[(size_t)b * 6 + (dir - dir % 2 + (dir + 1) % 2)] = li;
+            w->vox_links[(size_t)b * 6 + (dir ^ 1)] = li;
         }
     }
     // VX3 attachment: a new link between two voxels of one sticky material takes the combined
@@ -831,12 +838,9 @@ bool build_world(const SimDesc& d, SimWorld* w, std::string* err) {
     if (d.enable_attach) {
         for (int m = 0; m < (int)d.mats.size(); m++) {
             if (!d.mats[m].sticky) continue;
-            int lmi = -1;
-            for (int k = 0; k < (int)lm_pairs.size(); k++)
-                if (lm_pairs[k].first == m && lm_pairs[k].second == m) { lmi = k; break; }
+            int& lmi = pair_lmat[(size_t)m * nm + m];
             if (lmi < 0) {
-                lmi = (int)lm_pairs.size();
-                lm_pairs.emplace_back(m, m);
+                lmi = (int)w->lmats.size();
                 w->lmats.push_back(make_link_material(w->vmats[m], w->vmats[m], m, m));
             }
             w->attach_lmat[m] = lmi;
