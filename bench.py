@@ -427,7 +427,9 @@ def serve_stream(args, device, budget, n_requests, rates):
             while nxt < len(reqs) and arrivals[nxt] <= free_at:
                 waiting.append(nxt)
                 nxt += 1
-            pick = min(waiting, key=lambda i: (work[i], i)) if args.serve_order == 1 else waiting[0]
+            # one request at a time: a lane for the longest changes nothing, so orders 1 and 2 are
+            # the least work first
+            pick = min(waiting, key=lambda i: (work[i], i)) if args.serve_order >= 1 else waiting[0]
             waiting.remove(pick)
             free_at += service[pick]
             plat.append(free_at - arrivals[pick])
@@ -442,14 +444,16 @@ def serve_stream(args, device, budget, n_requests, rates):
     return dict(
         requests=len(reqs), voxels_min=min(vs), voxels_max=max(vs), voxel_steps_total=int(sum(work)),
         collide=int(sum(1 for c, _ in reqs if c.meta.get("collide"))), chunk_steps=args.chunk_steps,
-        policy=dict(order="least voxels x horizon first" if args.serve_order == 1 else "first come first served",
+        policy=dict(order={0: "first come first served", 1: "least voxels x horizon first",
+                           2: "least voxels x horizon first, beside a lane for the most work queued"}[args.serve_order],
                     max_active_voxels=args.serve_cap_voxels, both_arms=True),
         stream=("Poisson arrivals at each offered rate (seeded); creatures with V log-uniform in [100, 1e5] (fill "
                 "U(0.5, 0.9), 4 materials E log-uniform [1e5, 1e7] Pa), horizons U[1e3, 5e4] steps, 20% with "
                 "self-collision; the same requests at every rate"),
         plain_arm=(f"each request alone in PLAIN mode (one simulation per launch): load + first step measured, then "
                    f"min(horizon, {args.plain_sample_steps}) steps measured and scaled to its horizon; the stream's "
-                   "queue replayed first come first served with those service times"),
+                   "queue replayed with those service times, in the served arm's order (least work first for "
+                   "orders 1 and 2, a lane being no use to one request at a time)"),
         plain_service_s_total=sum(service), generate_s=round(gen_s, 2), target_served_vs_plain=10.0, rates=out)
 
 
@@ -626,7 +630,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16, help="requests of the serving stream (per offered rate)")
     ap.add_argument("--serve-rates", default="50,200,2000", help="offered request rates (req/s) of the serving stream")
     ap.add_argument("--chunk-steps", type=int, default=64)
-    ap.add_argument("--serve-order", type=int, default=1, help="admission order: 0 first come first served, 1 least work first")
+    ap.add_argument("--serve-order", type=int, default=1, choices=(0, 1, 2),
+                    help="admission order: 0 first come first served, 1 least work first, 2 least work first beside a "
+                         "lane for the most work queued")
     ap.add_argument("--serve-cap-voxels", type=int, default=150000,
                     help="most voxels in the running batch (0: the HBM budget decides); 150k voxels (~450k links) keep the "
                          "step kernels' resident warps busy several times over")

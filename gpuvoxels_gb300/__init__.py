@@ -24,7 +24,7 @@ import numpy as np
 from . import build as _build
 
 PLAIN, BATCHED = 0, 1
-SERVE_FCFS, SERVE_LEAST_WORK = 0, 1
+SERVE_FCFS, SERVE_LEAST_WORK, SERVE_LONG_LANE = 0, 1, 2
 EXACT, FMA = 0, 1
 SIM_IDLE, SIM_RUNNING, SIM_DONE, SIM_DIVERGED, SIM_ERROR = range(5)
 ERRORS = {-1: "VX3_E_PARSE", -2: "VX3_E_OOM_BUDGET", -3: "VX3_E_DIVERGED", -4: "VX3_E_TIMEOUT", -5: "VX3_E_CUDA",
@@ -341,8 +341,10 @@ class Context:
         self.L.vx3_set_tuning(self.h, block_links, block_voxels, items_links, items_voxels, graph_steps)
 
     def set_serving(self, order: int = 0, max_active_voxels: int = 0):
-        """Admission policy of poll(): order 0 first come first served, 1 least voxels x horizon first;
-        max_active_voxels caps the running batch (0 = the HBM budget decides)."""
+        """Admission policy of poll(): order 0 first come first served, 1 least voxels x horizon first,
+        2 least work first beside one lane that takes the queued request with the most work whenever
+        it is free; max_active_voxels caps the running batch (0 = the HBM budget decides; the lane's
+        request is not counted)."""
         self._check(self.L.vx3_set_serving(self.h, order, max_active_voxels))
 
     def set_claim_sizes(self, claim_links=0, claim_voxels=0):

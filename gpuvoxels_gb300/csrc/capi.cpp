@@ -101,36 +101,19 @@ int vx3_load_vxa_many(vx3_ctx* c, const char* base, const char* const* vxds, con
     if (!base)
         for (int i = 0; i < n; i++)
             if (!vxds[i]) return fail(c, VX3_E_ARG, "without a base every entry must be a whole VXA");
-    std::vector<gvx::SimDesc> descs((size_t)n);
+    // each VXD merged into its own copy of the base, read and built on the engine's host threads
     std::vector<std::string> errs((size_t)n);
     std::vector<int> rc((size_t)n, VX3_OK);
-    // parse on host threads: each VXD merged into its own copy of the base
-    std::atomic<int> next{0};
-    auto work = [&]() {
-        for (int i = next++; i < n; i = next++) {
-            const bool ok = base ? gvx::parse_vxa(base, vxds ? vxds[i] : nullptr, &descs[i], &errs[i])
-                                 : gvx::parse_vxa(vxds[i], nullptr, &descs[i], &errs[i]);
-            if (!ok) rc[i] = VX3_E_PARSE;
-            descs[i].name = (names && names[i]) ? names[i] : "";
-        }
-    };
-    const int nt = std::max(1, std::min(n, (int)std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    for (int t = 1; t < nt; t++) pool.emplace_back(work);
-    work();
-    for (auto& t : pool) t.join();
-    std::vector<const gvx::SimDesc*> ok;
-    std::vector<int> where;
-    for (int i = 0; i < n; i++)
-        if (rc[i] == VX3_OK) { ok.push_back(&descs[i]); where.push_back(i); }
-    std::vector<int64_t> got(ok.size());
-    std::vector<std::string> berr(ok.size());
-    c->eng->add_sims(ok.data(), (int)ok.size(), got.data(), berr.data());
-    for (size_t k = 0; k < ok.size(); k++) {
-        const int i = where[k];
-        if (got[k] < 0) { rc[i] = VX3_E_PARSE; errs[i] = berr[k]; continue; }
-        ids[i] = got[k];
-        c->names[got[k]] = descs[i].name;
+    std::vector<int64_t> got((size_t)n, -1);
+    c->eng->add_sims_read(n, [&](int i, gvx::SimDesc* d, std::string* e) {
+        const bool ok = base ? gvx::parse_vxa(base, vxds ? vxds[i] : nullptr, d, e) : gvx::parse_vxa(vxds[i], nullptr, d, e);
+        d->name = (names && names[i]) ? names[i] : "";
+        return ok;
+    }, got.data(), errs.data());
+    for (int i = 0; i < n; i++) {
+        if (got[i] < 0) { rc[i] = VX3_E_PARSE; continue; }
+        ids[i] = got[i];
+        c->names[got[i]] = (names && names[i]) ? names[i] : "";
     }
     int first = VX3_OK;
     for (int i = 0; i < n; i++) {
@@ -547,7 +530,7 @@ int vx3_autotune(vx3_ctx* c, const vx3_sim_id* ids, int n) {
 
 int vx3_set_serving(vx3_ctx* c, int order, int64_t max_active_voxels) {
     if (!c) return VX3_E_ARG;
-    return c->eng->set_serving(order, max_active_voxels) ? fail(c, VX3_E_ARG, "order must be 0 or 1, the voxel cap >= 0") : VX3_OK;
+    return c->eng->set_serving(order, max_active_voxels) ? fail(c, VX3_E_ARG, "order must be 0, 1 or 2, the voxel cap >= 0") : VX3_OK;
 }
 
 int vx3_set_claim_sizes(vx3_ctx* c, int claim_links, int claim_voxels) {

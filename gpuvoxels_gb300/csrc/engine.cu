@@ -113,6 +113,19 @@ __global__ void k_scatter_regions(const char* __restrict__ stage, const RegionCo
         dst[i] = i < ni ? src[i] : make_uint4(0u, 0u, 0u, 0u);
 }
 
+// The work-list fields of a new batch's control blocks in one launch: per batch entry the
+// number and the first index of the simulation's voxel items, and the completion counters
+// cleared (one small copy per simulation took about a millisecond for 512 of them).
+__global__ void k_set_batch_items(dev::Ctl* ctl, const int* __restrict__ slots, const int2* __restrict__ items, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dev::Ctl& c = ctl[slots[i]];
+    c.n_vox_items = items[i].x;
+    c.item_begin = items[i].y;
+    c.done_items = 0;
+    c.sig_done_items = 0;
+}
+
 // Host tables of the C library's powf(x, -nu) for every float x in [0.5, 2), one per Poisson
 // ratio: the reference's CPU path takes the Poisson strain's power from that function
 // (CVX_Voxel::strain, Voxelyze3/src/old/VX_Voxel.cpp:327), whose results are not always the
@@ -312,8 +325,10 @@ public:
     int2* d_vox_perm_ = nullptr;
     size_t cap_vbins_ = 0, cap_vperm_ = 0;
     int* d_batch_slots_ = nullptr;
+    int2* d_batch_items_ = nullptr;          // per batch entry: voxel items, first voxel item
     int n_batch_ = 0, cap_batch_ = 0;
     std::vector<int> batch_slots_host_;
+    std::vector<int2> batch_items_host_;
     int n_attach_ = 0, cap_attach_ = 0;     // simulations with VX3 attachment in the batch
     int64_t graph_launches_ = 0;            // kernels one replay of the captured graph launches
     int* d_attach_slots_ = nullptr;
@@ -361,7 +376,7 @@ public:
         cudaFree(d_spill_p_); cudaFree(d_spill_f_);
         cudaFree(d_attach_slots_);
         cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
-        cudaFree(d_vox_hist_); cudaFree(d_vox_base_); cudaFree(d_vox_total_); cudaFree(d_vox_perm_); cudaFree(d_batch_slots_);
+        cudaFree(d_vox_hist_); cudaFree(d_vox_base_); cudaFree(d_vox_total_); cudaFree(d_vox_perm_); cudaFree(d_batch_slots_); cudaFree(d_batch_items_);
         cudaFree(arena_base_);
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
@@ -424,6 +439,7 @@ public:
         CK(cudaMalloc(&d_vox_perm_, sizeof(int2) * cap_vperm_));
         CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
         CK(cudaMalloc(&d_batch_slots_, sizeof(int) * cap_batch_));
+        CK(cudaMalloc(&d_batch_items_, sizeof(int2) * cap_batch_));
         CK(cudaMalloc(&d_attach_slots_, sizeof(int) * cap_attach_));
         return 0;
     }
@@ -530,8 +546,12 @@ public:
     static bool attaches(const SimDesc& d) { return d.enable_attach && d.collisions; }
     static int link_capacity(const SimWorld& w) { return attaches(w.desc) ? std::max(w.nl, 3 * w.nv) : w.nl; }
     static int target_count(const SimWorld& w) {
+        std::vector<char> target(w.desc.mats.size(), 0);
+        bool any = false;
+        for (size_t m = 0; m < w.desc.mats.size(); m++) any |= (target[m] = w.desc.mats[m].is_target ? 1 : 0) != 0;
+        if (!any) return 0;
         int n = 0;
-        for (int i = 0; i < w.nv; i++) n += w.desc.mats[w.desc.voxels[4 * i + 3]].is_target ? 1 : 0;
+        for (int i = 0; i < w.nv; i++) n += target[(size_t)w.desc.voxels[4 * i + 3]];
         return n;
     }
 
@@ -627,6 +647,20 @@ public:
     }
 
     int add_sims(const SimDesc* const* descs, int n, int64_t* ids, std::string* errs) override {
+        return add_sims_with(n, [&](int i, SimRec* r, std::string* e) { return prepare(*descs[i], r, e); }, ids, errs);
+    }
+
+    int add_sims_read(int n, const std::function<bool(int, SimDesc*, std::string*)>& read, int64_t* ids,
+                      std::string* errs) override {
+        return add_sims_with(n, [&](int i, SimRec* r, std::string* e) {
+            SimDesc d;
+            return read(i, &d, e) && prepare(d, r, e);
+        }, ids, errs);
+    }
+
+    // make(i, rec, err) prepares simulation i's record on one of the host threads
+    template <typename Make>
+    int add_sims_with(int n, const Make& make, int64_t* ids, std::string* errs) {
         TraceClock tc;
         std::vector<std::unique_ptr<SimRec>> recs((size_t)std::max(n, 0));
         std::vector<char> ok((size_t)std::max(n, 0), 0);
@@ -634,7 +668,7 @@ public:
         auto work = [&]() {
             for (int i = next++; i < n; i = next++) {
                 recs[i] = std::make_unique<SimRec>();
-                ok[i] = prepare(*descs[i], recs[i].get(), &errs[i]) ? 1 : 0;
+                ok[i] = make(i, recs[i].get(), &errs[i]) ? 1 : 0;
             }
         };
         const int nt = std::max(1, std::min(n, (int)std::thread::hardware_concurrency()));
@@ -1039,6 +1073,7 @@ public:
     // on host threads into one pinned generation buffer, then the copies in order.  Returns
     // the number begun (those before a failure) through *begun.
     int upload_many(const std::vector<SimRec*>& rs, std::vector<SimRec*>* begun, std::string* err) {
+        TraceClock tc;
         std::vector<UpPlan> plans(rs.size());
         std::vector<size_t> at(rs.size());
         size_t total = 0;
@@ -1082,7 +1117,6 @@ public:
             }
             return rc;
         }
-        TraceClock tc;
         tc.mark("upload_many: reserve");
         // the images, then the list of region copies, in one pinned buffer and one copy to a
         // device staging buffer; one kernel then places every image and clears the rest of
@@ -1361,12 +1395,21 @@ public:
             n_batch_ = (int)slots.size();
             if (n_batch_ > cap_batch_) {
                 cudaFree(d_batch_slots_);
+                cudaFree(d_batch_items_);
+                d_batch_items_ = nullptr;
                 cap_batch_ = std::max(n_batch_, 2 * cap_batch_);
                 CK(cudaMalloc(&d_batch_slots_, sizeof(int) * cap_batch_));
+                CK(cudaMalloc(&d_batch_items_, sizeof(int2) * cap_batch_));
             }
-            batch_slots_host_ = slots;   // kept alive for the asynchronous copy
-            if (n_batch_)
+            batch_slots_host_ = slots;   // kept alive for the asynchronous copies
+            batch_items_host_.resize(slots.size());
+            for (size_t i = 0; i < slots.size(); i++) batch_items_host_[i] = make_int2(ctl_items[i].second, ctl_items[i].first);
+            if (n_batch_) {
                 CK(copy_async(d_batch_slots_, batch_slots_host_.data(), sizeof(int) * n_batch_, cudaMemcpyHostToDevice, stream_));
+                CK(copy_async(d_batch_items_, batch_items_host_.data(), sizeof(int2) * n_batch_, cudaMemcpyHostToDevice, stream_));
+                k_set_batch_items<<<(n_batch_ + 255) / 256, 256, 0, stream_>>>(d_ctl_, d_batch_slots_, d_batch_items_, n_batch_);
+                CK(cudaGetLastError());
+            }
         }
         if ((int)items.size() > cap_items_) {
             cudaFree(d_items_);
@@ -1383,14 +1426,6 @@ public:
         if (n_attach_) {
             attach_slots_host_ = attach_slots;   // kept alive for the asynchronous copy
             CK(copy_async(d_attach_slots_, attach_slots_host_.data(), sizeof(int) * n_attach_, cudaMemcpyHostToDevice, stream_));
-        }
-        for (size_t i = 0; i < slots.size(); i++) {
-            int vals[2] = {ctl_items[i].second, ctl_items[i].first};   // n_vox_items, item_begin
-            CK(copy_async(&d_ctl_[slots[i]].n_vox_items, vals, sizeof(vals), cudaMemcpyHostToDevice, stream_));
-            static const int zero = 0;
-            CK(copy_async(&d_ctl_[slots[i]].done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
-            if (slot_owner_[slots[i]]->w.desc.enable_signals)
-                CK(copy_async(&d_ctl_[slots[i]].sig_done_items, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_));
         }
         CK(cudaMemsetAsync(d_tickets_, 0, kTickets * sizeof(int), stream_));
         return 0;
@@ -1805,38 +1840,51 @@ public:
     }
     int pending() const override { return (int)(queue_.size() + active_.size()); }
 
-    // Serving policy: the order queued requests are admitted in (first come first served, or
-    // the least work — voxels x horizon steps — first) and the voxels the running batch may
-    // hold (0: as many as the HBM budget allows; the first request is always admitted).
+    // Serving policy: the order queued requests are admitted in (first come first served; the
+    // least work — voxels x horizon steps — first; or the least work first beside one lane for
+    // the most work queued) and the voxels the running batch may hold (0: as many as the HBM
+    // budget allows; the first request is always admitted; the lane's request is not counted).
     int serve_order_ = 0;
     int64_t serve_max_voxels_ = 0;
+    int64_t lane_id_ = -1;   // the request running in the lane of order 2, or -1
     int set_serving(int order, int64_t max_active_voxels) override {
-        if (order < 0 || order > 1 || max_active_voxels < 0) return -6;
+        if (order < 0 || order > 2 || max_active_voxels < 0) return -6;
         serve_order_ = order;
         serve_max_voxels_ = max_active_voxels;
         return 0;
+    }
+    double serve_work(int64_t id) {
+        SimRec* a = find(id);
+        return a ? (double)a->w.nv * (double)(a->horizon > 0 ? a->horizon : 1000000) : 0;
     }
 
     int poll(SimResult* out, int max, int chunk, std::string* err) override {
         // admit while the HBM budget (and the voxel cap) allows, in the policy's order; the
         // uploads of everything admitted now are finished together
         std::vector<SimRec*> begun, admitted;
-        int64_t active_voxels = 0;
-        for (int64_t id : active_) if (SimRec* a = find(id)) active_voxels += a->w.nv;
-        if (serve_order_ == 1 && queue_.size() > 1) {
+        if (serve_order_ != 2 || (lane_id_ >= 0 && std::find(active_.begin(), active_.end(), lane_id_) == active_.end()))
+            lane_id_ = -1;
+        int64_t active_voxels = 0;   // of the running batch, the lane's request left out
+        for (int64_t id : active_)
+            if (SimRec* a = find(id)) active_voxels += id == lane_id_ ? 0 : a->w.nv;
+        bool lane_first = false;
+        if (serve_order_ >= 1 && queue_.size() > 1) {
             // least work first; ties keep their arrival order
-            std::stable_sort(queue_.begin(), queue_.end(), [&](int64_t x, int64_t y) {
-                SimRec* a = find(x);
-                SimRec* b = find(y);
-                const double wa = a ? (double)a->w.nv * (double)(a->horizon > 0 ? a->horizon : 1000000) : 0;
-                const double wb = b ? (double)b->w.nv * (double)(b->horizon > 0 ? b->horizon : 1000000) : 0;
-                return wa < wb;
-            });
+            std::stable_sort(queue_.begin(), queue_.end(), [&](int64_t x, int64_t y) { return serve_work(x) < serve_work(y); });
+        }
+        if (serve_order_ == 2 && lane_id_ < 0 && !queue_.empty()) {
+            // the lane is free: the request with the most work goes first, so that the longest
+            // runs overlap the short ones instead of running alone at the end
+            const int64_t big = queue_.back();
+            queue_.pop_back();
+            queue_.push_front(big);
+            lane_first = true;
         }
         while (!queue_.empty()) {
             SimRec* r = find(queue_.front());
-            if (!r) { queue_.pop_front(); continue; }
-            if (serve_max_voxels_ > 0 && !(active_.empty() && admitted.empty()) &&
+            if (!r) { queue_.pop_front(); lane_first = false; continue; }
+            const bool in_lane = lane_first && admitted.empty();
+            if (!in_lane && serve_max_voxels_ > 0 && !(active_.empty() && admitted.empty()) &&
                 active_voxels + r->w.nv > serve_max_voxels_)
                 break;
             std::string e2;
@@ -1849,7 +1897,8 @@ public:
             if (e) { upload_finish(begun, err); *err = e2; return e; }
             if (fresh) begun.push_back(r);
             admitted.push_back(r);
-            active_voxels += r->w.nv;
+            if (in_lane) lane_id_ = r->id;
+            else active_voxels += r->w.nv;
             queue_.pop_front();
             r->start_s = now_s() - t0_;
             active_.push_back(r->id);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -59,6 +60,10 @@ public:
     // Many at once: topology and materials are built on host threads; ids[i] = -1 and
     // errs[i] set where descs[i] is rejected.  Returns the number rejected.
     virtual int add_sims(const SimDesc* const* descs, int n, int64_t* ids, std::string* errs) = 0;
+    // The same, with each description made on the host thread that builds it: read(i, &d,
+    // &err) fills simulation i's description or returns false with the reason.
+    virtual int add_sims_read(int n, const std::function<bool(int, SimDesc*, std::string*)>& read, int64_t* ids,
+                              std::string* errs) = 0;
     virtual int set_external(int64_t id, const External& x, std::string* err) = 0;
     // Advance the given simulations by exactly `steps` steps each (fewer if they stop).
     virtual int step(const int64_t* ids, int n, int mode, int64_t steps, std::string* err) = 0;

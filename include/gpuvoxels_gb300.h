@@ -115,11 +115,15 @@ int vx3_poll(vx3_ctx* ctx, vx3_result* out, int max, int chunk_steps);
 int vx3_pending(vx3_ctx* ctx);
 /* Serving policy of vx3_poll's admission (no reference counterpart): order 0 admits queued
  * simulations first come first served (the default), 1 the least work first (voxels x horizon
- * steps; ties in arrival order; under a never-ending stream long requests may wait indefinitely);
- * max_active_voxels caps the voxels the running batch holds (0 = as the HBM budget allows; a
- * request is always admitted into an empty batch). */
+ * steps; ties in arrival order; under a never-ending stream long requests may wait indefinitely),
+ * 2 the least work first beside one lane: whenever no request is running in the lane, the queued
+ * request with the most work is admitted into it first, so that the longest requests overlap the
+ * short ones rather than run alone at the end; max_active_voxels caps the voxels the running
+ * batch holds (0 = as the HBM budget allows; a request is always admitted into an empty batch;
+ * the lane's request is not counted). */
 #define VX3_SERVE_FCFS 0
 #define VX3_SERVE_LEAST_WORK 1
+#define VX3_SERVE_LONG_LANE 2
 int vx3_set_serving(vx3_ctx* ctx, int order, int64_t max_active_voxels);
 
 /* Replaces VX3_SimulationManager::collectResults for one simulation (VX3_SimulationManager.cu:416-458). */

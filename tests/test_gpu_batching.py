@@ -180,8 +180,9 @@ def _serve_all(order, cap, creatures, horizons, chunk=32):
 
 
 def test_serving_policies_change_order_not_results():
-    """Least-work-first admission under a voxel cap finishes the small jobs first; every
-    simulation's result is bit-identical to first-come-first-served admission."""
+    """Least-work-first admission under a voxel cap finishes the small jobs first; with the lane
+    for the longest, the request with the most work starts first; every simulation's result is
+    bit-identical to first-come-first-served admission."""
     cs = sorted(synth.config1_batch(6, seed=41, sim_time=10.0), key=lambda c: c.num_voxel)[::-1]
     horizons = [600, 500, 400, 300, 200, 100]    # the larger creatures run longer: work order = arrival order reversed
     cap = max(c.num_voxel for c in cs) + min(c.num_voxel for c in cs)   # about two at a time
@@ -189,11 +190,15 @@ def test_serving_policies_change_order_not_results():
     lw, done = _serve_all(g.SERVE_LEAST_WORK, cap, cs, horizons)
     work = [c.num_voxel * h for c, h in zip(cs, horizons)]
     assert done[0] == int(np.argmin(work))
+    lane, done_lane = _serve_all(g.SERVE_LONG_LANE, cap, cs, horizons)
+    big = int(np.argmax(work))
+    assert all(lane[big].start_time_s <= lane[k].start_time_s for k in range(len(cs)))
+    assert done_lane[0] == int(np.argmin(work))
     for k in range(len(cs)):
-        a, b = fcfs[k], lw[k]
-        assert a.steps == b.steps == horizons[k]
-        assert list(a.current_center_of_mass) == list(b.current_center_of_mass)
-        assert a.total_distance_of_all_voxels == b.total_distance_of_all_voxels
+        a, b, c = fcfs[k], lw[k], lane[k]
+        assert a.steps == b.steps == c.steps == horizons[k]
+        assert list(a.current_center_of_mass) == list(b.current_center_of_mass) == list(c.current_center_of_mass)
+        assert a.total_distance_of_all_voxels == b.total_distance_of_all_voxels == c.total_distance_of_all_voxels
     with g.Context(0, 1 << 30) as c:
         with pytest.raises(g.VX3Error):
-            c.set_serving(2, 0)
+            c.set_serving(3, 0)
