@@ -1584,7 +1584,10 @@ public:
                 batch_dirty_ = false;
                 tc.mark("drive: build_items");
             }
-            if (!graph_) {
+            // a graph is captured only when a whole one will run: fewer steps than a graph holds
+            // go out as single launches (a capture the GPU waits for would cost more)
+            const bool use_graph = exact_steps_ < 0 ? !profiling_ : (!profiling_ && exact_steps_ >= graph_steps_);
+            if (!graph_ && use_graph) {
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
                 bins_dirty_ = true;   // every replay starts by regrouping the links
@@ -1602,7 +1605,7 @@ public:
                 // a known step count: whole graphs, then single steps for the remainder, no polling
                 int64_t left = exact_steps_;
                 while (left > 0) {
-                    if (!profiling_ && left >= graph_len_) {
+                    if (graph_ && !profiling_ && left >= graph_len_) {
                         CK(cudaGraphLaunch(graph_, stream_));
                         timing_.launches += graph_launches_;
                         left -= graph_len_;

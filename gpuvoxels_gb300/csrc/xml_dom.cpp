@@ -64,26 +64,28 @@ struct Parser {
     void skip_ws() { while (i < s.size() && isspace((unsigned char)s[i])) i++; }
     bool fail(const std::string& m) { if (err.empty()) err = m + " at offset " + std::to_string(i); return false; }
 
-    static std::string decode(const std::string& in) {
-        std::string out;
-        out.reserve(in.size());
+    // appends the text s[b, e) to out with its entity references replaced
+    void decode_into(size_t b, size_t e, std::string* out) const {
+        const char* amp = (const char*)memchr(s.data() + b, '&', e - b);
+        if (!amp) { out->append(s, b, e - b); return; }   // the usual case: no references
+        const std::string in = s.substr(b, e - b);
+        out->reserve(out->size() + in.size());
         for (size_t k = 0; k < in.size(); k++) {
-            if (in[k] != '&') { out += in[k]; continue; }
+            if (in[k] != '&') { *out += in[k]; continue; }
             size_t semi = in.find(';', k);
-            if (semi == std::string::npos) { out += in[k]; continue; }
+            if (semi == std::string::npos) { *out += in[k]; continue; }
             std::string ent = in.substr(k + 1, semi - k - 1);
-            if (ent == "lt") out += '<';
-            else if (ent == "gt") out += '>';
-            else if (ent == "amp") out += '&';
-            else if (ent == "quot") out += '"';
-            else if (ent == "apos") out += '\'';
+            if (ent == "lt") *out += '<';
+            else if (ent == "gt") *out += '>';
+            else if (ent == "amp") *out += '&';
+            else if (ent == "quot") *out += '"';
+            else if (ent == "apos") *out += '\'';
             else if (!ent.empty() && ent[0] == '#') {
                 long code = ent.size() > 1 && (ent[1] == 'x' || ent[1] == 'X') ? strtol(ent.c_str() + 2, nullptr, 16) : strtol(ent.c_str() + 1, nullptr, 10);
-                if (code > 0 && code < 128) out += (char)code;
-            } else { out += '&'; continue; }
+                if (code > 0 && code < 128) *out += (char)code;
+            } else { *out += '&'; continue; }
             k = semi;
         }
-        return out;
     }
     bool skip_misc() {  // comments, declarations, processing instructions
         for (;;) {
@@ -107,7 +109,7 @@ struct Parser {
         size_t b = i;
         while (i < s.size() && (isalnum((unsigned char)s[i]) || s[i] == '_' || s[i] == '-' || s[i] == ':' || s[i] == '.')) i++;
         if (i == b) return fail("expected a name");
-        *out = s.substr(b, i - b);
+        out->assign(s, b, i - b);
         return true;
     }
     bool element(XmlNode* n, int depth) {
@@ -133,7 +135,8 @@ struct Parser {
             char q = s[i++];
             size_t e = s.find(q, i);
             if (e == std::string::npos) return fail("unterminated attribute");
-            n->attrs.emplace_back(an, decode(s.substr(i, e - i)));
+            n->attrs.emplace_back(std::move(an), std::string());
+            decode_into(i, e, &n->attrs.back().second);
             i = e + 1;
         }
         for (;;) {
@@ -150,7 +153,7 @@ struct Parser {
             } else if (starts("<![CDATA[")) {
                 size_t e = s.find("]]>", i);
                 if (e == std::string::npos) return fail("unterminated CDATA");
-                n->text += s.substr(i + 9, e - i - 9);
+                n->text.append(s, i + 9, e - i - 9);
                 i = e + 3;
             } else if (starts("<!--")) {
                 size_t e = s.find("-->", i);
@@ -167,7 +170,7 @@ struct Parser {
             } else {
                 size_t e = s.find('<', i);
                 if (e == std::string::npos) e = s.size();
-                n->text += decode(s.substr(i, e - i));
+                decode_into(i, e, &n->text);
                 i = e;
             }
         }

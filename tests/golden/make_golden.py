@@ -83,6 +83,15 @@ def worlds():
           "<DisplaceZ>0.002</DisplaceZ><ForceY>0.1</ForceY></FRegion></Boundary_Conditions>")
     vxa = synth.config0_creature(0).vxa.replace("<Boundary_Conditions><NumBCs>0</NumBCs></Boundary_Conditions>", bc)
     w["bc_regions"] = dict(vxa=vxa, ext=[], snaps=[1, 300, 1000])
+    # the smallest worlds: one voxel (no link: the time step from the voxel's own frequency),
+    # dropped on the floor and pushed sideways (contact, static then kinetic friction)
+    one = np.ones((1, 1, 1), np.int32)
+    vxa = grid_world(one, [STIFF], vary_temp=False)
+    w["single_voxel"] = dict(vxa=vxa, ext=[dict(voxel=0, force=(0.009, 0.002, 0.0))], snaps=[1, 400, 1500])
+    # two voxels and one link, actuated (a thermal material beside a passive one)
+    pair = np.array([[[1, 2]]], np.int32)
+    vxa = grid_world(pair, [dict(SOFT, cte=0.01), STIFF])
+    w["one_link"] = dict(vxa=vxa, ext=[], snaps=[1, 400, 1500])
     return w
 
 

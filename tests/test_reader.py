@@ -92,6 +92,19 @@ def test_vxd_overrides_structure():
     assert p["voxels"][:, 3].tolist() == [0, 1]
 
 
+def test_entity_references_and_cdata_are_read():
+    """Character and entity references in text and attributes are replaced (tinyxml's reading),
+    CDATA is taken as it stands."""
+    base = synth.config0_creature(0).vxa
+    vxd = ("<VXD><Structure replace=\"VXA.VXC.Structure\" Compression=\"ASCII_READABL&#69;\"><X_Voxels>&#50;</X_Voxels>"
+           "<Y_Voxels>1</Y_Voxels><Z_Voxels>1</Z_Voxels><Data><Layer><![CDATA[12]]></Layer></Data></Structure>"
+           "<Lattice replace=\"VXA.VXC.Lattice\"><Lattice_Dim>0.0&#x32;</Lattice_Dim></Lattice>"
+           "<DtFrac replace=\"VXA.Simulator.Integration.DtFrac\">0.&#55;5</DtFrac></VXD>")
+    p = g.inspect_vxa(base, vxd)
+    assert p["counts"]["voxels"] == 2 and p["counts"]["links"] == 1
+    assert p["env"]["vox_size"] == 0.02 and p["env"]["dt_frac"] == 0.75
+
+
 def test_formula_evaluation():
     vxa = synth.config0_creature(0, stop_time=0.25).vxa
     vars9 = [0.1, 0.2, 0.3, 0, 0.3, 0, 0, 0, 100]
