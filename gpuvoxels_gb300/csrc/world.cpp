@@ -470,11 +470,16 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
         have_phase = true;
         auto pl = po->children_named("Layer");
         for (int k = 0; k < Z; k++) {
-            std::vector<const char*> arr;   // start of each comma-separated field, read in place
-            const char* end = nullptr;
-            if (k < (int)pl.size()) { comma_fields(pl[k]->text, &arr); end = pl[k]->text.c_str() + pl[k]->text.size(); }
-            for (int j = 0; j < X * Y; j++)
-                if (cells[(size_t)k * X * Y + j] > 0) phase_by_voxel.push_back(j < (int)arr.size() ? field_atof(arr[j], end) : 0.0);
+            // the comma-separated fields read in place, one pass; cells past the last field read 0
+            const char* p = k < (int)pl.size() ? pl[k]->text.c_str() : nullptr;
+            const char* end = p ? p + pl[k]->text.size() : nullptr;
+            for (int j = 0; j < X * Y; j++) {
+                if (cells[(size_t)k * X * Y + j] > 0) phase_by_voxel.push_back(p ? field_atof(p, end) : 0.0);
+                if (p) {
+                    const char* c = (const char*)memchr(p, ',', (size_t)(end - p));
+                    p = c ? c + 1 : nullptr;
+                }
+            }
         }
     }
     /* BaseCiliaForce and ShiftCiliaForce: per filled cell an x,y,z triple, layer by layer; a
@@ -494,23 +499,25 @@ bool parse_vxa(const std::string& base_xml, const char* vxd_xml, SimDesc* d, std
     };
     if (const XmlNode* bcf = st->child("BaseCiliaForce")) read_triples(bcf, &d->base_cilia);
     if (const XmlNode* scf = st->child("ShiftCiliaForce")) read_triples(scf, &d->shift_cilia);
-    int n = 0;
+    // voxels in structure order (x fastest), with their lattice indices and material
+    size_t filled = 0;
+    for (uint8_t c : cells) filled += (signed char)c > 0;
+    d->voxels.resize(4 * filled);
+    d->phase.resize(filled);
     {
-        size_t filled = 0;
-        for (uint8_t c : cells) filled += (signed char)c > 0;
-        d->voxels.reserve(4 * filled);
-        d->phase.reserve(filled);
-    }
-    for (long i = 0; i < (long)X * Y * Z; i++) {
-        int mi = (int)(signed char)cells[i] - 1;
-        if (mi < 0) continue;
-        if (mi >= (int)d->mats.size()) { *err = "voxel references a material missing from the palette"; return false; }
-        d->voxels.push_back((int32_t)(i % X));
-        d->voxels.push_back((int32_t)((i / X) % Y));
-        d->voxels.push_back((int32_t)(i / ((long)X * Y)));
-        d->voxels.push_back(mi);
-        d->phase.push_back(have_phase ? phase_by_voxel[n] : 0.0);
-        n++;
+        const int nm = (int)d->mats.size();
+        size_t n = 0, i = 0;
+        for (int z = 0; z < Z; z++)
+            for (int y = 0; y < Y; y++)
+                for (int x = 0; x < X; x++, i++) {
+                    const int mi = (int)(signed char)cells[i] - 1;
+                    if (mi < 0) continue;
+                    if (mi >= nm) { *err = "voxel references a material missing from the palette"; return false; }
+                    int32_t* v = &d->voxels[4 * n];
+                    v[0] = x; v[1] = y; v[2] = z; v[3] = mi;
+                    d->phase[n] = have_phase ? phase_by_voxel[n] : 0.0;
+                    n++;
+                }
     }
     if (!apply_boundary_conditions(root.get(), vxc, X, Y, Z, cells, d, err)) return false;
     /* VX3 keys, Voxelyze3/src/VX3/VX3_SimulationManager.cu:326-367 */
