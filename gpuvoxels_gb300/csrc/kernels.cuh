@@ -85,27 +85,30 @@ __device__ __forceinline__ void beam_forces(const LMat& m, double fx, const d3& 
 }
 
 // CVX_Link::updateForces with orientLink, updateStrain and updateTransverseInfo
-// (Voxelyze3/src/old/VX_Link.cpp:72-113, 136-141, 143-241).  Writes the two
-// end forces/moments and axial strains into the voxels' direction slots.
-__device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool* diverged) {
+// (Voxelyze3/src/old/VX_Link.cpp:72-113, 136-141, 143-241), in two parts: link_orient
+// (orientLink up to the small/large-angle hysteresis test) and link_finish (the rest),
+// which writes the two end forces/moments and axial strains into the voxels' direction
+// slots.  A link's pose in its own frame and its mode for this step:
+struct LinkOrient {
+    d3 pos2;          // positive end relative to the negative end, in the negative end's frame on +x
+    q4 angle2;        // positive end's orientation in that frame
+    double restLen;   // CVX_Link::updateRestLength
+    bool small, lvv;  // small-angle mode and valid previous state for this step
+};
+
+// False for a link that is not updated (detached or removed, or between two Fixed voxels).
+__device__ __forceinline__ bool link_orient(const Sim& S, int l, LinkOrient* out) {
     const int ng = __ldg(S.lneg + l), pv = __ldg(S.lpos + l);
     const int axis = __ldg(S.lax + l);
-    const LMat& m = S.lm[__ldg(S.lmt + l)];
     const VMat& vN = S.vm[__ldg(S.vmat + ng)];
     const VMat& vP = S.vm[__ldg(S.vmat + pv)];
-    uint8_t fl = S.lfl[l];
+    const uint8_t fl = S.lfl[l];
     // VX3 extras: detached and removed links are no longer updated (VX3_VoxelyzeKernel.cu:565-575),
     // nor are links between two voxels of Fixed materials
-    if (fl & LF_GONE) return;
-    if ((S.flags & SF_FIXEDMAT) && (vN.vx3 & vP.vx3 & VM_FIXED)) return;
+    if (fl & LF_GONE) return false;
+    if ((S.flags & SF_FIXEDMAT) && (vN.vx3 & vP.vx3 & VM_FIXED)) return false;
     const float tN = S.temp[ng], tP = S.temp[pv];
     const double restLen = half(base_size(vN, tN) + base_size(vP, tP));   // CVX_Link::updateRestLength
-    const int nl = S.nl;
-    double* st = S.lst;
-    const d3 o2 = D3(st[l], st[nl + l], st[2 * nl + l]);
-    const d3 oa1 = D3(st[3 * nl + l], st[4 * nl + l], st[5 * nl + l]);
-    const d3 oa2 = D3(st[6 * nl + l], st[7 * nl + l], st[8 * nl + l]);
-    float strain = S.lsf[l], maxStrain = S.lsf[nl + l], strainOffset = S.lsf[2 * nl + l];
     bool small = fl & LF_SMALL, lvv = fl & LF_LVV;
 
     // orientLink
@@ -115,7 +118,6 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
     const q4 tr = Q4(angle1.w, -angle1.x, -angle1.y, -angle1.z);
     pos2 = qrot(tr, pos2);
     angle2 = qmul(tr, angle2);
-    angle1 = Q4(1, 0, 0, 0);
     // SmallTurn = (float)((|z|+|y|)/x), ExtendPerc = (float)|1 - x/restLength|, compared with the
     // hysteresis thresholds (VX_Link.cpp:85-94); decided without dividing unless near a threshold
     const double turnNum = fabs(pos2.z) + fabs(pos2.y);
@@ -125,6 +127,28 @@ __device__ __forceinline__ void link_update(const Sim& S, int l, float dt, bool*
         small = false;
         lvv = false;
     }
+    out->pos2 = pos2; out->angle2 = angle2; out->restLen = restLen; out->small = small; out->lvv = lvv;
+    return true;
+}
+
+// The rest of CVX_Link::updateForces for a link oriented by link_orient.
+__device__ __forceinline__ void link_finish(const Sim& S, int l, float dt, const LinkOrient& lo, bool* diverged) {
+    const int ng = __ldg(S.lneg + l), pv = __ldg(S.lpos + l);
+    const int axis = __ldg(S.lax + l);
+    const LMat& m = S.lm[__ldg(S.lmt + l)];
+    const VMat& vN = S.vm[__ldg(S.vmat + ng)];
+    const VMat& vP = S.vm[__ldg(S.vmat + pv)];
+    const double restLen = lo.restLen;
+    const int nl = S.nl;
+    double* st = S.lst;
+    const d3 o2 = D3(st[l], st[nl + l], st[2 * nl + l]);
+    const d3 oa1 = D3(st[3 * nl + l], st[4 * nl + l], st[5 * nl + l]);
+    const d3 oa2 = D3(st[6 * nl + l], st[7 * nl + l], st[8 * nl + l]);
+    float strain = S.lsf[l], maxStrain = S.lsf[nl + l], strainOffset = S.lsf[2 * nl + l];
+    bool small = lo.small, lvv = lo.lvv;
+    d3 pos2 = lo.pos2;
+    q4 angle2 = lo.angle2;
+    q4 angle1 = Q4(1, 0, 0, 0);
     d3 a1v;
     bool wide1 = false, acos1 = false, wide2 = false;   // branches taken, kept as the next step's ordering key
     if (small) {
@@ -466,30 +490,89 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sim
 }
 
 // Warps take chunks of `claim` consecutive links of the binned list (one atomic per
-// chunk; claim is a multiple of 32, so each lane updates claim/32 links of whatever
-// simulations they belong to).
+// chunk; claim is a multiple of 32) and update them 32 at a time, one per lane.
+// The grouping keys come from the previous step, so a link that changes between small-
+// and large-angle mode this step sits among links of the other mode, and its warp would
+// run both paths (on GB300 the FP64 pipe spends the same cycles on a warp instruction
+// whatever its active lanes).  So each round first orients the 32 links and decides their
+// modes; the minority mode waits in the warp's queue for that mode (its links' ids only)
+// while the majority finishes, and a queue that holds 32 links is run as one full round of
+// a single mode: its links are oriented again (the same inputs give the same pose and
+// mode) and finished.  What is left in the queues at the end runs in one last round per
+// mode.  Every link still writes only its own state and its two direction slots, so the
+// order changes no result.
+constexpr int kLinkDefer = 48;   // a queue holds at most 31 + 16 links between rounds
 __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
                                                                      const int* __restrict__ total, int cap, int n_slots, int* tickets,
                                                                      int claim) {
+    __shared__ int2 s_defer[GVX_STEP_BLOCK / 32][2][kLinkDefer];   // per warp: large-angle (0), small-angle (1)
     // this step's queues of the kernels that follow, and the contact spill pool's records
     if (blockIdx.x == 0 && threadIdx.x == 0) { tickets[1] = 0; tickets[2] = 0; tickets[3] = 0; tickets[4] = 0; }
     const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    int2* q0 = s_defer[threadIdx.x >> 5][0];
+    int2* q1 = s_defer[threadIdx.x >> 5][1];
+    int qn0 = 0, qn1 = 0;        // links waiting in each queue (the same in every lane)
+    int kb = 0, k1 = 0;          // the claimed chunk: next round's first link, its end
+    bool more = true;            // chunks may remain
     for (;;) {
-        int chunk = 0;
-        if (lane == 0) chunk = atomicAdd(&tickets[0], 1);
-        chunk = __shfl_sync(0xffffffffu, chunk, 0);
-        const int k0 = chunk * claim;
-        if (k0 >= n) break;
-        const int k1 = min(n, k0 + claim);
-        for (int k = k0 + lane; k < k1; k += 32) {
-            const int2 e = __ldg(perm + k);
-            if ((unsigned)e.x >= (unsigned)n_slots) continue;   // never: the grouping lists running slots
+        // this round's links: a full queue, else the claimed chunk (claiming one when it is
+        // used up), else what the queues hold at the end
+        int src, cnt = 32;       // src: -1 the chunk, 0 / 1 a queue
+        if (qn0 >= 32) src = 0;
+        else if (qn1 >= 32) src = 1;
+        else {
+            if (kb >= k1 && more) {
+                int chunk = 0;
+                if (lane == 0) chunk = atomicAdd(&tickets[0], 1);
+                chunk = __shfl_sync(0xffffffffu, chunk, 0);
+                kb = chunk * claim;
+                k1 = min(n, kb + claim);
+                if (kb >= n) more = false;
+            }
+            if (kb < k1) src = -1;
+            else if (qn0 > 0) { src = 0; cnt = qn0; }
+            else if (qn1 > 0) { src = 1; cnt = qn1; }
+            else break;
+        }
+        int2 e = make_int2(-1, -1);
+        if (src < 0) {
+            if (kb + lane < k1) e = __ldg(perm + kb + lane);
+            kb += 32;
+        } else {
+            int2* q = src ? q1 : q0;
+            const int left = (src ? qn1 : qn0) - cnt;   // at most 15 after a full round, else 0
+            if (lane < cnt) e = q[lane];
+            __syncwarp();
+            if (lane < left) q[lane] = q[cnt + lane];
+            __syncwarp();
+            if (src) qn1 = left; else qn0 = left;
+        }
+        // e.x >= n_slots never happens (the grouping lists running slots); a simulation may
+        // have stopped since the grouping was made
+        bool act = e.x >= 0 && (unsigned)e.x < (unsigned)n_slots && ctl[e.x].status == 1 && (unsigned)e.y < (unsigned)sims[e.x].nl;
+        LinkOrient o;
+        act = act && link_orient(sims[e.x], e.y, &o);
+        if (src < 0) {
+            const unsigned am = __ballot_sync(0xffffffffu, act), sm = __ballot_sync(0xffffffffu, act && o.small);
+            const bool major_small = 2 * __popc(sm) >= __popc(am);
+            const bool defer = act && o.small != major_small;
+            const unsigned dm = __ballot_sync(0xffffffffu, defer);
+            if (dm) {
+                // the deferred lanes' mode is the other one: small when the majority is large
+                int2* q = major_small ? q0 : q1;
+                const int at = major_small ? qn0 : qn1;
+                if (defer) q[at + __popc(dm & below)] = e;
+                if (major_small) qn0 += __popc(dm); else qn1 += __popc(dm);
+                __syncwarp();
+            }
+            act = act && !defer;
+        }
+        if (act) {
             Ctl& c = ctl[e.x];
-            if (c.status != 1) continue;   // stopped since the grouping was made
-            if ((unsigned)e.y >= (unsigned)sims[e.x].nl) continue;
             bool div = false;
-            link_update(sims[e.x], e.y, c.dt, &div);
+            link_finish(sims[e.x], e.y, c.dt, o, &div);
             if (div) c.diverged = 1;
         }
     }
