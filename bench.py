@@ -62,18 +62,31 @@ def measured_peaks():
 
 
 # FP64-pipe thread instructions (DADD/DMUL/DFMA, compares, conversions; predicated-on lanes)
-# per link (k_links) and per voxel (k_voxels) of one step, read by ncu per workload
-# (sm__thread_inst_executed_pipe_fp64_pred_on.sum / links or voxels), and DRAM bytes per
-# link of one k_links launch (dram__bytes_read.sum + dram__bytes_write.sum / links).
-# Sources: profiles/k_links_k_voxels_batch512_fp64_mix.md (batch, step 201).
+# per link (k_links) and per voxel (k_voxels) of one step, read by ncu per workload in the
+# steps the workload's value is timed over (sm__thread_inst_executed_pipe_fp64_pred_on.sum /
+# links or voxels); the lanes a warp's FP64 instruction keeps busy on average (that sum /
+# sm__inst_executed_pipe_fp64.sum: the pipe costs the same per warp instruction whatever
+# its active lanes); and DRAM bytes per link of one k_links launch (dram__bytes_read.sum +
+# dram__bytes_write.sum / links).  profiles/fp64_counts_by_workload.md has the captures.
 FP64_COUNTS = {
-    "batch": dict(per_link=672121856 / 1627115, per_voxel=199437824 / 844972,
-                  traffic_per_link=(409993728 + 359042560) / 1627115, source="ncu, 512-creature batch, step 201"),
-    # profiles/fp64_counts_collide_slab.md: 8 of the 64 collision creatures and a 100x100x50 slab, step 201
-    "collide": dict(per_link=156123968 / 373621, per_voxel=60842368 / 249183,
-                    traffic_per_link=(111591680 + 71004928) / 373621, source="ncu, 8 collision creatures 40^3, step 201"),
-    "slab": dict(per_link=732160544 / 1480000, per_voxel=117621120 / 500000,
-                 traffic_per_link=(193994496 + 228061696) / 1480000, source="ncu, 100x100x50 slab, step 201"),
+    # batch of 512 creatures, step 288 (the settled window the line's value is timed over)
+    "batch": dict(per_link=655165600 / 1627115, per_voxel=195889184 / 844972,
+                  lanes_link=655165600 / 21707472, lanes_voxel=195889184 / 6829054,
+                  traffic_per_link=764864000 / 1627115, source="ncu, 512-creature batch, step 288"),
+    # 8 of the 64 collision creatures, mean of steps 201, 1001 and 1901 (the 2,000 timed steps)
+    "collide": dict(per_link=(149924800 + 139983552 + 137419616) / 3 / 373621,
+                    per_voxel=(64035808 + 59213696 + 58503680) / 3 / 249183,
+                    lanes_link=(149924800 + 139983552 + 137419616) / (5079772 + 4651183 + 4567875),
+                    lanes_voxel=(64035808 + 59213696 + 58503680) / (2291351 + 2149824 + 2144277),
+                    traffic_per_link=(180225280 + 181382912 + 181297408) / 3 / 373621,
+                    source="ncu, 8 collision creatures 40^3, mean of steps 201, 1001, 1901"),
+    # a 100x100x50 slab, mean of steps 201, 1001 and 1901
+    "slab": dict(per_link=(695043520 + 694503200 + 694274368) / 3 / 1480000,
+                 per_voxel=(117620192 + 117357888 + 117292448) / 3 / 500000,
+                 lanes_link=(695043520 + 694503200 + 694274368) / (22570878 + 22544145 + 22522796),
+                 lanes_voxel=(117620192 + 117357888 + 117292448) / (3896502 + 3879244 + 3875868),
+                 traffic_per_link=(420665344 + 421070336 + 421153792) / 3 / 1480000,
+                 source="ncu, 100x100x50 slab, mean of steps 201, 1001, 1901"),
 }
 FP64_INSTR_PER_LINK = FP64_COUNTS["batch"]["per_link"]
 FP64_INSTR_PER_VOXEL = FP64_COUNTS["batch"]["per_voxel"]
@@ -288,7 +301,11 @@ def rooflines(ctx, ids, workload, link_ms, con_ms, vox_ms, peak64):
                 "unit": "G FP64 thread-instructions/s", "frac": ach_l / peak64,
                 "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FMA/s)",
                 "instr_per_link": counts["per_link"], "k_voxels_achieved": ach_v / 1e9, "k_voxels_frac": ach_v / peak64,
-                "instr_per_voxel": counts["per_voxel"], "counts_source": counts["source"]}
+                "instr_per_voxel": counts["per_voxel"], "counts_source": counts["source"],
+                # the pipe's issue capacity in use: a warp instruction costs the same with idle lanes
+                "lanes_per_instr": counts["lanes_link"], "pipe_frac": ach_l / peak64 * 32 / counts["lanes_link"],
+                "k_voxels_lanes_per_instr": counts["lanes_voxel"],
+                "k_voxels_pipe_frac": ach_v / peak64 * 32 / counts["lanes_voxel"]}
     traffic = counts["traffic_per_link"] * n_links if (counts and dom == "k_links" and counts.get("traffic_per_link")) else None
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
@@ -474,9 +491,19 @@ def run_ours(args):
         ctx.set_tuning(bl, bv, il, iv, args.graph_steps)
     else:
         ctx.set_tuning(graph_steps=args.graph_steps)
-        if not args.no_autotune:
-            ctx.autotune(ids)                         # launch shape picked on the live batch
+    # a freshly loaded batch's first steps (creatures settling on the floor and starting to
+    # move: many links change angle mode) are timed on their own; the line's value is timed
+    # after `settle_steps` more, in the regime the rest of the run (tens of thousands of
+    # steps for this configuration) stays in
+    fdev_s, fvsteps, _, _, _ = measure_resident(ctx, ids, args.steps, args.warmup, dist, sample_clocks=False, device=local)
+    fdev_s, fvsteps = reduce_timing(dist, fdev_s, fvsteps)
+    fresh = dict(value=fvsteps / fdev_s, ms_per_step=fdev_s * 1e3 / args.steps,
+                 window=f"steps {2 + args.warmup}-{1 + args.warmup + args.steps} of the run, launch shape before tuning")
+    ctx.step(ids, args.settle_steps, g.BATCHED)
+    if not args.tuning and not args.no_autotune:
+        ctx.autotune(ids)                             # launch shape picked on the live batch
     tuning = ctx.tuning()
+    first = 2 + 2 * args.warmup + args.steps + args.settle_steps
     dev_s, vsteps, launches, clocks, wall = measure_resident(ctx, ids, args.steps, args.warmup, dist, device=local)
     dev_s, vsteps = reduce_timing(dist, dev_s, vsteps)
     value = vsteps / dev_s
@@ -552,6 +579,9 @@ def run_ours(args):
         "config": dict(desc, simulations=len(cs) * ws, voxels=n_vox * ws, links=n_links * ws, mode="batched",
                        kernel_build=args.precision, tuning=tuning,
                        tuning_source="vx3_autotune on the live batch" if not (args.tuning or args.no_autotune) else "set",
+                       timed_window=f"steps {first}-{first + args.steps - 1} of the run (after {args.settle_steps} "
+                                    "settling steps; the configuration runs 35,000-56,000)",
+                       fresh_batch=fresh,
                        l2="device state larger than L2; no flush needed", parallelism=f"replicas x{ws} (no collective)"),
         "e2e": e2e,
         "gpu_launches": launches,
@@ -644,6 +674,8 @@ def main():
     ap.add_argument("--slab-dims", default="200,200,100", help="slab size X,Y,Z for --profile-steps (a smaller case for ncu)")
     ap.add_argument("--no-modes", action="store_true", help="skip the serving, collision and single-body blocks")
     ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--settle-steps", type=int, default=256,
+                    help="untimed steps between the fresh-batch window and the timed window of the line's value")
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--graph-steps", type=int, default=64)
     ap.add_argument("--tuning", default="", help="block_links,block_voxels,items_links,items_voxels (0 = keep); skips the autotuner")

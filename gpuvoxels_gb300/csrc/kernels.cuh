@@ -94,6 +94,7 @@ struct LinkOrient {
     q4 angle2;        // positive end's orientation in that frame
     double restLen;   // CVX_Link::updateRestLength
     bool small, lvv;  // small-angle mode and valid previous state for this step
+    bool switched;    // the mode differs from the previous step's
 };
 
 // False for a link that is not updated (detached or removed, or between two Fixed voxels).
@@ -128,6 +129,7 @@ __device__ __forceinline__ bool link_orient(const Sim& S, int l, LinkOrient* out
         lvv = false;
     }
     out->pos2 = pos2; out->angle2 = angle2; out->restLen = restLen; out->small = small; out->lvv = lvv;
+    out->switched = small != ((fl & LF_SMALL) != 0);
     return true;
 }
 
@@ -494,14 +496,21 @@ __global__ void __launch_bounds__(256) k_bin_scatter(const Sim* __restrict__ sim
 // The grouping keys come from the previous step, so a link that changes between small-
 // and large-angle mode this step sits among links of the other mode, and its warp would
 // run both paths (on GB300 the FP64 pipe spends the same cycles on a warp instruction
-// whatever its active lanes).  So each round first orients the 32 links and decides their
-// modes; the minority mode waits in the warp's queue for that mode (its links' ids only)
-// while the majority finishes, and a queue that holds 32 links is run as one full round of
-// a single mode: its links are oriented again (the same inputs give the same pose and
-// mode) and finished.  What is left in the queues at the end runs in one last round per
-// mode.  Every link still writes only its own state and its two direction slots, so the
-// order changes no result.
-constexpr int kLinkDefer = 48;   // a queue holds at most 31 + 16 links between rounds
+// whatever its active lanes).  While many links change mode (a fresh batch's first tens of
+// steps: more than 1 in 256 links did in the previous step) and every warp has many rounds
+// to fill its queues with (at least 256 links per resident warp), each round first orients
+// the 32 links and decides their modes; the minority mode waits in
+// the warp's queue for that mode (its links' ids only) while the majority finishes, and a
+// queue that holds 32 links is run as one full round of a single mode: its links are
+// oriented again (the same inputs give the same pose and mode) and finished.  What is
+// left in the queues at the end runs in one last round per mode.  When few links change
+// mode, or a warp has few rounds, the queues would rarely fill and the last rounds would
+// run nearly empty, so every link is finished in its own round.  Every link still writes only its own state and its
+// two direction slots, so the order changes no result.  tickets[5] counts this launch's
+// mode changes; k_voxels moves the count to tickets[6] for the next step's decision.
+constexpr int kLinkDefer = 48;          // a queue holds at most 31 + 16 links between rounds
+constexpr int kDeferPerWarp = 256;      // queues only with at least this many links per resident warp
+constexpr int kDeferRate = 256;         // queues while more than 1 link in kDeferRate changed mode
 __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(const Sim* __restrict__ sims, Ctl* ctl, const int2* __restrict__ perm,
                                                                      const int* __restrict__ total, int cap, int n_slots, int* tickets,
                                                                      int claim) {
@@ -514,6 +523,9 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(
     int2* q0 = s_defer[threadIdx.x >> 5][0];
     int2* q1 = s_defer[threadIdx.x >> 5][1];
     int qn0 = 0, qn1 = 0;        // links waiting in each queue (the same in every lane)
+    const bool queues = (long long)n >= (long long)kDeferPerWarp * (gridDim.x * (blockDim.x / 32)) &&
+                        (long long)tickets[6] * kDeferRate > (long long)n;
+    int switched = 0;            // mode changes seen by this warp
     int kb = 0, k1 = 0;          // the claimed chunk: next round's first link, its end
     bool more = true;            // chunks may remain
     for (;;) {
@@ -556,8 +568,9 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(
         act = act && link_orient(sims[e.x], e.y, &o);
         if (src < 0) {
             const unsigned am = __ballot_sync(0xffffffffu, act), sm = __ballot_sync(0xffffffffu, act && o.small);
+            switched += __popc(__ballot_sync(0xffffffffu, act && o.switched));
             const bool major_small = 2 * __popc(sm) >= __popc(am);
-            const bool defer = act && o.small != major_small;
+            const bool defer = queues && act && o.small != major_small;
             const unsigned dm = __ballot_sync(0xffffffffu, defer);
             if (dm) {
                 // the deferred lanes' mode is the other one: small when the majority is large
@@ -576,6 +589,7 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_LINKS_MIN_BLOCKS) k_links(
             if (div) c.diverged = 1;
         }
     }
+    if (lane == 0 && switched) atomicAdd(&tickets[5], switched);
 }
 
 // Overlap test and repelling force for one voxel pair (CVX_Collision::updateContactForce,
@@ -1434,7 +1448,11 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxel
     // the voxels of the running simulations, grouped by key like the links (k_bin_*); warps
     // take chunks of `claim` voxels (a multiple of 32), so no warp waits at a block barrier
     // for a costlier one
-    if (blockIdx.x == 0 && threadIdx.x == 0) tickets[0] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        tickets[0] = 0;
+        tickets[6] = tickets[5];   // the last k_links launch's mode changes, for the next one
+        tickets[5] = 0;
+    }
     const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
     for (;;) {
