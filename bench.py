@@ -88,6 +88,8 @@ FP64_COUNTS = {
                  traffic_per_link=(420665344 + 421070336 + 421153792) / 3 / 1480000,
                  source="ncu, 100x100x50 slab, mean of steps 201, 1001, 1901"),
 }
+# steps a whole run of each workload takes (the batch: 0.5 s simulated at its creatures' time steps)
+RUN_STEPS = {"batch": "35,000-56,000", "collide": "20,000", "slab": "2,000", "plain": "10,000"}
 FP64_INSTR_PER_LINK = FP64_COUNTS["batch"]["per_link"]
 FP64_INSTR_PER_VOXEL = FP64_COUNTS["batch"]["per_voxel"]
 LINK_TRAFFIC_PER_LINK = FP64_COUNTS["batch"]["traffic_per_link"]
@@ -580,7 +582,7 @@ def run_ours(args):
                        kernel_build=args.precision, tuning=tuning,
                        tuning_source="vx3_autotune on the live batch" if not (args.tuning or args.no_autotune) else "set",
                        timed_window=f"steps {first}-{first + args.steps - 1} of the run (after {args.settle_steps} "
-                                    "settling steps; the configuration runs 35,000-56,000)",
+                                    f"settling steps; the configuration runs {RUN_STEPS.get(args.workload, 'more')})",
                        fresh_batch=fresh,
                        l2="device state larger than L2; no flush needed", parallelism=f"replicas x{ws} (no collective)"),
         "e2e": e2e,

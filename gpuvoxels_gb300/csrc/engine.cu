@@ -114,16 +114,27 @@ __global__ void k_scatter_regions(const char* __restrict__ stage, const RegionCo
 }
 
 // The work-list fields of a new batch's control blocks in one launch: per batch entry the
-// number and the first index of the simulation's voxel items, and the completion counters
-// cleared (one small copy per simulation took about a millisecond for 512 of them).
-__global__ void k_set_batch_items(dev::Ctl* ctl, const int* __restrict__ slots, const int2* __restrict__ items, int n) {
+// number and the first index of the simulation's voxel items and the first index and number
+// of its contact items, and the completion counters cleared (one small copy per simulation
+// took about a millisecond for 512 of them).
+__global__ void k_set_batch_items(dev::Ctl* ctl, const int* __restrict__ slots, const int4* __restrict__ items, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     dev::Ctl& c = ctl[slots[i]];
     c.n_vox_items = items[i].x;
     c.item_begin = items[i].y;
+    c.c_item_begin = items[i].z;
+    c.c_item_count = items[i].w;
     c.done_items = 0;
     c.sig_done_items = 0;
+}
+
+// Every contact item listed for the first step of a new batch's watch-list passes (the
+// items each simulation's previous step would have listed are not known).
+__global__ void k_list_all_items(int* stale_items, int n, int* tickets) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) stale_items[i] = i;
+    if (i == 0) tickets[7] = n;
 }
 
 // Host tables of the C library's powf(x, -nu) for every float x in [0.5, 2), one per Poisson
@@ -284,13 +295,17 @@ public:
     // device copies, shared with the other contexts on this device)
     std::map<uint32_t, const float*> dev_pow_;
     dev::Item* d_items_ = nullptr;
+    int* d_stale_items_ = nullptr;   // contact items whose simulations regenerate their watch lists next
     int cap_items_ = 0;
     double* d_com4_ = nullptr;
     // tuning
     int block_links_ = 256, block_voxels_ = 256, items_links_ = 1024, items_voxels_ = 1024, graph_steps_ = 64;
     int claim_links_ = 32, claim_voxels_ = 32;   // elements a warp claims from the step queues at a time
-    // link binning: regrouped every bin_every_ steps (the first step after a batch change always)
-    int bin_every_ = 1, bin_phase_ = 0;
+    // link binning: regrouped every bin_every_ steps (the first step after a batch change
+    // always); every second step measured 1.9% faster than every step on the 512-creature
+    // batch once it has settled (keys change slowly: 0.1% of links a step) and 1% faster on
+    // a fresh one, every fourth no faster than every second
+    int bin_every_ = 2, bin_phase_ = 0;
     bool bins_dirty_ = true;
     // Small batches (serving at low load) are bound by launch latency, not by the FP64 pipe:
     // their links and voxels are regrouped only when the batch changes and at the start of
@@ -325,10 +340,10 @@ public:
     int2* d_vox_perm_ = nullptr;
     size_t cap_vbins_ = 0, cap_vperm_ = 0;
     int* d_batch_slots_ = nullptr;
-    int2* d_batch_items_ = nullptr;          // per batch entry: voxel items, first voxel item
+    int4* d_batch_items_ = nullptr;          // per batch entry: voxel items, first voxel item, first contact item, contact items
     int n_batch_ = 0, cap_batch_ = 0;
     std::vector<int> batch_slots_host_;
-    std::vector<int2> batch_items_host_;
+    std::vector<int4> batch_items_host_;
     int n_attach_ = 0, cap_attach_ = 0;     // simulations with VX3 attachment in the batch
     int64_t graph_launches_ = 0;            // kernels one replay of the captured graph launches
     int* d_attach_slots_ = nullptr;
@@ -372,7 +387,7 @@ public:
         }
         cudaFree(d_gather_);
         cudaFree(d_stage_);
-        cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_com4_);
+        cudaFree(d_sims_); cudaFree(d_ctl_); cudaFree(d_tickets_); cudaFree(d_items_); cudaFree(d_stale_items_); cudaFree(d_com4_);
         cudaFree(d_spill_p_); cudaFree(d_spill_f_);
         cudaFree(d_attach_slots_);
         cudaFree(d_link_hist_); cudaFree(d_link_base_); cudaFree(d_link_total_); cudaFree(d_link_perm_);
@@ -438,8 +453,9 @@ public:
         CK(cudaMemset(d_vox_total_, 0, sizeof(int)));
         CK(cudaMalloc(&d_vox_perm_, sizeof(int2) * cap_vperm_));
         CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
+        CK(cudaMalloc(&d_stale_items_, sizeof(int) * cap_items_));
         CK(cudaMalloc(&d_batch_slots_, sizeof(int) * cap_batch_));
-        CK(cudaMalloc(&d_batch_items_, sizeof(int2) * cap_batch_));
+        CK(cudaMalloc(&d_batch_items_, sizeof(int4) * cap_batch_));
         CK(cudaMalloc(&d_attach_slots_, sizeof(int) * cap_attach_));
         return 0;
     }
@@ -1348,7 +1364,9 @@ public:
             cap_perm_ = std::max(std::max<size_t>(1, links_total), 2 * cap_perm_);
             CK(cudaMalloc(&d_link_perm_, sizeof(int2) * cap_perm_));
         }
-        for (int s : slots) {
+        std::vector<std::pair<int, int>> contact_items(slots.size(), std::make_pair(0, 0));   // per batch entry: first, count
+        for (size_t k = 0; k < slots.size(); k++) {
+            const int s = slots[k];
             SimRec* r = slot_owner_[s];
             if (r->w.desc.enable_signals) any_signals_ = true;
             if (attaches(r->w.desc)) attach_slots.push_back(s);
@@ -1356,8 +1374,10 @@ public:
             if (!r->w.desc.collisions || ns == 0) continue;
             any_collide_ = true;
             if (watches(r->w.desc)) any_watch_ = true;
-            const int chunk = 128;
+            const int chunk = 128;   // at most 128 surface voxels an item (the watch passes' work units rely on it)
+            const int first = (int)items.size() - n_link_items_;
             for (int b = 0; b < ns; b += chunk) items.push_back({s, b, std::min(ns, b + chunk), 0});
+            contact_items[k] = std::make_pair(first, (int)items.size() - n_link_items_ - first);
         }
         n_contact_items_ = (int)items.size() - n_link_items_;
         std::vector<std::pair<int, int>> ctl_items;   // slot -> (begin, count)
@@ -1399,22 +1419,26 @@ public:
                 d_batch_items_ = nullptr;
                 cap_batch_ = std::max(n_batch_, 2 * cap_batch_);
                 CK(cudaMalloc(&d_batch_slots_, sizeof(int) * cap_batch_));
-                CK(cudaMalloc(&d_batch_items_, sizeof(int2) * cap_batch_));
+                CK(cudaMalloc(&d_batch_items_, sizeof(int4) * cap_batch_));
             }
             batch_slots_host_ = slots;   // kept alive for the asynchronous copies
             batch_items_host_.resize(slots.size());
-            for (size_t i = 0; i < slots.size(); i++) batch_items_host_[i] = make_int2(ctl_items[i].second, ctl_items[i].first);
+            for (size_t i = 0; i < slots.size(); i++)
+                batch_items_host_[i] = make_int4(ctl_items[i].second, ctl_items[i].first, contact_items[i].first, contact_items[i].second);
             if (n_batch_) {
                 CK(copy_async(d_batch_slots_, batch_slots_host_.data(), sizeof(int) * n_batch_, cudaMemcpyHostToDevice, stream_));
-                CK(copy_async(d_batch_items_, batch_items_host_.data(), sizeof(int2) * n_batch_, cudaMemcpyHostToDevice, stream_));
+                CK(copy_async(d_batch_items_, batch_items_host_.data(), sizeof(int4) * n_batch_, cudaMemcpyHostToDevice, stream_));
                 k_set_batch_items<<<(n_batch_ + 255) / 256, 256, 0, stream_>>>(d_ctl_, d_batch_slots_, d_batch_items_, n_batch_);
                 CK(cudaGetLastError());
             }
         }
         if ((int)items.size() > cap_items_) {
             cudaFree(d_items_);
+            cudaFree(d_stale_items_);
+            d_stale_items_ = nullptr;
             cap_items_ = std::max((int)items.size(), 2 * cap_items_);
             CK(cudaMalloc(&d_items_, sizeof(dev::Item) * cap_items_));
+            CK(cudaMalloc(&d_stale_items_, sizeof(int) * cap_items_));
         }
         if (!items.empty()) CK(copy_async(d_items_, items.data(), sizeof(dev::Item) * items.size(), cudaMemcpyHostToDevice, stream_));
         n_attach_ = (int)attach_slots.size();
@@ -1428,6 +1452,10 @@ public:
             CK(copy_async(d_attach_slots_, attach_slots_host_.data(), sizeof(int) * n_attach_, cudaMemcpyHostToDevice, stream_));
         }
         CK(cudaMemsetAsync(d_tickets_, 0, kTickets * sizeof(int), stream_));
+        if (any_watch_ && n_contact_items_ > 0) {
+            k_list_all_items<<<(n_contact_items_ + 255) / 256, 256, 0, stream_>>>(d_stale_items_, n_contact_items_, d_tickets_);
+            CK(cudaGetLastError());
+        }
         return 0;
     }
 
@@ -1468,7 +1496,9 @@ public:
         ks_.links(grid_chunks(batch_links_, bl, 0), bl, st, d_sims_, d_ctl_, d_link_perm_, d_link_total_,
                   (int)cap_perm_, cap_slots_, d_tickets_, claim_links_);
         if (prof) cudaEventRecord(evk_[1], st);
-        if (any_watch_) ks_.watch(grid_for(n_contact_items_, 128), st, d_sims_, d_ctl_, ci, n_contact_items_, d_batch_slots_, n_batch_);
+        // the watch-list passes: a persistent grid of 256-thread blocks over the listed items' work units
+        if (any_watch_) ks_.watch(4 * sm_count_, st, d_sims_, d_ctl_, ci, n_contact_items_, d_stale_items_, d_tickets_, d_batch_slots_,
+                                  n_batch_);
         if (any_collide_) ks_.contacts(grid_for(n_contact_items_, 128), 128, st, d_sims_, d_ctl_, ci, n_contact_items_, d_tickets_);
         if (n_attach_) ks_.attach(st, d_sims_, d_ctl_, d_attach_slots_, n_attach_);
         if (prof) cudaEventRecord(evk_[2], st);
@@ -1476,7 +1506,7 @@ public:
         ks_.voxels(grid_chunks(batch_voxels_, bv, 1), bv, st, d_sims_, d_ctl_, d_vox_perm_, d_vox_total_,
                    (int)cap_vperm_, cap_slots_, d_tickets_, claim_voxels_);
         if (prof) cudaEventRecord(evk_[4], st);
-        ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_);
+        ks_.sim_end(st, d_sims_, d_ctl_, d_batch_slots_, n_batch_, d_tickets_, d_stale_items_);
         if (any_signals_) ks_.signals(grid_for(n_vox_items_, 256), 256, st, d_sims_, d_ctl_, vi, n_vox_items_, d_tickets_);
         return launched;
     }
@@ -1503,6 +1533,13 @@ public:
         k_ctl_run<<<(unsigned)((n + 255) / 256), 256, 0, stream_>>>(d_ctl_, (const int*)d_gather_, (const int64_t*)(d_gather_ + o_tg),
                                                                    (int)n, no_stop);
         CK(cudaGetLastError());
+        // a simulation that stopped at the end of its last step (target reached) was not listed
+        // for its watch-list regeneration by k_sim_end: list every contact item again (a batch
+        // about to change is listed afresh by build_items)
+        if (any_watch_ && n_contact_items_ > 0 && n_contact_items_ <= cap_items_) {
+            k_list_all_items<<<(n_contact_items_ + 255) / 256, 256, 0, stream_>>>(d_stale_items_, n_contact_items_, d_tickets_);
+            CK(cudaGetLastError());
+        }
         return 0;
     }
 

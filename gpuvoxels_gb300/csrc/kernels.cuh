@@ -828,11 +828,12 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
 // each side enough to cover the radius), in three passes (count, offsets, fill) that run
 // only in the steps that regenerate.
 
-// Calls fn(q) for every partner q of surface voxel v on its regenerated watch list, in no
-// particular order; the exact test is the reference's: squared centre distance (double)
-// not above the squared watch radius (float).
+// Calls fn(q) for every partner q of surface voxel v on its regenerated watch list found in
+// the hash cells c0, c0 + cstep, ... of the (2R+1)^3 cells around v (the lanes of a warp
+// share a voxel's cells), in no particular order; the exact test is the reference's:
+// squared centre distance (double) not above the squared watch radius (float).
 template <typename Fn>
-__device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int parity, Fn fn) {
+__device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int parity, int c0, int cstep, Fn fn) {
     const float4 pv = S.cpos[v];
     const float ic = S.inv_cell;
     const int cx = cell_of(pv.x, ic), cy = cell_of(pv.y, ic), cz = cell_of(pv.z, ic);
@@ -841,11 +842,10 @@ __device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int 
     const int* head = S.hash_head + (size_t)parity * S.hash_size;
     const double wr2 = (double)S.watch_r2;
     const float lim = sqrtf(S.watch_r2) * 1.02f + 2.4e-7f * (fabsf(pv.x) + fabsf(pv.y) + fabsf(pv.z)) * 2.0f;
-    const int R = S.wcells;
+    const int R = S.wcells, side = 2 * R + 1, ncell = side * side * side;
     const double ax = S.px[v], ay = S.py[v], az = S.pz[v];
-    for (int dz = -R; dz <= R; dz++)
-        for (int dy = -R; dy <= R; dy++)
-            for (int dx = -R; dx <= R; dx++) {
+    for (int cc = c0; cc < ncell; cc += cstep) {
+                const int dx = cc % side - R, dy = (cc / side) % side - R, dz = cc / (side * side) - R;
                 const int tx = cx + dx, ty = cy + dy, tz = cz + dz;
                 int q = head[cell_hash(tx, ty, tz, S.hash_size - 1)];
                 int guard = 0;
@@ -869,26 +869,47 @@ __device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int 
                     }
                     q = nq;
                 }
-            }
+    }
+}
+
+// The watch-list passes 1 and 3 run over the contact items of the simulations that
+// regenerate this step (listed by the previous step's k_sim_end, or every item after the
+// batch changed), in units of 4 surface voxels, one warp per voxel with its lanes splitting
+// the hash cells (a voxel visits up to 343 cells): a regeneration of one creature spreads
+// over the whole GPU, and a step without one costs a launch.
+constexpr int kWatchUnit = 4;                 // surface voxels per work unit
+constexpr int kWatchUnitsPerItem = 128 / kWatchUnit;   // contact items hold at most 128 surface voxels
+template <typename Fn>
+__device__ __forceinline__ void for_each_watch_voxel(const Sim* sims, const Ctl* ctl, const Item* items, int n_items,
+                                                     const int* stale_items, const int* tickets, bool need_ok, Fn fn) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    const int n = min(tickets[7], n_items);
+    for (int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n * kWatchUnitsPerItem; u += warps) {
+        const int it = stale_items[u / kWatchUnitsPerItem];
+        if ((unsigned)it >= (unsigned)n_items) continue;
+        const Item w = items[it];
+        const Ctl& c = ctl[w.sim];
+        const Sim& S = sims[w.sim];
+        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale || (need_ok && !c.watch_ok)) continue;
+        const int b = w.begin + (u % kWatchUnitsPerItem) * kWatchUnit, e = min(w.end, b + kWatchUnit);
+        for (int i = b; i < e; i++) fn(S, c, i, lane);
+    }
 }
 
 // Pass 1: every surface voxel of a regenerating simulation counts its partners (into
 // woff[si + 1]) and records its position as the regeneration's (lastColWatchPosition).
-__global__ void __launch_bounds__(128) k_watch_count(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                     int n_items) {
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-        const Item w = items[it];
-        const Ctl& c = ctl[w.sim];
-        const Sim& S = sims[w.sim];
-        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale) continue;
-        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) {
-            const int v = S.surf[i];
-            S.watch[v] = make_float4(d2f(S.px[v]), d2f(S.py[v]), d2f(S.pz[v]), 0.0f);
-            int n = 0;
-            for_each_watch_partner(S, v, c.hash_parity, [&](int) { n++; });
-            S.woff[i + 1] = n;
-        }
-    }
+__global__ void __launch_bounds__(256) k_watch_count(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                     int n_items, const int* __restrict__ stale_items, const int* tickets) {
+    for_each_watch_voxel(sims, ctl, items, n_items, stale_items, tickets, false, [&](const Sim& S, const Ctl& c, int i, int lane) {
+        const int v = S.surf[i];
+        if (lane == 0) S.watch[v] = make_float4(d2f(S.px[v]), d2f(S.py[v]), d2f(S.pz[v]), 0.0f);
+        int n = 0;
+        for_each_watch_partner(S, v, c.hash_parity, lane, 32, [&](int) { n++; });
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+        if (lane == 0) S.woff[i + 1] = n;
+    });
 }
 
 // Pass 2, one block per simulation of the batch: the counts become offsets (an exclusive
@@ -929,28 +950,53 @@ __global__ void __launch_bounds__(1024) k_watch_scan(const Sim* __restrict__ sim
     }
 }
 
-// Pass 3: every surface voxel writes its partners into its run and sorts them.
-__global__ void __launch_bounds__(128) k_watch_fill(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                    int n_items) {
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
-        const Item w = items[it];
-        const Ctl& c = ctl[w.sim];
-        const Sim& S = sims[w.sim];
-        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale || !c.watch_ok) continue;
-        for (int i = w.begin + threadIdx.x; i < w.end; i += blockDim.x) {
-            const int v = S.surf[i];
-            int* out = S.wlist + S.woff[i];
-            const int n = S.woff[i + 1] - S.woff[i];
-            int k = 0;
-            for_each_watch_partner(S, v, c.hash_parity, [&](int q) { if (k < n) out[k++] = q; });
-            for (int a = 1; a < k; a++) {   // insertion sort: the reference's increasing partner order
-                const int q = out[a];
-                int j = a;
-                while (j > 0 && out[j - 1] > q) { out[j] = out[j - 1]; j--; }
-                out[j] = q;
+// Pass 3: every surface voxel writes its partners into its run (one warp per voxel, as
+// pass 1) and sorts them into the reference's increasing partner order: each lane ranks
+// up to four entries against the whole run (partners are distinct, so the ranks are a
+// permutation); a run longer than 128 is sorted by one lane.
+__global__ void __launch_bounds__(256) k_watch_fill(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+                                                    int n_items, const int* __restrict__ stale_items, const int* tickets) {
+    __shared__ int s_found[8];
+    const int wid = threadIdx.x >> 5;
+    for_each_watch_voxel(sims, ctl, items, n_items, stale_items, tickets, true, [&](const Sim& S, const Ctl& c, int i, int lane) {
+        const int v = S.surf[i];
+        const int w0 = S.woff[i];
+        int n = S.woff[i + 1] - w0;
+        if (w0 < 0 || n < 0 || w0 + n > S.wcap) n = 0;   // never: the offsets lie within the lists (k_watch_scan)
+        int* out = S.wlist + (n > 0 ? w0 : 0);
+        if (lane == 0) s_found[wid] = 0;
+        __syncwarp();
+        for_each_watch_partner(S, v, c.hash_parity, lane, 32, [&](int q) {
+            const int k = atomicAdd(&s_found[wid], 1);
+            if (k < n) out[k] = q;
+        });
+        __syncwarp();
+        const int k = min(s_found[wid], n);
+        __syncwarp();
+        if (k > 128) {
+            if (lane == 0)
+                for (int a = 1; a < k; a++) {
+                    const int q = out[a];
+                    int j = a;
+                    while (j > 0 && out[j - 1] > q) { out[j] = out[j - 1]; j--; }
+                    out[j] = q;
+                }
+        } else if (k > 1) {
+            int e[4], r[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) { e[t] = lane + 32 * t < k ? out[lane + 32 * t] : 0; r[t] = 0; }
+            for (int j = 0; j < k; j++) {
+                const int x = out[j];
+#pragma unroll
+                for (int t = 0; t < 4; t++) r[t] += x < e[t] ? 1 : 0;
             }
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                if (lane + 32 * t < k) out[r[t]] = e[t];
         }
-    }
+        __syncwarp();
+    });
 }
 
 // The contact pass of surface voxel v (surface index si) from its watch list: the list is in
@@ -961,13 +1007,18 @@ __device__ void voxel_contacts_watch(const Sim& S, int v, int si, Ctl& c) {
     const int cap = min(max(S.contact_inline, 1), kContactInline);
     float* out = S.cforce + (size_t)v * 3 * kContactInline;
     const float4 pv = S.cpos[v];
-    const int b = S.woff[si], e = S.woff[si + 1];
+    int b = S.woff[si], e = S.woff[si + 1];
+    if (b < 0 || e > S.wcap || b > e) {   // never: a run outside the lists is read as empty
+        atomicOr(&c.error, 4);
+        b = e = 0;
+    }
     const bool targets = S.flags & SF_TARGETS;
     const bool tv = targets && (S.vm[__ldg(S.vmat + v)].vx3 & VM_TARGET);
     int n = 0, pairs = 0;
     bool hit = false;
     for (int k = b; k < e; k++) {
         const int q = S.wlist[k];
+        if ((unsigned)q >= (unsigned)S.nv) { atomicOr(&c.error, 4); continue; }   // never: not a voxel
         if (!maybe_touching(pv, S.cpos[q], S.env_radius)) continue;
         float f3[3];
         if (!pair_force(S, v < q ? v : q, v < q ? q : v, f3)) continue;
@@ -988,6 +1039,7 @@ __device__ void voxel_contacts_watch(const Sim& S, int v, int si, Ctl& c) {
         int j = 0;
         for (int k = b; k < e && j < n; k++) {
             const int q = S.wlist[k];
+            if ((unsigned)q >= (unsigned)S.nv) continue;
             if (!maybe_touching(pv, S.cpos[q], S.env_radius)) continue;
             float f3[3];
             if (!pair_force(S, v < q ? v : q, v < q ? q : v, f3)) continue;
@@ -1452,6 +1504,7 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxel
         tickets[0] = 0;
         tickets[6] = tickets[5];   // the last k_links launch's mode changes, for the next one
         tickets[5] = 0;
+        tickets[7] = 0;            // this step's watch-list passes are done: k_sim_end lists the next
     }
     const int n = min(*total, cap);
     const int lane = threadIdx.x & 31;
@@ -1481,8 +1534,10 @@ __global__ void __launch_bounds__(GVX_STEP_BLOCK, GVX_VOXELS_MIN_BLOCKS) k_voxel
 
 // The end of a step for each simulation of the batch, one block each: on cycle steps the
 // centre of mass of the measured voxels (the fixed-order sum of k_com), then sim_control.
-__global__ void __launch_bounds__(256) k_sim_end(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
+__global__ void __launch_bounds__(256) k_sim_end(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n, int* tickets,
+                                                 int* stale_items) {
     __shared__ double red[256];
+    __shared__ int s_base;
     if ((int)blockIdx.x >= n) return;
     const int sim = slots[blockIdx.x];
     Ctl& c = ctl[sim];
@@ -1502,7 +1557,14 @@ __global__ void __launch_bounds__(256) k_sim_end(const Sim* __restrict__ sims, C
         }
         for (int k = 0; k < 4; k++) s4[k] = block_sum(a[k], red);
     }
-    if (threadIdx.x == 0) sim_control(S, c, div, t_next, stepno, com_step, S.flags, S.nv, s4);
+    if (threadIdx.x == 0) {
+        sim_control(S, c, div, t_next, stepno, com_step, S.flags, S.nv, s4);
+        // the next step's watch-list passes go over the items of the simulations that regenerate
+        s_base = (c.status == 1 && (S.flags & SF_WATCH) && c.col_stale && c.c_item_count > 0) ? atomicAdd(&tickets[7], c.c_item_count) : -1;
+    }
+    __syncthreads();
+    if (s_base >= 0)
+        for (int k = threadIdx.x; k < c.c_item_count; k += blockDim.x) stale_items[s_base + k] = c.c_item_begin + k;
 }
 
 // VX3 attachment (handle_collision_attachment, VX3_VoxelyzeKernel.cu:729-827) for one
@@ -1774,17 +1836,18 @@ inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, con
     k_links<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk, claim);
 }
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
-inline void l_watch(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n_items, const int* slots, int n_sims) {
-    k_watch_count<<<g, 128, 0, s>>>(sims, ctl, it, n_items);
+inline void l_watch(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n_items, const int* stale, const int* tk,
+                    const int* slots, int n_sims) {
+    k_watch_count<<<g, 256, 0, s>>>(sims, ctl, it, n_items, stale, tk);
     if (n_sims > 0) k_watch_scan<<<n_sims, 1024, 0, s>>>(sims, ctl, slots, n_sims);
-    k_watch_fill<<<g, 128, 0, s>>>(sims, ctl, it, n_items);
+    k_watch_fill<<<g, 256, 0, s>>>(sims, ctl, it, n_items, stale, tk);
 }
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
                      int* tk, int claim) {
     k_voxels<<<g, b, 0, s>>>(sims, ctl, perm, total, cap, n_slots, tk, claim);
 }
-inline void l_sim_end(cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n) {
-    if (n > 0) k_sim_end<<<n, 256, 0, s>>>(sims, ctl, slots, n);
+inline void l_sim_end(cudaStream_t s, const Sim* sims, Ctl* ctl, const int* slots, int n, int* tk, int* stale) {
+    if (n > 0) k_sim_end<<<n, 256, 0, s>>>(sims, ctl, slots, n, tk, stale);
 }
 inline void l_signals(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) {
     k_signals<<<g, b, 0, s>>>(sims, ctl, it, n, tk);

@@ -19,8 +19,10 @@ struct KernelSet {
     void (*contacts)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
     void (*voxels)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int2* perm, const int* total, int cap,
                    int n_slots, int* tickets, int claim);
-    // the end of the step for n simulations (slot list): centre-of-mass sample, time, stop
-    void (*sim_end)(cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n);
+    // the end of the step for n simulations (slot list): centre-of-mass sample, time, stop;
+    // simulations whose watch lists go stale append their contact items to stale_items
+    // (count in tickets[7])
+    void (*sim_end)(cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const int* slots, int n, int* tickets, int* stale_items);
     // VX3 signals relayed between neighbours (after voxels, over the voxel items)
     void (*signals)(int grid, int block, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n, int* tickets);
     // VX3 attachment: new links for this step's candidate pairs of n simulations (device slot list)
@@ -37,10 +39,11 @@ struct KernelSet {
     // resident blocks per SM of k_links (0) or k_voxels (1) at a block size
     int (*resident_blocks)(int which, int block);
     int max_block;   // largest block k_links / k_voxels are compiled for
-    // watch-list regeneration (count, offsets, fill) of the simulations that need it, over the
-    // contact items and the batch's slot list
-    void (*watch)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n_items, const int* slots,
-                  int n_sims);
+    // watch-list regeneration (count, offsets, fill) of the simulations that need it: over the
+    // contact items listed in stale_items (tickets[7] of them, at most n_items) and the batch's
+    // slot list
+    void (*watch)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n_items,
+                  const int* stale_items, const int* tickets, const int* slots, int n_sims);
 };
 
 KernelSet kernelset_exact();   // every multiply and add rounded separately (the reference's CPU rounding)

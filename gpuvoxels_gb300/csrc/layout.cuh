@@ -216,6 +216,8 @@ struct Ctl {
     int32_t col_moved;          // SF_WATCH: a surface voxel moved beyond the re-check distance this step
     int32_t watch_ok;           // SF_WATCH: the lists hold the current regeneration (else the hash search runs)
     int32_t watch_regens;       // regenerations so far
+    int32_t c_item_begin;       // the simulation's contact items in the batch's contact item list
+    int32_t c_item_count;
     double init_com[3];         // initial centre of mass (host value, reset by the secondary experiment)
     MathTree stop;
 };

@@ -92,6 +92,26 @@ def test_collision_heavy_creature_long_run(ctx):
         ctx.free(sim)
 
 
+def test_watch_lists_across_step_calls_are_bit_identical():
+    """Collision creatures stepped in many short calls (each call stops them at its target and
+    starts them again, some of them right before a watch-list regeneration) end exactly where
+    one long call takes them."""
+    cs = synth.config2_batch(3, seed=31)
+    out = []
+    for calls in ([600], [37] * 16 + [8]):
+        with g.Context(0, 4 << 30) as c:
+            ids = [c.load_vxa(cr.vxa, name=f"w{i}") for i, cr in enumerate(cs)]
+            for n in calls:
+                c.step(ids, n, g.BATCHED)
+            for i in ids:
+                info = c.info(i)
+                assert info.steps == 600 and info.status == g.SIM_IDLE, (info.steps, info.status)
+            out.append([_state(c, i) for i in ids])
+    for a, b in zip(out[0], out[1]):
+        for x, y in zip(a, b):
+            assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8))
+
+
 def test_contact_slots_argument_checked(ctx):
     for bad in (0, 17):
         with pytest.raises(g.VX3Error):
