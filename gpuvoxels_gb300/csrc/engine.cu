@@ -639,7 +639,7 @@ public:
             if (watches(d)) {
                 const size_t ns = std::max(1, contact_list_size(w));
                 t.watch = L->add(16 * nv);
-                t.woff = L->add(4 * (ns + 1));
+                t.woff = L->add(4 * 2 * ns);   // per surface voxel: its run's start and length
                 t.wlist = L->add(4 * (size_t)kWatchPerVoxel * ns);
             }
         }
@@ -1041,6 +1041,8 @@ public:
         for (int k = 0; k < 3; k++) c.com[k] = c.init_com[k] = r->init_com[k];
         c.n_links = w.nl;
         c.col_stale = 1;   // the first step regenerates the watch lists (the reference's nearbyStale)
+        c.watch_ok = 1;    // until the regeneration finds the lists too small
+        c.watch_used = 0;
         r->pending_ctl = c;
     }
 

@@ -825,8 +825,8 @@ __device__ void voxel_contacts(const Sim& S, int v, int parity, Ctl& c) {
 // within the watch radius, (2 boundingRadius + watchDistance) voxel sizes, and each step
 // sums the forces of the pairs on it.  SF_WATCH simulations keep the same lists: per
 // surface voxel its partners in increasing order, found through the spatial hash (cells on
-// each side enough to cover the radius), in three passes (count, offsets, fill) that run
-// only in the steps that regenerate.
+// each side enough to cover the radius, those farther than the radius skipped), in one pass
+// that runs only in the steps that regenerate.
 
 // Calls fn(q) for every partner q of surface voxel v on its regenerated watch list found in
 // the hash cells c0, c0 + cstep, ... of the (2R+1)^3 cells around v (the lanes of a warp
@@ -844,9 +844,16 @@ __device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int 
     const float lim = sqrtf(S.watch_r2) * 1.02f + 2.4e-7f * (fabsf(pv.x) + fabsf(pv.y) + fabsf(pv.z)) * 2.0f;
     const int R = S.wcells, side = 2 * R + 1, ncell = side * side * side;
     const double ax = S.px[v], ay = S.py[v], az = S.pz[v];
+    // a cell whose box lies farther than lim from v holds no partner: its voxels' float
+    // positions have that cell's index, so they lie in the box up to rounding (the box is
+    // taken a thousandth of a cell, and a few ulps of the coordinates, larger on each side)
+    const float cs = 1.0f / ic, pad = 1e-3f * cs + 4.8e-7f * (fabsf(pv.x) + fabsf(pv.y) + fabsf(pv.z));
+    auto gap = [&](int t, float p) { return fmaxf(0.0f, fmaxf(t * cs - pad - p, p - (t + 1) * cs - pad)); };
     for (int cc = c0; cc < ncell; cc += cstep) {
                 const int dx = cc % side - R, dy = (cc / side) % side - R, dz = cc / (side * side) - R;
                 const int tx = cx + dx, ty = cy + dy, tz = cz + dz;
+                const float gx = gap(tx, pv.x), gy = gap(ty, pv.y), gz = gap(tz, pv.z);
+                if (gx * gx + gy * gy + gz * gz > lim * lim) continue;
                 int q = head[cell_hash(tx, ty, tz, S.hash_size - 1)];
                 int guard = 0;
                 while (q >= 0 && guard++ < nv) {
@@ -872,16 +879,16 @@ __device__ __forceinline__ void for_each_watch_partner(const Sim& S, int v, int 
     }
 }
 
-// The watch-list passes 1 and 3 run over the contact items of the simulations that
-// regenerate this step (listed by the previous step's k_sim_end, or every item after the
-// batch changed), in units of 4 surface voxels, one warp per voxel with its lanes splitting
-// the hash cells (a voxel visits up to 343 cells): a regeneration of one creature spreads
-// over the whole GPU, and a step without one costs a launch.
+// The watch-list pass runs over the contact items of the simulations that regenerate this
+// step (listed by the previous step's k_sim_end, or every item after the batch changed or
+// simulations were restarted), in units of 4 surface voxels, one warp per voxel with its
+// lanes splitting the hash cells: a regeneration of one creature spreads over the whole GPU,
+// and a step without one costs a launch.
 constexpr int kWatchUnit = 4;                 // surface voxels per work unit
 constexpr int kWatchUnitsPerItem = 128 / kWatchUnit;   // contact items hold at most 128 surface voxels
 template <typename Fn>
-__device__ __forceinline__ void for_each_watch_voxel(const Sim* sims, const Ctl* ctl, const Item* items, int n_items,
-                                                     const int* stale_items, const int* tickets, bool need_ok, Fn fn) {
+__device__ __forceinline__ void for_each_watch_voxel(const Sim* sims, Ctl* ctl, const Item* items, int n_items,
+                                                     const int* stale_items, const int* tickets, Fn fn) {
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (blockDim.x >> 5);
     const int n = min(tickets[7], n_items);
@@ -889,111 +896,60 @@ __device__ __forceinline__ void for_each_watch_voxel(const Sim* sims, const Ctl*
         const int it = stale_items[u / kWatchUnitsPerItem];
         if ((unsigned)it >= (unsigned)n_items) continue;
         const Item w = items[it];
-        const Ctl& c = ctl[w.sim];
+        Ctl& c = ctl[w.sim];
         const Sim& S = sims[w.sim];
-        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale || (need_ok && !c.watch_ok)) continue;
+        if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale) continue;
         const int b = w.begin + (u % kWatchUnitsPerItem) * kWatchUnit, e = min(w.end, b + kWatchUnit);
         for (int i = b; i < e; i++) fn(S, c, i, lane);
     }
 }
 
-// Pass 1: every surface voxel of a regenerating simulation counts its partners (into
-// woff[si + 1]) and records its position as the regeneration's (lastColWatchPosition).
-__global__ void __launch_bounds__(256) k_watch_count(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
+// One pass: every surface voxel of a regenerating simulation finds its partners (one warp per
+// voxel, its lanes splitting the hash cells) into a per-warp buffer, takes a run of the
+// simulation's list for them (one atomic on the simulation's count) and writes them in the
+// reference's increasing partner order (each lane ranks up to four entries against the
+// buffer: partners are distinct, so the ranks are a permutation); it records its position
+// as the regeneration's (lastColWatchPosition).  More partners than the buffer or the list
+// holds leave the simulation on the per-step hash search until the next regeneration.
+constexpr int kWatchBuf = 128;   // partners one surface voxel may have in a list
+__global__ void __launch_bounds__(256) k_watch_build(const Sim* __restrict__ sims, Ctl* ctl, const Item* __restrict__ items,
                                                      int n_items, const int* __restrict__ stale_items, const int* tickets) {
-    for_each_watch_voxel(sims, ctl, items, n_items, stale_items, tickets, false, [&](const Sim& S, const Ctl& c, int i, int lane) {
-        const int v = S.surf[i];
-        if (lane == 0) S.watch[v] = make_float4(d2f(S.px[v]), d2f(S.py[v]), d2f(S.pz[v]), 0.0f);
-        int n = 0;
-        for_each_watch_partner(S, v, c.hash_parity, lane, 32, [&](int) { n++; });
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-        if (lane == 0) S.woff[i + 1] = n;
-    });
-}
-
-// Pass 2, one block per simulation of the batch: the counts become offsets (an exclusive
-// scan over the surface voxels); a regeneration that exceeds the lists' capacity leaves the
-// simulation on the hash search until the next one.
-__global__ void __launch_bounds__(1024) k_watch_scan(const Sim* __restrict__ sims, Ctl* ctl, const int* __restrict__ slots, int n) {
-    __shared__ int s_sum[1024];
-    if ((int)blockIdx.x >= n) return;
-    const int sim = slots[blockIdx.x];
-    Ctl& c = ctl[sim];
-    const Sim& S = sims[sim];
-    if (c.status != 1 || c.diverged || !(S.flags & SF_WATCH) || !c.col_stale) return;
-    const int ns = S.nsurf;
-    const int per = (ns + blockDim.x - 1) / blockDim.x;
-    const int b0 = min(ns, (int)threadIdx.x * per), b1 = min(ns, b0 + per);
-    int sum = 0;
-    for (int i = b0; i < b1; i++) sum += S.woff[i + 1];
-    s_sum[threadIdx.x] = sum;
-    __syncthreads();
-    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
-        const int x = (int)threadIdx.x >= off ? s_sum[threadIdx.x - off] : 0;
-        __syncthreads();
-        s_sum[threadIdx.x] += x;
-        __syncthreads();
-    }
-    int run = threadIdx.x ? s_sum[threadIdx.x - 1] : 0;
-    for (int i = b0; i < b1; i++) {
-        const int cnt = S.woff[i + 1];
-        S.woff[i + 1] = run + cnt;   // the end of voxel i's run = the start of voxel i + 1's
-        run += cnt;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        S.woff[0] = 0;
-        const int total = s_sum[blockDim.x - 1];
-        c.watch_ok = total <= S.wcap ? 1 : 0;
-        c.watch_regens += 1;
-    }
-}
-
-// Pass 3: every surface voxel writes its partners into its run (one warp per voxel, as
-// pass 1) and sorts them into the reference's increasing partner order: each lane ranks
-// up to four entries against the whole run (partners are distinct, so the ranks are a
-// permutation); a run longer than 128 is sorted by one lane.
-__global__ void __launch_bounds__(256) k_watch_fill(const Sim* __restrict__ sims, const Ctl* __restrict__ ctl, const Item* __restrict__ items,
-                                                    int n_items, const int* __restrict__ stale_items, const int* tickets) {
     __shared__ int s_found[8];
+    __shared__ int s_buf[8][kWatchBuf];
     const int wid = threadIdx.x >> 5;
-    for_each_watch_voxel(sims, ctl, items, n_items, stale_items, tickets, true, [&](const Sim& S, const Ctl& c, int i, int lane) {
+    for_each_watch_voxel(sims, ctl, items, n_items, stale_items, tickets, [&](const Sim& S, Ctl& c, int i, int lane) {
         const int v = S.surf[i];
-        const int w0 = S.woff[i];
-        int n = S.woff[i + 1] - w0;
-        if (w0 < 0 || n < 0 || w0 + n > S.wcap) n = 0;   // never: the offsets lie within the lists (k_watch_scan)
-        int* out = S.wlist + (n > 0 ? w0 : 0);
-        if (lane == 0) s_found[wid] = 0;
+        if (lane == 0) {
+            S.watch[v] = make_float4(d2f(S.px[v]), d2f(S.py[v]), d2f(S.pz[v]), 0.0f);
+            s_found[wid] = 0;
+        }
         __syncwarp();
         for_each_watch_partner(S, v, c.hash_parity, lane, 32, [&](int q) {
             const int k = atomicAdd(&s_found[wid], 1);
-            if (k < n) out[k] = q;
+            if (k < kWatchBuf) s_buf[wid][k] = q;
         });
         __syncwarp();
-        const int k = min(s_found[wid], n);
-        __syncwarp();
-        if (k > 128) {
-            if (lane == 0)
-                for (int a = 1; a < k; a++) {
-                    const int q = out[a];
-                    int j = a;
-                    while (j > 0 && out[j - 1] > q) { out[j] = out[j - 1]; j--; }
-                    out[j] = q;
-                }
-        } else if (k > 1) {
+        const int k = s_found[wid];
+        int base = 0;
+        if (lane == 0) {
+            base = k <= kWatchBuf ? atomicAdd(&c.watch_used, k) : -1;
+            if (base < 0 || base > S.wcap - k) { c.watch_ok = 0; base = -1; }
+            S.woff[2 * i] = base < 0 ? 0 : base;
+            S.woff[2 * i + 1] = base < 0 ? 0 : k;
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= 0 && k > 0) {
             int e[4], r[4];
 #pragma unroll
-            for (int t = 0; t < 4; t++) { e[t] = lane + 32 * t < k ? out[lane + 32 * t] : 0; r[t] = 0; }
+            for (int t = 0; t < 4; t++) { e[t] = lane + 32 * t < k ? s_buf[wid][lane + 32 * t] : 0; r[t] = 0; }
             for (int j = 0; j < k; j++) {
-                const int x = out[j];
+                const int x = s_buf[wid][j];
 #pragma unroll
                 for (int t = 0; t < 4; t++) r[t] += x < e[t] ? 1 : 0;
             }
-            __syncwarp();
 #pragma unroll
             for (int t = 0; t < 4; t++)
-                if (lane + 32 * t < k) out[r[t]] = e[t];
+                if (lane + 32 * t < k) S.wlist[base + r[t]] = e[t];
         }
         __syncwarp();
     });
@@ -1007,7 +963,7 @@ __device__ void voxel_contacts_watch(const Sim& S, int v, int si, Ctl& c) {
     const int cap = min(max(S.contact_inline, 1), kContactInline);
     float* out = S.cforce + (size_t)v * 3 * kContactInline;
     const float4 pv = S.cpos[v];
-    int b = S.woff[si], e = S.woff[si + 1];
+    int b = S.woff[2 * si], e = b + S.woff[2 * si + 1];
     if (b < 0 || e > S.wcap || b > e) {   // never: a run outside the lists is read as empty
         atomicOr(&c.error, 4);
         b = e = 0;
@@ -1445,7 +1401,11 @@ __device__ __noinline__ void sim_control(const Sim& S, Ctl& c, bool div, double 
     c.steps = stepno;
     if (flags & SF_VARY) c.t_cycles = (c.t + c.dt) / S.temp_period;   // the next step's actuation phase
     if (flags & SF_COLLIDE) c.hash_parity ^= 1;
-    if (flags & SF_WATCH) { c.col_stale = c.col_moved; c.col_moved = 0; }
+    if (flags & SF_WATCH) {
+        c.col_stale = c.col_moved;
+        c.col_moved = 0;
+        if (c.col_stale) { c.watch_used = 0; c.watch_ok = 1; c.watch_regens += 1; }   // the next step regenerates
+    }
     if (com_step) {
         c.angle_samples++;
         for (int j = 0; j < 3; j++) { c.com_hist[0][j] = c.com_hist[1][j]; c.com_hist[1][j] = c.com[j]; }
@@ -1838,9 +1798,8 @@ inline void l_links(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, con
 inline void l_contacts(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n, int* tk) { k_contacts<<<g, b, 0, s>>>(sims, ctl, it, n, tk); }
 inline void l_watch(int g, cudaStream_t s, const Sim* sims, Ctl* ctl, const Item* it, int n_items, const int* stale, const int* tk,
                     const int* slots, int n_sims) {
-    k_watch_count<<<g, 256, 0, s>>>(sims, ctl, it, n_items, stale, tk);
-    if (n_sims > 0) k_watch_scan<<<n_sims, 1024, 0, s>>>(sims, ctl, slots, n_sims);
-    k_watch_fill<<<g, 256, 0, s>>>(sims, ctl, it, n_items, stale, tk);
+    (void)slots; (void)n_sims;
+    k_watch_build<<<g, 256, 0, s>>>(sims, ctl, it, n_items, stale, tk);
 }
 inline void l_voxels(int g, int b, cudaStream_t s, const Sim* sims, Ctl* ctl, const int2* perm, const int* total, int cap, int n_slots,
                      int* tk, int claim) {

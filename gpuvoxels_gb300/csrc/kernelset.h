@@ -39,7 +39,7 @@ struct KernelSet {
     // resident blocks per SM of k_links (0) or k_voxels (1) at a block size
     int (*resident_blocks)(int which, int block);
     int max_block;   // largest block k_links / k_voxels are compiled for
-    // watch-list regeneration (count, offsets, fill) of the simulations that need it: over the
+    // watch-list regeneration (one pass) of the simulations that need it: over the
     // contact items listed in stale_items (tickets[7] of them, at most n_items) and the batch's
     // slot list
     void (*watch)(int grid, cudaStream_t s, const dev::Sim* sims, dev::Ctl* ctl, const dev::Item* items, int n_items,

@@ -218,6 +218,8 @@ struct Ctl {
     int32_t watch_regens;       // regenerations so far
     int32_t c_item_begin;       // the simulation's contact items in the batch's contact item list
     int32_t c_item_count;
+    int32_t watch_used;         // SF_WATCH: list entries taken by this regeneration's runs
+    int32_t pad_watch;
     double init_com[3];         // initial centre of mass (host value, reset by the secondary experiment)
     MathTree stop;
 };
