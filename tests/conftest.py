@@ -11,8 +11,8 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GOLDEN_WORLDS = ["c0_seed0", "c1_poisson", "falling_blocks", "bilinear_cantilever", "large_angle", "partial_fix", "bc_regions",
-                 "single_voxel", "one_link", "ref_zoo_basic", "ref_example", "ref_signaling", "ref_memleaking", "ref_circle_push",
-                 "ref_target_only"]
+                 "single_voxel", "one_link", "collide_creature", "ref_zoo_basic", "ref_example", "ref_signaling",
+                 "ref_memleaking", "ref_circle_push", "ref_target_only"]
 
 
 def pytest_configure(config):

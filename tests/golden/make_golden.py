@@ -92,6 +92,14 @@ def worlds():
     pair = np.array([[[1, 2]]], np.int32)
     vxa = grid_world(pair, [dict(SOFT, cte=0.01), STIFF])
     w["one_link"] = dict(vxa=vxa, ext=[], snaps=[1, 400, 1500])
+    # a small creature of the collision configuration's materials (soft E=1e5 among E=1e6,
+    # contraction-only actuation, self-collision on): it folds onto itself, so its watch lists
+    # regenerate many times over the run
+    mats = [dict(E=1e5, rho=1000.0, nu=0.35, cte=0.01, mus=1.0, muk=0.5),
+            dict(E=1e6, rho=1000.0, nu=0.35, cte=0.01, mus=1.0, muk=0.5),
+            dict(E=1e6, rho=1000.0, nu=0.35, cte=0.0, mus=1.0, muk=0.5)]
+    cr = synth.random_creature(77, (12, 12, 12), 0.5, mats, collision=True, expansion=False)
+    w["collide_creature"] = dict(vxa=cr.vxa, ext=[], snaps=[1, 800, 2000])
     return w
 
 
