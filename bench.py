@@ -8,8 +8,11 @@ materials with E log-uniform in [1e5, 1e7] Pa, rho=1000, nu=0.35, one or two
 actuated at 5 Hz), gravity and floor on, no self-collision, FP64, all creatures
 packed into shared launches.  A "step" is one physics step of the whole batch.
 The batch's device state (~1 GB) is larger than L2, so no flush is needed
-between timed iterations.  The launch shape is picked by the autotuner
-(vx3_autotune) first and recorded in config.tuning.
+between timed iterations.  The first steps of the fresh batch are timed on
+their own (config.fresh_batch); after 256 more settling steps the launch shape
+is picked by the autotuner (vx3_autotune, recorded in config.tuning) and the
+line's K steps are timed (config.timed_window): the configuration's runs are
+35,000-56,000 steps long, nearly all of them in that settled regime.
 
 The same line carries, under "modes":
   plain_vs_batched  the one-simulation-per-launch form against the batched form on
